@@ -1,0 +1,390 @@
+// flint_abi.cu -- the extern "C" boundary of include/flint_gpu.h.
+//
+// A handle (flint_mech_s) replaces FLINT's module globals (the tables and
+// stoichiometry that read_idealgas_thermo / read_chemistry fill,
+// Lib_ThermoTransport.f90:8-25, Lib_Chemistry_data.f90:4-32): it owns one
+// packed, 16-byte-aligned device image of the mechanism that every kernel
+// stages into shared memory.  Several handles may coexist (FLINT allows one
+// mechanism per process).  No exception crosses the boundary: every entry
+// point returns a status and records a message for flint_last_error().
+#include <atomic>
+#include <cstdarg>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+#include <algorithm>
+
+#include "flint_host.h"
+
+namespace flint {
+
+static std::atomic<int64_t> g_launches{0};
+void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+
+static thread_local std::string g_err;
+
+static int fail(int code, const char* fmt, ...) __attribute__((format(printf, 2, 3)));
+static int fail(int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  g_err = buf;
+  return code;
+}
+
+static int cuda_fail(cudaError_t e, const char* what) {
+  return fail(FLINT_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+static int rup(int x, int m) { return (x + m - 1) / m * m; }
+
+}  // namespace flint
+
+using namespace flint;
+
+struct flint_mech_s {
+  ImageLayout L;
+  std::vector<uint8_t> himg;
+  uint8_t* dimg = nullptr;
+  unsigned int* dcounter = nullptr;
+  int device = 0;
+  // staging buffers of the *_host entry points (grow only)
+  void* dstage = nullptr;
+  size_t stage_bytes = 0;
+};
+
+namespace flint {
+
+// Pack a mechanism description into the device image (see ImageLayout).
+static int pack(const flint_mech_desc* d, ImageLayout& L, std::vector<uint8_t>& img) {
+  const int ns = d->ns, nr = d->nr;
+  if (ns < 1 || nr < 0) return fail(FLINT_ERR_ARG, "ns=%d nr=%d", ns, nr);
+  if (ns > 31) return fail(FLINT_ERR_MECH, "ns=%d: the kernels of this build support up to 31 species", ns);
+  if (!d->mw || !d->nasa7 || (nr > 0 && (!d->rtype || !d->reversible || !d->arrh || !d->rsp || !d->rnu ||
+                                         !d->rord || !d->psp || !d->pnu)))
+    return fail(FLINT_ERR_ARG, "NULL array in mechanism description");
+  for (int k = 0; k < ns; ++k)
+    if (!(d->mw[k] > 0.0)) return fail(FLINT_ERR_MECH, "species %d: molar mass %g", k, d->mw[k]);
+  // order reactions by type: elementary, three-body, Lindemann, Troe
+  std::vector<int> order(nr);
+  for (int r = 0; r < nr; ++r) order[r] = r;
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return d->rtype[a] < d->rtype[b]; });
+  int ntb = 0;
+  for (int r = 0; r < nr; ++r) {
+    int t = d->rtype[r];
+    if (t < 0 || t > 3) return fail(FLINT_ERR_MECH, "reaction %d: type %d", r, t);
+    if (t != 0) {
+      if (!d->eff) return fail(FLINT_ERR_ARG, "third-body reactions need efficiencies");
+      if (t >= 2 && (!d->arrh0 || (t == 3 && !d->troe))) return fail(FLINT_ERR_ARG, "falloff data missing");
+      ++ntb;
+    }
+    for (int s = 0; s < 3; ++s) {
+      int a = d->rsp[3 * r + s], b = d->psp[3 * r + s];
+      if (a < -1 || a >= ns || b < -1 || b >= ns) return fail(FLINT_ERR_MECH, "reaction %d: species index", r);
+      if (a >= 0 && (d->rnu[3 * r + s] < 0.0 || d->rord[3 * r + s] < 0.0))
+        return fail(FLINT_ERR_MECH, "reaction %d: negative order", r);
+    }
+  }
+  if (ntb > 255) return fail(FLINT_ERR_MECH, "more than 255 third-body/falloff reactions");
+  L = ImageLayout{};
+  L.ns = ns; L.nr = nr; L.nsp = rup(ns, 32); L.nrpad = rup(std::max(nr, 1), 32); L.ntb = std::max(ntb, 1);
+  L.r_eos = d->r_eos; L.r_thermo = d->r_thermo;
+  L.lnpref_rth = std::log(d->p_ref / d->r_thermo);
+  // CSR species -> (reaction, net nu)
+  std::vector<std::vector<std::pair<int, double>>> lists(ns);
+  for (int rr = 0; rr < nr; ++rr) {
+    int r = order[rr];
+    std::vector<double> net(ns, 0.0);
+    for (int s = 0; s < 3; ++s) {
+      if (d->rsp[3 * r + s] >= 0) net[d->rsp[3 * r + s]] -= d->rnu[3 * r + s];
+      if (d->psp[3 * r + s] >= 0) net[d->psp[3 * r + s]] += d->pnu[3 * r + s];
+    }
+    for (int k = 0; k < ns; ++k)
+      if (net[k] != 0.0) lists[k].push_back({rr, net[k]});
+  }
+  int nlist = 0;
+  for (auto& l : lists) nlist += (int)l.size();
+  L.nlist = nlist;
+  const int S = L.nsp, P = L.nrpad;
+  int off = 0;
+  auto sec = [&](int bytes) { int o = off; off = rup(off + bytes, 16); return o; };
+  L.o_mw = sec(8 * S); L.o_invmw = sec(8 * S); L.o_nasa = sec(8 * 16 * S);
+  L.o_A = sec(8 * P); L.o_b = sec(8 * P); L.o_E = sec(8 * P);
+  L.o_A0 = sec(8 * P); L.o_b0 = sec(8 * P); L.o_E0 = sec(8 * P); L.o_tr = sec(8 * 4 * P);
+  L.o_rnu = sec(8 * 3 * P); L.o_rord = sec(8 * 3 * P); L.o_pnu = sec(8 * 3 * P);
+  L.o_rsp = sec(4 * 3 * P); L.o_psp = sec(4 * 3 * P); L.o_code = sec(4 * P); L.o_dnu = sec(8 * P);
+  L.o_eff = sec(8 * L.ntb * S);
+  L.o_cstart = sec(4 * (S + 1)); L.o_lr = sec(4 * std::max(nlist, 1)); L.o_lnu = sec(8 * std::max(nlist, 1));
+  L.bytes = off;
+  img.assign(off, 0);
+  auto D = [&](int o) { return reinterpret_cast<double*>(img.data() + o); };
+  auto I = [&](int o) { return reinterpret_cast<int*>(img.data() + o); };
+  for (int k = 0; k < ns; ++k) {
+    D(L.o_mw)[k] = d->mw[k];
+    D(L.o_invmw)[k] = 1.0 / d->mw[k];
+    const double* c = d->nasa7 + 17 * k;
+    for (int j = 0; j < 7; ++j) {
+      D(L.o_nasa)[j * S + k] = c[3 + j];
+      D(L.o_nasa)[(7 + j) * S + k] = c[10 + j];
+    }
+    D(L.o_nasa)[14 * S + k] = c[1];
+  }
+  for (int i = 0; i < 3 * P; ++i) { I(L.o_rsp)[i] = -1; I(L.o_psp)[i] = -1; }
+  int tb = 0;
+  for (int rr = 0; rr < nr; ++rr) {
+    int r = order[rr];
+    int t = d->rtype[r];
+    D(L.o_A)[rr] = d->arrh[3 * r]; D(L.o_b)[rr] = d->arrh[3 * r + 1]; D(L.o_E)[rr] = d->arrh[3 * r + 2];
+    if (t >= 2) { D(L.o_A0)[rr] = d->arrh0[3 * r]; D(L.o_b0)[rr] = d->arrh0[3 * r + 1]; D(L.o_E0)[rr] = d->arrh0[3 * r + 2]; }
+    if (t == 3) for (int j = 0; j < 4; ++j) D(L.o_tr)[j * P + rr] = d->troe[4 * r + j];
+    uint32_t w = (uint32_t)t | ((d->reversible[r] ? 1u : 0u) << 2);
+    double dn = 0.0;
+    for (int s = 0; s < 3; ++s) {
+      int a = d->rsp[3 * r + s], b = d->psp[3 * r + s];
+      I(L.o_rsp)[s * P + rr] = a; I(L.o_psp)[s * P + rr] = b;
+      if (a >= 0) {
+        double nu = d->rnu[3 * r + s], ord = d->rord[3 * r + s];
+        D(L.o_rnu)[s * P + rr] = nu; D(L.o_rord)[s * P + rr] = ord;
+        uint32_t oc = ord == 1.0 ? 1 : ord == 2.0 ? 2 : ord == 3.0 ? 3 : ord == 0.0 ? 0 : 4;
+        w |= oc << (16 + 4 * s);
+        dn -= nu;
+      }
+      if (b >= 0) { D(L.o_pnu)[s * P + rr] = d->pnu[3 * r + s]; dn += d->pnu[3 * r + s]; }
+    }
+    if (t != 0) {
+      w |= (uint32_t)tb << 8;
+      for (int k = 0; k < ns; ++k) D(L.o_eff)[tb * S + k] = d->eff[(size_t)r * ns + k];
+      ++tb;
+    }
+    reinterpret_cast<uint32_t*>(img.data() + L.o_code)[rr] = w;
+    D(L.o_dnu)[rr] = dn;
+  }
+  int e = 0;
+  for (int k = 0; k < S; ++k) {
+    I(L.o_cstart)[k] = e;
+    if (k < ns)
+      for (auto& pr : lists[k]) { I(L.o_lr)[e] = pr.first; D(L.o_lnu)[e] = pr.second; ++e; }
+  }
+  I(L.o_cstart)[S] = e;
+  return FLINT_OK;
+}
+
+static int ensure_stage(flint_mech_s* h, size_t bytes) {
+  if (bytes <= h->stage_bytes) return FLINT_OK;
+  if (h->dstage) cudaFree(h->dstage);
+  h->dstage = nullptr;
+  h->stage_bytes = 0;
+  cudaError_t e = cudaMalloc(&h->dstage, bytes);
+  if (e != cudaSuccess) return fail(FLINT_ERR_NOMEM, "staging buffer of %zu bytes: %s", bytes, cudaGetErrorString(e));
+  h->stage_bytes = bytes;
+  return FLINT_OK;
+}
+
+}  // namespace flint
+
+extern "C" {
+
+const char* flint_last_error(void) { return g_err.c_str(); }
+const char* flint_version(void) { return "flint_gb300 0.1.0 sm_103a"; }
+int64_t flint_kernel_launch_count(void) { return g_launches.load(); }
+
+int flint_mech_create(const flint_mech_desc* desc, flint_mech_t* out) {
+  if (!desc || !out) return fail(FLINT_ERR_ARG, "NULL argument");
+  *out = nullptr;
+  auto* h = new flint_mech_s();
+  int rc = pack(desc, h->L, h->himg);
+  if (rc != FLINT_OK) { delete h; return rc; }
+  cudaGetDevice(&h->device);
+  cudaError_t e = cudaMalloc(&h->dimg, h->himg.size());
+  if (e != cudaSuccess) { delete h; return fail(FLINT_ERR_NOMEM, "device image: %s", cudaGetErrorString(e)); }
+  e = cudaMemcpy(h->dimg, h->himg.data(), h->himg.size(), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMalloc(&h->dcounter, 256);
+  if (e != cudaSuccess) {
+    cudaFree(h->dimg);
+    delete h;
+    return cuda_fail(e, "flint_mech_create");
+  }
+  *out = h;
+  return FLINT_OK;
+}
+
+int flint_mech_destroy(flint_mech_t h) {
+  if (!h) return FLINT_OK;
+  if (h->dimg) cudaFree(h->dimg);
+  if (h->dcounter) cudaFree(h->dcounter);
+  if (h->dstage) cudaFree(h->dstage);
+  delete h;
+  return FLINT_OK;
+}
+
+int flint_mech_sizes(flint_mech_t h, int* ns, int* nr) {
+  if (!h) return fail(FLINT_ERR_ARG, "NULL handle");
+  if (ns) *ns = h->L.ns;
+  if (nr) *nr = h->L.nr;
+  return FLINT_OK;
+}
+
+static int check_common(flint_mech_t h, int64_t n, int layout) {
+  if (!h) return fail(FLINT_ERR_ARG, "NULL handle");
+  if (n < 0) return fail(FLINT_ERR_ARG, "negative cell count");
+  if (layout != FLINT_CELL_MAJOR && layout != FLINT_SPECIES_MAJOR) return fail(FLINT_ERR_ARG, "layout %d", layout);
+  return FLINT_OK;
+}
+
+int flint_wdot_batch(flint_mech_t h, int64_t n, int layout, const double* T, const double* p, const double* Y,
+                     double* wdot, double* cp, double* hm, void* stream) {
+  int rc = check_common(h, n, layout);
+  if (rc) return rc;
+  if (n == 0) return FLINT_OK;
+  if (!T || !p || !Y || !wdot) return fail(FLINT_ERR_ARG, "NULL array");
+  cudaError_t e = launch_wdot(h->dimg, h->L, n, layout, T, p, Y, wdot, cp, hm, (cudaStream_t)stream);
+  return e == cudaSuccess ? FLINT_OK : cuda_fail(e, "flint_wdot_batch");
+}
+
+int flint_thermo_batch(flint_mech_t h, int64_t n, int layout, const double* T, const double* Y, double* cp,
+                       double* hm, void* stream) {
+  int rc = check_common(h, n, layout);
+  if (rc) return rc;
+  if (n == 0) return FLINT_OK;
+  if (!T || !Y) return fail(FLINT_ERR_ARG, "NULL array");
+  cudaError_t e = launch_thermo(h->dimg, h->L, n, layout, T, Y, cp, hm, (cudaStream_t)stream);
+  return e == cudaSuccess ? FLINT_OK : cuda_fail(e, "flint_thermo_batch");
+}
+
+int flint_chemistry_source_batch(flint_mech_t h, int64_t n, double* roi, const double* T, double* omegadot,
+                                 void* stream) {
+  int rc = check_common(h, n, FLINT_CELL_MAJOR);
+  if (rc) return rc;
+  if (n == 0) return FLINT_OK;
+  if (!roi || !T || !omegadot) return fail(FLINT_ERR_ARG, "NULL array");
+  if (h->L.ns > 16) return fail(FLINT_ERR_MECH, "chemistry_source batch supports up to 16 species in this build");
+  cudaError_t e = launch_chemistry_source(h->dimg, h->L, n, roi, T, omegadot, (cudaStream_t)stream);
+  return e == cudaSuccess ? FLINT_OK : cuda_fail(e, "flint_chemistry_source_batch");
+}
+
+int flint_wdot_jac_batch(flint_mech_t h, int64_t n, int layout, const double* T, const double* p, const double* Y,
+                         double* wdot, double* jac, void* stream) {
+  int rc = check_common(h, n, layout);
+  if (rc) return rc;
+  if (n == 0) return FLINT_OK;
+  if (!T || !p || !Y || !jac) return fail(FLINT_ERR_ARG, "NULL array");
+  cudaError_t e = launch_wdot_jac(h->dimg, h->L, n, layout, T, p, Y, wdot, jac, (cudaStream_t)stream);
+  return e == cudaSuccess ? FLINT_OK : cuda_fail(e, "flint_wdot_jac_batch");
+}
+
+int flint_rhs_constp_batch(flint_mech_t h, int64_t n, const double* T, const double* p, const double* Y, double* f,
+                           void* stream) {
+  int rc = check_common(h, n, FLINT_CELL_MAJOR);
+  if (rc) return rc;
+  if (n == 0) return FLINT_OK;
+  if (!T || !p || !Y || !f) return fail(FLINT_ERR_ARG, "NULL array");
+  cudaError_t e = launch_rhs(h->dimg, h->L, n, T, p, Y, f, (cudaStream_t)stream);
+  return e == cudaSuccess ? FLINT_OK : cuda_fail(e, "flint_rhs_constp_batch");
+}
+
+void flint_reactor_default_opts(flint_reactor_opts* o) {
+  if (!o) return;
+  o->rtol = 1e-8; o->atol = 1e-14; o->max_steps = 20000; o->max_order = 5;
+  o->constant_volume = 0; o->reserved = 0; o->tmin = 200.0; o->tmax = 6000.0;
+}
+
+int flint_reactor_advance(flint_mech_t h, int64_t n, double* T, const double* p, double* Y, const double* dt,
+                          const flint_reactor_opts* opts, int* status, int* nsteps, void* stream) {
+  int rc = check_common(h, n, FLINT_CELL_MAJOR);
+  if (rc) return rc;
+  if (n == 0) return FLINT_OK;
+  if (!T || !p || !Y || !dt) return fail(FLINT_ERR_ARG, "NULL array");
+  flint_reactor_opts o;
+  if (opts) o = *opts; else flint_reactor_default_opts(&o);
+  if (!(o.rtol > 0.0) || !(o.atol > 0.0) || o.max_steps < 1 || o.max_order < 1 || o.max_order > 5)
+    return fail(FLINT_ERR_ARG, "reactor options out of range");
+  if (o.constant_volume) return fail(FLINT_ERR_ARG, "constant-volume reactor is not in this build");
+  cudaError_t e = launch_reactor(h->dimg, h->L, n, T, p, Y, dt, o, status, nsteps, h->dcounter,
+                                 (cudaStream_t)stream);
+  return e == cudaSuccess ? FLINT_OK : cuda_fail(e, "flint_reactor_advance");
+}
+
+// ------------------------------------------------------------------ host forms
+int flint_wdot_batch_host(flint_mech_t h, int64_t n, int layout, const double* T, const double* p, const double* Y,
+                          double* wdot, double* cp, double* hm) {
+  int rc = check_common(h, n, layout);
+  if (rc || n == 0) return rc;
+  const int ns = h->L.ns;
+  size_t nb = (size_t)n * 8;
+  rc = ensure_stage(h, nb * (4 + 2 * ns));
+  if (rc) return rc;
+  double* dT = (double*)h->dstage;
+  double* dp = dT + n;
+  double* dY = dp + n;
+  double* dw = dY + (size_t)n * ns;
+  double* dcp = dw + (size_t)n * ns;
+  double* dh = dcp + n;
+  cudaError_t e = cudaMemcpy(dT, T, nb, cudaMemcpyHostToDevice);
+  if (!e) e = cudaMemcpy(dp, p, nb, cudaMemcpyHostToDevice);
+  if (!e) e = cudaMemcpy(dY, Y, nb * ns, cudaMemcpyHostToDevice);
+  if (e) return cuda_fail(e, "H2D");
+  rc = flint_wdot_batch(h, n, layout, dT, dp, dY, dw, cp ? dcp : nullptr, hm ? dh : nullptr, nullptr);
+  if (rc) return rc;
+  e = cudaMemcpy(wdot, dw, nb * ns, cudaMemcpyDeviceToHost);
+  if (!e && cp) e = cudaMemcpy(cp, dcp, nb, cudaMemcpyDeviceToHost);
+  if (!e && hm) e = cudaMemcpy(hm, dh, nb, cudaMemcpyDeviceToHost);
+  return e ? cuda_fail(e, "D2H") : FLINT_OK;
+}
+
+int flint_wdot_jac_batch_host(flint_mech_t h, int64_t n, int layout, const double* T, const double* p,
+                              const double* Y, double* wdot, double* jac) {
+  int rc = check_common(h, n, layout);
+  if (rc || n == 0) return rc;
+  const int ns = h->L.ns, nv = ns + 1;
+  size_t nb = (size_t)n * 8;
+  rc = ensure_stage(h, nb * (2 + 2 * ns + nv * nv));
+  if (rc) return rc;
+  double* dT = (double*)h->dstage;
+  double* dp = dT + n;
+  double* dY = dp + n;
+  double* dw = dY + (size_t)n * ns;
+  double* dj = dw + (size_t)n * ns;
+  cudaError_t e = cudaMemcpy(dT, T, nb, cudaMemcpyHostToDevice);
+  if (!e) e = cudaMemcpy(dp, p, nb, cudaMemcpyHostToDevice);
+  if (!e) e = cudaMemcpy(dY, Y, nb * ns, cudaMemcpyHostToDevice);
+  if (e) return cuda_fail(e, "H2D");
+  rc = flint_wdot_jac_batch(h, n, layout, dT, dp, dY, wdot ? dw : nullptr, dj, nullptr);
+  if (rc) return rc;
+  if (wdot) e = cudaMemcpy(wdot, dw, nb * ns, cudaMemcpyDeviceToHost);
+  if (!e) e = cudaMemcpy(jac, dj, nb * nv * nv, cudaMemcpyDeviceToHost);
+  return e ? cuda_fail(e, "D2H") : FLINT_OK;
+}
+
+int flint_reactor_advance_host(flint_mech_t h, int64_t n, double* T, const double* p, double* Y, const double* dt,
+                               const flint_reactor_opts* opts, int* status, int* nsteps) {
+  int rc = check_common(h, n, FLINT_CELL_MAJOR);
+  if (rc || n == 0) return rc;
+  const int ns = h->L.ns;
+  size_t nb = (size_t)n * 8;
+  rc = ensure_stage(h, nb * (3 + ns) + (size_t)n * 8);
+  if (rc) return rc;
+  double* dT = (double*)h->dstage;
+  double* dp = dT + n;
+  double* dY = dp + n;
+  double* ddt = dY + (size_t)n * ns;
+  int* dst = (int*)(ddt + n);
+  int* dns = dst + n;
+  cudaError_t e = cudaMemcpy(dT, T, nb, cudaMemcpyHostToDevice);
+  if (!e) e = cudaMemcpy(dp, p, nb, cudaMemcpyHostToDevice);
+  if (!e) e = cudaMemcpy(dY, Y, nb * ns, cudaMemcpyHostToDevice);
+  if (!e) e = cudaMemcpy(ddt, dt, nb, cudaMemcpyHostToDevice);
+  if (e) return cuda_fail(e, "H2D");
+  rc = flint_reactor_advance(h, n, dT, dp, dY, ddt, opts, dst, dns, nullptr);
+  if (rc) return rc;
+  e = cudaMemcpy(T, dT, nb, cudaMemcpyDeviceToHost);
+  if (!e) e = cudaMemcpy(Y, dY, nb * ns, cudaMemcpyDeviceToHost);
+  if (!e && status) e = cudaMemcpy(status, dst, (size_t)n * 4, cudaMemcpyDeviceToHost);
+  if (!e && nsteps) e = cudaMemcpy(nsteps, dns, (size_t)n * 4, cudaMemcpyDeviceToHost);
+  return e ? cuda_fail(e, "D2H") : FLINT_OK;
+}
+
+}  // extern "C"

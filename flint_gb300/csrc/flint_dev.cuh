@@ -1,0 +1,424 @@
+// flint_dev.cuh -- device-side mechanism image and warp-per-cell kinetics.
+//
+// One warp owns one cell.  Species-parallel work (thermo, production sums,
+// Jacobian rows) maps species k to lane k (k + 32 for the second row block);
+// reaction-parallel work (rate constants, rates of progress) maps reaction r
+// to lane r % 32 in rounds of 32.  The mechanism image is staged once per
+// block in shared memory as structure-of-arrays so that the 32 lanes of a
+// round read 32 consecutive words (no bank conflicts).
+//
+// Math follows FLINT's chemistry path (paths within the FLINT project):
+//   rates of progress, third body, species sums  src/lib/Lib_Chemistry_wdot.f90:96-220
+//   Lindemann / Troe blending, f_F              src/lib/Lib_Chemistry_falloff.f90:12-80
+//   reverse rate kb = kf / kc                   src/lib/Lib_Chemistry_falloff.f90:31,56
+// with kf, kc, Fcent evaluated from the Arrhenius / NASA-7 / Troe parameters
+// the reference's tables were generated from (Kc = exp(-dG/RT)(p_ref/RT)^dnu).
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace flint {
+
+constexpr int WARP = 32;
+constexpr int MAXSIDE = 3;
+constexpr unsigned FULL = 0xffffffffu;
+
+// Reaction code word: bits 0-1 type, bit 2 reversible, bits 8-15 third-body
+// row, bits 16-27 order codes of the 3 reactant slots (4 bits each) and
+// bits 28-31 unused.  Order code: 0 absent, 1..3 integral power, 4 general pow.
+__host__ __device__ inline int rx_type(uint32_t w) { return w & 3; }
+__host__ __device__ inline bool rx_rev(uint32_t w) { return (w >> 2) & 1; }
+__host__ __device__ inline int rx_tbrow(uint32_t w) { return (w >> 8) & 0xff; }
+__host__ __device__ inline int rx_ordcode(uint32_t w, int s) { return (w >> (16 + 4 * s)) & 0xf; }
+
+// Offsets (in bytes) of each section of the packed image.  All sections are
+// 16-byte aligned; the image is copied to shared memory with 16-byte loads.
+struct ImageLayout {
+  int ns, nr, nrpad, nsp;        // nsp = species padded to a multiple of 32
+  int ntb;                       // rows of third-body efficiencies
+  int nlist;                     // CSR entries (species -> reactions)
+  int bytes;                     // total image size
+  double r_eos, r_thermo, lnpref_rth;   // ln(p_ref / r_thermo)
+  // species
+  int o_mw, o_invmw, o_nasa;     // nasa: [16][nsp] : low a0..a6, high a0..a6, tmid, unused
+  // reactions (nrpad each)
+  int o_A, o_b, o_E, o_A0, o_b0, o_E0, o_tr;   // tr: [4][nrpad]
+  int o_rnu, o_rord, o_pnu;      // [3][nrpad]
+  int o_rsp, o_psp;              // int32 [3][nrpad]
+  int o_code;                    // uint32 [nrpad]
+  int o_dnu;                     // double [nrpad]
+  int o_eff;                     // [ntb][nsp]
+  int o_cstart;                  // int32 [nsp+1]
+  int o_lr;                      // int32 [nlist]
+  int o_lnu;                     // double [nlist]
+};
+
+struct MechView {
+  int ns, nr, nrpad, nsp, ntb;
+  double r_eos, r_thermo, lnpref_rth;
+  const double *mw, *invmw, *nasa;
+  const double *A, *b, *E, *A0, *b0, *E0, *tr;
+  const double *rnu, *rord, *pnu, *dnu;
+  const int *rsp, *psp, *cstart, *lr;
+  const uint32_t* code;
+  const double *eff, *lnu;
+
+  __host__ __device__ void bind(const ImageLayout& L, const uint8_t* base) {
+    ns = L.ns; nr = L.nr; nrpad = L.nrpad; nsp = L.nsp; ntb = L.ntb;
+    r_eos = L.r_eos; r_thermo = L.r_thermo; lnpref_rth = L.lnpref_rth;
+    mw = (const double*)(base + L.o_mw); invmw = (const double*)(base + L.o_invmw);
+    nasa = (const double*)(base + L.o_nasa);
+    A = (const double*)(base + L.o_A); b = (const double*)(base + L.o_b); E = (const double*)(base + L.o_E);
+    A0 = (const double*)(base + L.o_A0); b0 = (const double*)(base + L.o_b0); E0 = (const double*)(base + L.o_E0);
+    tr = (const double*)(base + L.o_tr);
+    rnu = (const double*)(base + L.o_rnu); rord = (const double*)(base + L.o_rord);
+    pnu = (const double*)(base + L.o_pnu); dnu = (const double*)(base + L.o_dnu);
+    rsp = (const int*)(base + L.o_rsp); psp = (const int*)(base + L.o_psp);
+    code = (const uint32_t*)(base + L.o_code);
+    eff = (const double*)(base + L.o_eff);
+    cstart = (const int*)(base + L.o_cstart); lr = (const int*)(base + L.o_lr);
+    lnu = (const double*)(base + L.o_lnu);
+  }
+};
+
+// Copy the image (global) into shared memory; whole block participates.
+__device__ inline void stage_image(uint8_t* smem, const uint8_t* __restrict__ g, int bytes) {
+  const int4* src = reinterpret_cast<const int4*>(g);
+  int4* dst = reinterpret_cast<int4*>(smem);
+  for (int i = threadIdx.x; i < bytes / 16; i += blockDim.x) dst[i] = __ldg(src + i);
+  __syncthreads();
+}
+
+__device__ inline double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(FULL, v, o);
+  return v;   // identical on every lane (xor butterfly)
+}
+
+__device__ inline double warp_max(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(FULL, v, o));
+  return v;
+}
+
+// NASA-7 thermo of species k at T (lane-local).
+struct SpThermo { double cpR, hRT, sR, dcpR; };
+
+__device__ inline SpThermo nasa7(const MechView& m, int k, double T, double lnT, double invT) {
+  const int S = m.nsp;
+  const double tmid = m.nasa[14 * S + k];
+  const double* a = m.nasa + ((T <= tmid) ? 0 : 7 * S) + k;
+  double a0 = a[0], a1 = a[S], a2 = a[2 * S], a3 = a[3 * S], a4 = a[4 * S], a5 = a[5 * S], a6 = a[6 * S];
+  SpThermo t;
+  t.cpR = a0 + T * (a1 + T * (a2 + T * (a3 + T * a4)));
+  t.hRT = a0 + T * (a1 * 0.5 + T * (a2 * (1.0 / 3.0) + T * (a3 * 0.25 + T * a4 * 0.2))) + a5 * invT;
+  t.sR = a0 * lnT + T * (a1 + T * (a2 * 0.5 + T * (a3 * (1.0 / 3.0) + T * a4 * 0.25))) + a6;
+  t.dcpR = a1 + T * (2.0 * a2 + T * (3.0 * a3 + T * 4.0 * a4));
+  return t;
+}
+
+// c^ord by order code (1..3 integral, 4 general) with the derivative d(c^ord)/dc.
+__device__ inline double powc(double c, int code, double ord, double* d) {
+  switch (code) {
+    case 1: *d = 1.0; return c;
+    case 2: *d = 2.0 * c; return c * c;
+    case 3: *d = 3.0 * c * c; return c * c * c;
+    case 4: {
+      double cc = c > 0.0 ? c : 0.0;
+      if (cc > 0.0) {
+        double pw = exp(ord * log(cc));
+        *d = ord * pw / cc;
+        return pw;
+      }
+      *d = 0.0;
+      return 0.0;
+    }
+    default: *d = 0.0; return 1.0;
+  }
+}
+
+__device__ inline int ordcode_of(double nu) {
+  return nu == 1.0 ? 1 : (nu == 2.0 ? 2 : (nu == 3.0 ? 3 : (nu == 0.0 ? 0 : 4)));
+}
+
+// Per-warp scratch (doubles) used by the kinetics.
+struct WarpScratch {
+  double* c;      // [nsp]
+  double* hRT;    // [nsp]
+  double* gRT;    // [nsp]
+  double* q;      // [nrpad] rates of progress
+  // Jacobian mode only
+  double* dq;     // [8][nrpad]: 6 sparse partials (3 reactant, 3 product slots), tb coef, dq/dT
+  double* Jr;     // [n][ldj] rows (species rows then T row), ldj = nsp+1 (odd stride)
+  int ldj;
+};
+
+__host__ __device__ inline int scratch_doubles(int nsp, int nrpad, bool jac) {
+  int base = 3 * nsp + nrpad;
+  if (jac) base += 8 * nrpad + (nsp + 1) * (nsp + 1);
+  return (base + 1) & ~1;   // keep 16-byte alignment
+}
+
+__device__ inline WarpScratch carve(double* p, int nsp, int nrpad, bool jac) {
+  WarpScratch s;
+  s.c = p; s.hRT = p + nsp; s.gRT = p + 2 * nsp; s.q = p + 3 * nsp;
+  s.ldj = nsp + 1;
+  if (jac) { s.dq = s.q + nrpad; s.Jr = s.dq + 8 * nrpad; } else { s.dq = nullptr; s.Jr = nullptr; }
+  return s;
+}
+
+// Cell-level results held per lane: lane k (< ns) gets species k, the T-row
+// quantities are uniform across the warp.
+struct CellOut {
+  double wmol;    // lane k: molar production (kmol/m^3/s)
+  double cpR;     // lane k: cp_k / R
+  double f;       // lane k < ns: dY_k/dt; lane ns (if < 32): dT/dt
+  double fT;      // dT/dt (uniform)
+  double rho;     // uniform
+  double cp_mass, h_mass;   // uniform: mixture cp [J/kg/K], h [J/kg]
+};
+
+// Troe / Lindemann effective forward coefficient with its derivatives.
+struct Falloff { double keff, dlnkeff, dkeff_dM; };
+
+__device__ inline Falloff falloff_eval(const MechView& m, int r, int type, double kinf, double dlnkinf,
+                                       double M, double T, double lnT, double invT) {
+  double k0 = m.A0[r] * exp(m.b0[r] * lnT - m.E0[r] * invT);
+  double dlnk0 = (m.b0[r] + m.E0[r] * invT) * invT;
+  double kratio = k0 / kinf;
+  double Pr = kratio * M;
+  double F = 1.0, G = 0.0, dlnF_T = 0.0;
+  if (type == 3) {
+    const int P = m.nrpad;
+    double a = m.tr[r], T3 = m.tr[P + r], T1 = m.tr[2 * P + r], T2 = m.tr[3 * P + r];
+    double e3 = exp(-T / T3), e1 = exp(-T / T1);
+    double Fc = (1.0 - a) * e3 + a * e1;
+    double dFc = -(1.0 - a) / T3 * e3 - a / T1 * e1;
+    if (T2 != 0.0) {
+      double e2 = exp(-T2 * invT);
+      Fc += e2;
+      dFc += T2 * invT * invT * e2;
+    }
+    double logFc = log10(Fc);
+    double cc = -0.4 - 0.67 * logFc;
+    double nn = 0.75 - 1.27 * logFc;
+    double x = log10(Pr > 1e-300 ? Pr : 1e-300) + cc;
+    double den = nn - 0.14 * x;
+    double f1 = x / den;
+    double opf = 1.0 + f1 * f1;
+    F = exp(2.302585092994045684 * (logFc / opf));
+    double Aq = 2.0 * logFc * f1 / (opf * opf * den * den);
+    G = -Aq * nn;
+    dlnF_T = (1.0 / opf + Aq * (0.67 * nn - 1.27 * x)) * dFc / Fc;
+  }
+  double opr = 1.0 + Pr;
+  Falloff o;
+  o.keff = kinf * (Pr / opr) * F;
+  double dlnPr = dlnk0 - dlnkinf;
+  o.dlnkeff = dlnkinf + dlnPr / opr + G * dlnPr + dlnF_T;
+  o.dkeff_dM = kinf * F / opr * (1.0 / opr + G) * kratio;
+  return o;
+}
+
+// Warp-cooperative kinetics of one cell.  Lane k < ns supplies Y_k (others 0).
+// Computes c, thermo, rates of progress, molar production, the RHS of the
+// constant-pressure reactor and (JAC) the Jacobian rows in s.Jr:
+//   s.Jr[i*ldj + j] = d f_i / d x_j,  x = (Y_0..Y_{ns-1}, T), f = (dY/dt, dT/dt).
+template <bool JAC>
+__device__ void warp_kinetics(const MechView& m, const WarpScratch& s, int lane, double Yk,
+                              double T, double p, CellOut& out) {
+  const int ns = m.ns, nsp = m.nsp, nrpad = m.nrpad;
+  const double lnT = log(T), invT = 1.0 / T;
+  const double lnC0 = m.lnpref_rth - lnT;        // ln(p_ref / (R T))
+  // mixture molar mass and density
+  double sumYW = warp_sum(lane < ns ? Yk * m.invmw[lane] : 0.0);
+  double rho = p / (m.r_eos * T * sumYW);
+  double wbar = 1.0 / sumYW;
+  // species-parallel: concentrations and thermo, species k on lane k
+  // (the warp kernels are used for ns <= 31, so one pass covers all species)
+  double my_cpR = 0.0, my_hRT = 0.0, my_dcpR = 0.0, my_c = 0.0;
+  {
+    double ck = 0.0, hr = 0.0, gr = 0.0;
+    if (lane < ns) {
+      ck = rho * Yk * m.invmw[lane];
+      SpThermo th = nasa7(m, lane, T, lnT, invT);
+      hr = th.hRT; gr = th.hRT - th.sR;
+      my_cpR = th.cpR; my_hRT = th.hRT; my_dcpR = th.dcpR; my_c = ck;
+    }
+    s.c[lane] = ck; s.hRT[lane] = hr; s.gRT[lane] = gr;
+  }
+  __syncwarp();
+  // reaction-parallel: rates of progress
+  for (int r = lane; r < nrpad; r += WARP) {
+    double q = 0.0;
+    if (r < m.nr) {
+      const uint32_t w = m.code[r];
+      const int type = rx_type(w);
+      const bool rev = rx_rev(w);
+      double kf = m.A[r] * exp(m.b[r] * lnT - m.E[r] * invT);
+      double dlnkf = (m.b[r] + m.E[r] * invT) * invT;
+      double pwf[MAXSIDE], dpf[MAXSIDE], pwr[MAXSIDE], dpr[MAXSIDE];
+      double Pf = 1.0, Pr = 0.0;
+#pragma unroll
+      for (int sl = 0; sl < MAXSIDE; ++sl) {
+        int sp = m.rsp[sl * nrpad + r];
+        int oc = rx_ordcode(w, sl);
+        if (sp >= 0) pwf[sl] = powc(s.c[sp], oc, m.rord[sl * nrpad + r], &dpf[sl]);
+        else { pwf[sl] = 1.0; dpf[sl] = 0.0; }
+        Pf *= pwf[sl];
+      }
+      double invKc = 0.0, dlnKc = 0.0;
+      if (rev) {
+        double dG = 0.0, dH = 0.0;
+        Pr = 1.0;
+#pragma unroll
+        for (int sl = 0; sl < MAXSIDE; ++sl) {
+          int sp = m.psp[sl * nrpad + r];
+          if (sp >= 0) {
+            double nu = m.pnu[sl * nrpad + r];
+            dG += nu * s.gRT[sp];
+            if (JAC) dH += nu * s.hRT[sp];
+            pwr[sl] = powc(s.c[sp], ordcode_of(nu), nu, &dpr[sl]);
+          } else { pwr[sl] = 1.0; dpr[sl] = 0.0; }
+          Pr *= pwr[sl];
+          int sq = m.rsp[sl * nrpad + r];
+          if (sq >= 0) {
+            double nu = m.rnu[sl * nrpad + r];
+            dG -= nu * s.gRT[sq];
+            if (JAC) dH -= nu * s.hRT[sq];
+          }
+        }
+        const double dn = m.dnu[r];
+        // 1/Kc = exp(dG - dnu ln(p_ref/RT))
+        invKc = exp(dG - dn * lnC0);
+        dlnKc = (dH - dn) * invT;
+      }
+      double Mfac = 1.0, keff = kf, dlnkeff = dlnkf, dkdM = 0.0, M = 0.0;
+      const double* effrow = nullptr;
+      if (type != 0) {
+        effrow = m.eff + rx_tbrow(w) * nsp;
+        for (int k = 0; k < ns; ++k) M += effrow[k] * s.c[k];
+        if (type == 1) {
+          Mfac = M;
+        } else {
+          Falloff fo = falloff_eval(m, r, type, kf, dlnkf, M, T, lnT, invT);
+          keff = fo.keff; dlnkeff = fo.dlnkeff; dkdM = fo.dkeff_dM;
+        }
+      }
+      double fwd = Mfac * keff * Pf;
+      double rvs = rev ? Mfac * keff * invKc * Pr : 0.0;
+      q = fwd - rvs;
+      if (JAC) {
+        // sparse partials by slot: reactant slots 0..2, product slots 3..5
+        const double kM = Mfac * keff;
+#pragma unroll
+        for (int sl = 0; sl < MAXSIDE; ++sl) {
+          double d = dpf[sl];
+#pragma unroll
+          for (int u = 0; u < MAXSIDE; ++u) if (u != sl) d *= pwf[u];
+          s.dq[sl * nrpad + r] = kM * d;
+          double e = 0.0;
+          if (rev) {
+            e = dpr[sl];
+#pragma unroll
+            for (int u = 0; u < MAXSIDE; ++u) if (u != sl) e *= pwr[u];
+            e = -kM * invKc * e;
+          }
+          s.dq[(3 + sl) * nrpad + r] = e;
+        }
+        double tb = 0.0;
+        if (type == 1) tb = keff * (Pf - (rev ? invKc * Pr : 0.0));
+        else if (type >= 2) tb = dkdM * (Pf - (rev ? invKc * Pr : 0.0));
+        s.dq[6 * nrpad + r] = tb;
+        s.dq[7 * nrpad + r] = fwd * dlnkeff - rvs * (dlnkeff - dlnKc);
+      }
+    }
+    s.q[r] = q;
+  }
+  __syncwarp();
+  // species-parallel: production rates (lane k sums its reaction list)
+  double wm = 0.0;
+  if (lane < ns) {
+    for (int e = m.cstart[lane]; e < m.cstart[lane + 1]; ++e) wm += m.lnu[e] * s.q[m.lr[e]];
+  }
+  double Q = warp_sum(lane < ns ? my_hRT * wm : 0.0);
+  double D = warp_sum(lane < ns ? my_c * my_cpR : 0.0);
+  double fT = -T * Q / D;
+  out.wmol = wm;
+  out.cpR = my_cpR;
+  out.rho = rho;
+  out.fT = fT;
+  out.f = (lane < ns) ? m.mw[lane] * wm / rho : (lane == ns ? fT : 0.0);
+  // mixture cp and h (mass)
+  double cpm = warp_sum(lane < ns ? Yk * my_cpR * m.invmw[lane] : 0.0);
+  double hm = warp_sum(lane < ns ? Yk * my_hRT * m.invmw[lane] : 0.0);
+  out.cp_mass = cpm * m.r_thermo;
+  out.h_mass = hm * m.r_thermo * T;
+  if (!JAC) return;
+
+  // ---- Jacobian in concentration space: row k = species k (lane k) -------
+  const int ld = s.ldj;
+  double* Jrow = s.Jr + lane * ld;
+  double JT = 0.0;
+  if (lane < ns) {
+    for (int j = 0; j < ns; ++j) Jrow[j] = 0.0;
+    for (int e = m.cstart[lane]; e < m.cstart[lane + 1]; ++e) {
+      const int r = m.lr[e];
+      const double nu = m.lnu[e];
+#pragma unroll
+      for (int sl = 0; sl < MAXSIDE; ++sl) {
+        int sp = m.rsp[sl * nrpad + r];
+        if (sp >= 0) Jrow[sp] += nu * s.dq[sl * nrpad + r];
+        int sq = m.psp[sl * nrpad + r];
+        if (sq >= 0) Jrow[sq] += nu * s.dq[(3 + sl) * nrpad + r];
+      }
+      const uint32_t w = m.code[r];
+      if (rx_type(w) != 0) {
+        const double t = nu * s.dq[6 * nrpad + r];
+        const double* effrow = m.eff + rx_tbrow(w) * nsp;
+        for (int j = 0; j < ns; ++j) Jrow[j] += t * effrow[j];
+      }
+      JT += nu * s.dq[7 * nrpad + r];
+    }
+  }
+  __syncwarp();
+  // S_k = sum_j c_j Jc[k][j] (row k); HJ_m = sum_k hRT_k Jc[k][m] (column m)
+  double Sk = 0.0, HJ = 0.0;
+  if (lane < ns) {
+    for (int j = 0; j < ns; ++j) Sk += s.c[j] * Jrow[j];
+    for (int k = 0; k < ns; ++k) HJ += s.hRT[k] * s.Jr[k * ld + lane];
+  }
+  double HS = warp_sum(lane < ns ? my_hRT * Sk : 0.0);
+  __syncwarp();
+  const double wr = wbar / rho;
+  // T row pieces (lane m computes column m of the T row)
+  double dQT_l = 0.0, dDT_l = 0.0;
+  if (lane < ns) {
+    dQT_l = (my_cpR - my_hRT) * invT * wm + my_hRT * (JT - Sk * invT);
+    dDT_l = my_c * (my_dcpR - my_cpR * invT);
+  }
+  double dQT = warp_sum(dQT_l), dDT = warp_sum(dDT_l);
+  double JTT = -Q / D - (T / D) * (dQT - (Q / D) * dDT);
+  double JTm = 0.0;
+  if (lane < ns) {
+    double rw = rho * m.invmw[lane], ww = wbar * m.invmw[lane];
+    double dQ = rw * HJ - ww * HS;
+    double dD = rw * my_cpR - ww * D;
+    JTm = -(T / D) * (dQ - (Q / D) * dD);
+  }
+  // species rows in (Y, T) variables
+  if (lane < ns) {
+    const double tk = Sk - wm;
+    const double Wk = m.mw[lane];
+    for (int j = 0; j < ns; ++j) Jrow[j] = Wk * m.invmw[j] * (Jrow[j] - wr * tk);
+    Jrow[ns] = (Wk / rho) * (JT - tk * invT);
+  }
+  __syncwarp();
+  // T row (row ns)
+  double* JrowT = s.Jr + ns * ld;
+  if (lane < ns) JrowT[lane] = JTm;
+  if (lane == 0) JrowT[ns] = JTT;
+  __syncwarp();
+}
+
+}  // namespace flint

@@ -1,0 +1,27 @@
+// flint_host.h -- internal host-side declarations shared by the .cu files.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+#include "flint_dev.cuh"
+#include "../../include/flint_gpu.h"
+
+namespace flint {
+
+void count_launch();
+int device_sms();
+
+cudaError_t launch_wdot(const uint8_t* img, const ImageLayout& L, int64_t n, int layout, const double* T,
+                        const double* p, const double* Y, double* wdot, double* cp, double* h, cudaStream_t st);
+cudaError_t launch_thermo(const uint8_t* img, const ImageLayout& L, int64_t n, int layout, const double* T,
+                          const double* Y, double* cp, double* h, cudaStream_t st);
+cudaError_t launch_chemistry_source(const uint8_t* img, const ImageLayout& L, int64_t n, double* roi,
+                                    const double* T, double* omegadot, cudaStream_t st);
+cudaError_t launch_wdot_jac(const uint8_t* img, const ImageLayout& L, int64_t n, int layout, const double* T,
+                            const double* p, const double* Y, double* wdot, double* jac, cudaStream_t st);
+cudaError_t launch_rhs(const uint8_t* img, const ImageLayout& L, int64_t n, const double* T, const double* p,
+                       const double* Y, double* f, cudaStream_t st);
+cudaError_t launch_reactor(const uint8_t* img, const ImageLayout& L, int64_t n, double* T, const double* p,
+                           double* Y, const double* dt, const flint_reactor_opts& o, int* status, int* nsteps,
+                           unsigned int* work_counter, cudaStream_t st);
+
+}  // namespace flint

@@ -1,0 +1,303 @@
+// flint_kernels.cu -- batched source-term, Jacobian and thermo kernels.
+//
+//  k_wdot_small   one thread per cell, for small mechanisms (ns <= 16): the
+//                 2-step CH4/air case.  Mechanism staged in shared memory;
+//                 every thread reads the same reaction word at the same time
+//                 (broadcast), per-thread species arrays live in shared memory
+//                 as [species][thread] (conflict-free).
+//  k_wdot_warp    one warp per cell (ns <= 31): reaction-parallel rates of
+//                 progress, species-parallel sums; optional analytic Jacobian
+//                 written coalesced (lane = row, one column per store).
+//  k_rhs_warp     constant-pressure reactor right-hand side.
+//
+// All kernels are grid-stride loops over cells sized to whole waves of the 152
+// SMs, so any N (including 0 and ragged tails) is handled without a tail kernel.
+#include "flint_dev.cuh"
+#include "flint_host.h"
+
+namespace flint {
+
+constexpr int SMALL_NSMAX = 16;
+constexpr int SMALL_THREADS = 128;
+constexpr int WARP_THREADS = 256;
+
+// ---------------------------------------------------------------- small
+__global__ void __launch_bounds__(SMALL_THREADS)
+k_wdot_small(const uint8_t* __restrict__ img, ImageLayout L, int64_t n, int layout,
+             const double* __restrict__ Tg, const double* __restrict__ pg,
+             const double* __restrict__ Yg, double* __restrict__ wdot,
+             double* __restrict__ cpo, double* __restrict__ ho, int roi_mode, double* roi_io) {
+  extern __shared__ __align__(16) uint8_t smem[];
+  stage_image(smem, img, L.bytes);
+  MechView m;
+  m.bind(L, smem);
+  const int ns = m.ns, P = m.nrpad;
+  double* cs = reinterpret_cast<double*>(smem + L.bytes);      // [NSMAX][threads]
+  double* gs = cs + SMALL_NSMAX * SMALL_THREADS;
+  double* ws = gs + SMALL_NSMAX * SMALL_THREADS;
+  const int t = threadIdx.x;
+#define CS(k) cs[(k) * SMALL_THREADS + t]
+#define GS(k) gs[(k) * SMALL_THREADS + t]
+#define WS(k) ws[(k) * SMALL_THREADS + t]
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + t; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double T = Tg[i];
+    const double lnT = log(T), invT = 1.0 / T;
+    double rho;
+    double cpm = 0.0, hm = 0.0;
+    if (roi_mode) {
+      // chemistry_source(roi, T, omegadot): c = max(roi,0)/W (WD.f90:18-21)
+      rho = 0.0;
+      for (int k = 0; k < ns; ++k) {
+        double r = roi_io[i * ns + k];
+        r = r > 0.0 ? r : 0.0;
+        roi_io[i * ns + k] = r;
+        CS(k) = r * m.invmw[k];
+      }
+    } else {
+      double sumYW = 0.0;
+      for (int k = 0; k < ns; ++k) {
+        double y = (layout == 1) ? Yg[(int64_t)k * n + i] : Yg[i * ns + k];
+        CS(k) = y;
+        sumYW += y * m.invmw[k];
+      }
+      rho = pg[i] / (m.r_eos * T * sumYW);
+      for (int k = 0; k < ns; ++k) {
+        double y = CS(k);
+        SpThermo th = nasa7(m, k, T, lnT, invT);
+        cpm += y * th.cpR * m.invmw[k];
+        hm += y * th.hRT * m.invmw[k];
+        CS(k) = rho * y * m.invmw[k];
+        GS(k) = th.hRT - th.sR;
+      }
+    }
+    if (roi_mode) {
+      for (int k = 0; k < ns; ++k) {
+        SpThermo th = nasa7(m, k, T, lnT, invT);
+        GS(k) = th.hRT - th.sR;
+      }
+    }
+    for (int k = 0; k < ns; ++k) WS(k) = 0.0;
+    const double lnC0 = m.lnpref_rth - lnT;
+    for (int r = 0; r < m.nr; ++r) {
+      const uint32_t w = m.code[r];
+      const int type = rx_type(w);
+      double kf = m.A[r] * exp(m.b[r] * lnT - m.E[r] * invT);
+      double Pf = 1.0, d;
+#pragma unroll
+      for (int sl = 0; sl < MAXSIDE; ++sl) {
+        int sp = m.rsp[sl * P + r];
+        if (sp >= 0) Pf *= powc(CS(sp), rx_ordcode(w, sl), m.rord[sl * P + r], &d);
+      }
+      double rvsf = 0.0;
+      if (rx_rev(w)) {
+        double dG = 0.0, Pr = 1.0;
+#pragma unroll
+        for (int sl = 0; sl < MAXSIDE; ++sl) {
+          int sp = m.psp[sl * P + r];
+          if (sp >= 0) {
+            double nu = m.pnu[sl * P + r];
+            dG += nu * GS(sp);
+            Pr *= powc(CS(sp), ordcode_of(nu), nu, &d);
+          }
+          int sq = m.rsp[sl * P + r];
+          if (sq >= 0) dG -= m.rnu[sl * P + r] * GS(sq);
+        }
+        rvsf = exp(dG - m.dnu[r] * lnC0) * Pr;
+      }
+      double keff = kf, Mfac = 1.0;
+      if (type != 0) {
+        const double* effrow = m.eff + rx_tbrow(w) * m.nsp;
+        double M = 0.0;
+        for (int k = 0; k < ns; ++k) M += effrow[k] * CS(k);
+        if (type == 1) Mfac = M;
+        else keff = falloff_eval(m, r, type, kf, 0.0, M, T, lnT, invT).keff;
+      }
+      const double q = Mfac * keff * (Pf - rvsf);
+#pragma unroll
+      for (int sl = 0; sl < MAXSIDE; ++sl) {
+        int sp = m.rsp[sl * P + r];
+        if (sp >= 0) WS(sp) -= m.rnu[sl * P + r] * q;
+        int sq = m.psp[sl * P + r];
+        if (sq >= 0) WS(sq) += m.pnu[sl * P + r] * q;
+      }
+    }
+    if (wdot) {
+      for (int k = 0; k < ns; ++k) {
+        double v = m.mw[k] * WS(k);
+        if (roi_mode || layout == 0) wdot[i * ns + k] = v;
+        else wdot[(int64_t)k * n + i] = v;
+      }
+    }
+    (void)rho;
+    if (cpo) cpo[i] = cpm * m.r_thermo;
+    if (ho) ho[i] = hm * m.r_thermo * T;
+  }
+#undef CS
+#undef GS
+#undef WS
+}
+
+// ---------------------------------------------------------------- warp
+template <bool JAC>
+__global__ void __launch_bounds__(WARP_THREADS)
+k_wdot_warp(const uint8_t* __restrict__ img, ImageLayout L, int64_t n, int layout,
+            const double* __restrict__ Tg, const double* __restrict__ pg,
+            const double* __restrict__ Yg, double* __restrict__ wdot, double* __restrict__ cpo,
+            double* __restrict__ ho, double* __restrict__ jac, double* __restrict__ rhs_out) {
+  extern __shared__ __align__(16) uint8_t smem[];
+  stage_image(smem, img, L.bytes);
+  MechView m;
+  m.bind(L, smem);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int sd = scratch_doubles(m.nsp, m.nrpad, JAC);
+  WarpScratch s = carve(reinterpret_cast<double*>(smem + L.bytes) + wid * sd, m.nsp, m.nrpad, JAC);
+  const int ns = m.ns, nv = ns + 1;
+  const int64_t nwarps = (int64_t)gridDim.x * (blockDim.x >> 5);
+  for (int64_t cell = (int64_t)blockIdx.x * (blockDim.x >> 5) + wid; cell < n; cell += nwarps) {
+    const double T = Tg[cell], p = pg[cell];
+    double Yk = 0.0;
+    if (lane < ns) Yk = (layout == 1) ? Yg[(int64_t)lane * n + cell] : Yg[cell * ns + lane];
+    CellOut o;
+    warp_kinetics<JAC>(m, s, lane, Yk, T, p, o);
+    if (wdot && lane < ns) {
+      double v = m.mw[lane] * o.wmol;
+      if (layout == 1) wdot[(int64_t)lane * n + cell] = v;
+      else wdot[cell * ns + lane] = v;
+    }
+    if (rhs_out && lane < nv) rhs_out[cell * nv + lane] = o.f;
+    if (lane == 0) {
+      if (cpo) cpo[cell] = o.cp_mass;
+      if (ho) ho[cell] = o.h_mass;
+    }
+    if (JAC && jac) {
+      // Fortran (nv, nv, N): column j of this cell is contiguous; lane = row.
+      double* dst = jac + cell * (int64_t)nv * nv;
+      if (lane < nv)
+        for (int j = 0; j < nv; ++j) dst[(int64_t)j * nv + lane] = s.Jr[lane * s.ldj + j];
+    }
+    __syncwarp();
+  }
+}
+
+// ---------------------------------------------------------------- thermo
+// Mixture cp [J/kg/K] and h [J/kg] of N cells, one thread per cell
+// (f_cp / H of Lib_ThermoTransport.f90:251-271, :40-52 on NASA-7 data).
+__global__ void __launch_bounds__(SMALL_THREADS)
+k_thermo(const uint8_t* __restrict__ img, ImageLayout L, int64_t n, int layout, const double* __restrict__ Tg,
+         const double* __restrict__ Yg, double* __restrict__ cpo, double* __restrict__ ho) {
+  extern __shared__ __align__(16) uint8_t smem[];
+  stage_image(smem, img, L.bytes);
+  MechView m;
+  m.bind(L, smem);
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double T = Tg[i], lnT = log(T), invT = 1.0 / T;
+    double cpm = 0.0, hm = 0.0;
+    for (int k = 0; k < m.ns; ++k) {
+      const double y = (layout == 1) ? Yg[(int64_t)k * n + i] : Yg[i * m.ns + k];
+      SpThermo th = nasa7(m, k, T, lnT, invT);
+      cpm += y * th.cpR * m.invmw[k];
+      hm += y * th.hRT * m.invmw[k];
+    }
+    if (cpo) cpo[i] = cpm * m.r_thermo;
+    if (ho) ho[i] = hm * m.r_thermo * T;
+  }
+}
+
+// ---------------------------------------------------------------- launchers
+static int g_sms = 0;
+
+int device_sms() {
+  if (g_sms == 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&g_sms, cudaDevAttrMultiProcessorCount, dev);
+    if (g_sms <= 0) g_sms = 1;
+  }
+  return g_sms;
+}
+
+static int64_t grid_for(const void* fn, int threads, size_t smem, int64_t work_items) {
+  int per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, smem);
+  if (per_sm < 1) per_sm = 1;
+  int64_t full = (int64_t)device_sms() * per_sm;
+  int64_t need = (work_items + threads - 1) / threads;
+  if (need < 1) need = 1;
+  return need < full ? need : full;
+}
+
+size_t small_smem(const ImageLayout& L) { return L.bytes + 3 * SMALL_NSMAX * SMALL_THREADS * sizeof(double); }
+size_t warp_smem(const ImageLayout& L, bool jac) {
+  return L.bytes + (WARP_THREADS / 32) * scratch_doubles(L.nsp, L.nrpad, jac) * sizeof(double);
+}
+
+bool use_small_kernel(const ImageLayout& L) { return L.ns <= SMALL_NSMAX && L.ns <= 8; }
+
+cudaError_t launch_wdot(const uint8_t* img, const ImageLayout& L, int64_t n, int layout, const double* T,
+                        const double* p, const double* Y, double* wdot, double* cp, double* h,
+                        cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  if (use_small_kernel(L)) {
+    size_t sm = small_smem(L);
+    cudaFuncSetAttribute(k_wdot_small, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    int64_t g = grid_for((const void*)k_wdot_small, SMALL_THREADS, sm, n);
+    k_wdot_small<<<(unsigned)g, SMALL_THREADS, sm, st>>>(img, L, n, layout, T, p, Y, wdot, cp, h, 0, nullptr);
+  } else {
+    size_t sm = warp_smem(L, false);
+    cudaFuncSetAttribute(k_wdot_warp<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    int64_t g = grid_for((const void*)k_wdot_warp<false>, WARP_THREADS, sm, n * 32);
+    k_wdot_warp<false><<<(unsigned)g, WARP_THREADS, sm, st>>>(img, L, n, layout, T, p, Y, wdot, cp, h,
+                                                               nullptr, nullptr);
+  }
+  count_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t launch_thermo(const uint8_t* img, const ImageLayout& L, int64_t n, int layout, const double* T,
+                          const double* Y, double* cp, double* h, cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  size_t sm = L.bytes;
+  cudaFuncSetAttribute(k_thermo, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  int64_t g = grid_for((const void*)k_thermo, SMALL_THREADS, sm, n);
+  k_thermo<<<(unsigned)g, SMALL_THREADS, sm, st>>>(img, L, n, layout, T, Y, cp, h);
+  count_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t launch_chemistry_source(const uint8_t* img, const ImageLayout& L, int64_t n, double* roi,
+                                    const double* T, double* omegadot, cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  size_t sm = small_smem(L);
+  cudaFuncSetAttribute(k_wdot_small, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  int64_t g = grid_for((const void*)k_wdot_small, SMALL_THREADS, sm, n);
+  k_wdot_small<<<(unsigned)g, SMALL_THREADS, sm, st>>>(img, L, n, 0, T, nullptr, nullptr, omegadot, nullptr,
+                                                         nullptr, 1, roi);
+  count_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t launch_wdot_jac(const uint8_t* img, const ImageLayout& L, int64_t n, int layout, const double* T,
+                            const double* p, const double* Y, double* wdot, double* jac, cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  size_t sm = warp_smem(L, true);
+  cudaFuncSetAttribute(k_wdot_warp<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  int64_t g = grid_for((const void*)k_wdot_warp<true>, WARP_THREADS, sm, n * 32);
+  k_wdot_warp<true><<<(unsigned)g, WARP_THREADS, sm, st>>>(img, L, n, layout, T, p, Y, wdot, nullptr, nullptr,
+                                                            jac, nullptr);
+  count_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t launch_rhs(const uint8_t* img, const ImageLayout& L, int64_t n, const double* T, const double* p,
+                       const double* Y, double* f, cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  size_t sm = warp_smem(L, false);
+  cudaFuncSetAttribute(k_wdot_warp<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  int64_t g = grid_for((const void*)k_wdot_warp<false>, WARP_THREADS, sm, n * 32);
+  k_wdot_warp<false><<<(unsigned)g, WARP_THREADS, sm, st>>>(img, L, n, 0, T, p, Y, nullptr, nullptr, nullptr,
+                                                             nullptr, f);
+  count_launch();
+  return cudaGetLastError();
+}
+
+}  // namespace flint

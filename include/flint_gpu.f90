@@ -1,0 +1,92 @@
+!> FLINT_GPU -- ISO_C_BINDING interface to the GB300 chemistry library (flint_gpu.h).
+!>
+!> A FLINT caller replaces
+!>   read_idealgas_thermo / read_chemistry / Assign_Mechanism  -> flint_mech_create
+!>   loop over cells of chemistry_source(roi, T, omegadot)    -> flint_chemistry_source_batch
+!>   loop over cells of run_odesolver(neq, tin, tout, Z, rhs_native, err)
+!>                                                            -> flint_reactor_advance_host
+!>   free_chemistry_data                                       -> flint_mech_destroy
+!> Arrays are Fortran column-major: roi(ns, ncells), Y(ns, ncells),
+!> jac(ns+1, ns+1, ncells) -- the library's FLINT_CELL_MAJOR layout.
+!> No Fortran compiler exists in the build images of this project, so this
+!> module is checked only by the symbol test (tests/test_abi_cpu.py).
+module FLINT_GPU
+  use iso_c_binding
+  implicit none
+
+  integer(c_int), parameter :: FLINT_OK = 0
+  integer(c_int), parameter :: FLINT_CELL_MAJOR = 0, FLINT_SPECIES_MAJOR = 1
+
+  type, bind(C) :: flint_mech_desc
+    integer(c_int) :: ns, nr
+    type(c_ptr) :: mw, nasa7, rtype, reversible, arrh, arrh0, troe
+    type(c_ptr) :: rsp, rnu, rord, psp, pnu, eff
+    real(c_double) :: r_eos, r_thermo, p_ref
+  end type flint_mech_desc
+
+  type, bind(C) :: flint_reactor_opts
+    real(c_double) :: rtol, atol
+    integer(c_int) :: max_steps, max_order, constant_volume, reserved
+    real(c_double) :: tmin, tmax
+  end type flint_reactor_opts
+
+  interface
+    integer(c_int) function flint_mech_create(desc, mech) bind(C, name='flint_mech_create')
+      import :: c_int, c_ptr, flint_mech_desc
+      type(flint_mech_desc), intent(in) :: desc
+      type(c_ptr), intent(out) :: mech
+    end function
+
+    integer(c_int) function flint_mech_destroy(mech) bind(C, name='flint_mech_destroy')
+      import :: c_int, c_ptr
+      type(c_ptr), value :: mech
+    end function
+
+    type(c_ptr) function flint_last_error() bind(C, name='flint_last_error')
+      import :: c_ptr
+    end function
+
+    integer(c_int) function flint_chemistry_source_batch(mech, n, roi, temp, omegadot, stream) &
+        bind(C, name='flint_chemistry_source_batch')
+      import :: c_int, c_int64_t, c_ptr
+      type(c_ptr), value :: mech, roi, temp, omegadot, stream
+      integer(c_int64_t), value :: n
+    end function
+
+    integer(c_int) function flint_wdot_batch_host(mech, n, layout, temp, p, Y, wdot, cp, h) &
+        bind(C, name='flint_wdot_batch_host')
+      import :: c_int, c_int64_t, c_double, c_ptr
+      type(c_ptr), value :: mech
+      integer(c_int64_t), value :: n
+      integer(c_int), value :: layout
+      real(c_double), intent(in) :: temp(*), p(*), Y(*)
+      real(c_double), intent(out) :: wdot(*), cp(*), h(*)
+    end function
+
+    integer(c_int) function flint_wdot_jac_batch_host(mech, n, layout, temp, p, Y, wdot, jac) &
+        bind(C, name='flint_wdot_jac_batch_host')
+      import :: c_int, c_int64_t, c_double, c_ptr
+      type(c_ptr), value :: mech
+      integer(c_int64_t), value :: n
+      integer(c_int), value :: layout
+      real(c_double), intent(in) :: temp(*), p(*), Y(*)
+      real(c_double), intent(out) :: wdot(*), jac(*)
+    end function
+
+    integer(c_int) function flint_reactor_advance_host(mech, n, temp, p, Y, dt, opts, status, nsteps) &
+        bind(C, name='flint_reactor_advance_host')
+      import :: c_int, c_int64_t, c_double, c_ptr, flint_reactor_opts
+      type(c_ptr), value :: mech
+      integer(c_int64_t), value :: n
+      real(c_double), intent(inout) :: temp(*), Y(*)
+      real(c_double), intent(in) :: p(*), dt(*)
+      type(flint_reactor_opts), intent(in) :: opts
+      integer(c_int), intent(out) :: status(*), nsteps(*)
+    end function
+
+    subroutine flint_reactor_default_opts(opts) bind(C, name='flint_reactor_default_opts')
+      import :: flint_reactor_opts
+      type(flint_reactor_opts), intent(out) :: opts
+    end subroutine
+  end interface
+end module FLINT_GPU

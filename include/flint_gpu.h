@@ -1,0 +1,187 @@
+/*
+ * flint_gpu.h -- C-ABI of the GB300 (sm_103a) per-cell chemistry library.
+ *
+ * This is the drop-in boundary below FLINT's Fortran API.  Every entry point is
+ * plain C: opaque handles, plain pointers, 64-bit sizes, an explicit CUDA
+ * stream passed as `void*` (NULL = legacy default stream), and an `int` status
+ * (FLINT_OK = 0).  No C++ exception and no torch type crosses it.  The Fortran
+ * interface block a FLINT caller binds is include/flint_gpu.f90.
+ *
+ * Reference interfaces replaced (paths within the FLINT project):
+ *   read_idealgas_thermo(folder)          src/lib/Load_ThermoTransport.f90:7
+ *   read_chemistry(folder, mech_name)     src/lib/Load_Chemistry.f90:7
+ *   Assign_Mechanism(name)                src/lib/Lib_Chemistry_wdot.f90:24
+ *   chemistry_source(roi, temp, omegadot) src/lib/Lib_Chemistry_wdot.f90:6-20
+ *   general(roi, temp, omegadot)          src/lib/Lib_Chemistry_wdot.f90:96-220
+ *   f_cp / H (mixture cp and h)           src/lib/Lib_ThermoTransport.f90:251-271, :40-52
+ *   rhs_native(nz, time, Z, F)            src/lib/Lib_Chemistry_rhs.f90:15-52
+ *   setup_odesolver / run_odesolver       OSlo, call sites src/test/Fortran/test-batchF.f90:81,105
+ *   free_chemistry_data()                 src/lib/Lib_Chemistry_data.f90:168
+ *
+ * Device-pointer entry points take device (or managed) memory and are
+ * asynchronous on `stream`; the *_host variants take host memory, stage it
+ * through device buffers owned by the handle and return after the results are
+ * back on the host.
+ *
+ * Units: SI with kmol.  T [K], p [Pa], Y mass fractions, rho_i [kg/m^3],
+ * wdot [kg/m^3/s], cp [J/kg/K], h [J/kg].
+ */
+#ifndef FLINT_GPU_H
+#define FLINT_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- status */
+enum {
+  FLINT_OK = 0,
+  FLINT_ERR_ARG = 1,        /* bad argument (NULL pointer, size, layout)       */
+  FLINT_ERR_CUDA = 2,       /* a CUDA runtime call failed                       */
+  FLINT_ERR_MECH = 3,       /* mechanism outside what the kernels support       */
+  FLINT_ERR_IO = 4,         /* input file missing or malformed                  */
+  FLINT_ERR_NOMEM = 5       /* device allocation failed                         */
+};
+
+/* Per-cell status written by the reactor (one int per cell). */
+enum {
+  FLINT_CELL_OK = 0,
+  FLINT_CELL_T_OUT_OF_RANGE = 1,  /* T outside the mechanism's valid range     */
+  FLINT_CELL_NAN_INPUT = 2,       /* NaN/Inf or non-positive p in the input    */
+  FLINT_CELL_MAX_STEPS = 3,       /* internal step limit reached               */
+  FLINT_CELL_NEWTON_FAIL = 4,     /* repeated Newton convergence failures      */
+  FLINT_CELL_ERRTEST_FAIL = 5,    /* repeated local error test failures        */
+  FLINT_CELL_SURROGATE_REJECTED = 6 /* surrogate rejected; cell re-solved      */
+};
+
+/* Layout of per-species arrays (Y, rho_i, wdot) of N cells. */
+enum {
+  FLINT_CELL_MAJOR = 0,     /* Fortran (ns, N): a[cell*ns + k]                   */
+  FLINT_SPECIES_MAJOR = 1   /* structure of arrays (N, ns): a[k*N + cell]        */
+};
+
+/* Reaction forms (the reference's rxn_type plus the three-body flag). */
+enum {
+  FLINT_RXN_ELEMENTARY = 0,
+  FLINT_RXN_THREEBODY = 1,
+  FLINT_RXN_LINDEMANN = 2,
+  FLINT_RXN_TROE = 3
+};
+
+#define FLINT_MAXSP_PER_SIDE 3
+
+typedef struct flint_mech_s* flint_mech_t;
+
+/* Analytic mechanism description: NASA-7 thermo + Arrhenius / third-body /
+ * falloff kinetics with reverse rates from Kc (Gibbs).  All arrays are host
+ * memory, row-major, read once by flint_mech_create. */
+typedef struct {
+  int ns;                 /* species                                        */
+  int nr;                 /* reactions                                      */
+  const double* mw;       /* [ns] molar mass, kg/kmol                       */
+  const double* nasa7;    /* [ns][17]: Tlow, Tmid, Thigh, a_low[7], a_high[7] */
+  const int* rtype;       /* [nr] FLINT_RXN_*                               */
+  const int* reversible;  /* [nr] 1 = reverse rate from Kc, 0 = irreversible */
+  const double* arrh;     /* [nr][3] A (SI kmol), b, Ea/R [K]; high-P limit for falloff */
+  const double* arrh0;    /* [nr][3] low-pressure limit (falloff only)       */
+  const double* troe;     /* [nr][4] a, T3, T1, T2 (T2 = 0: term absent)     */
+  const int* rsp;         /* [nr][3] reactant species (-1 = unused slot)     */
+  const double* rnu;      /* [nr][3] reactant stoichiometric coefficients    */
+  const double* rord;     /* [nr][3] forward orders (= rnu unless custom)    */
+  const int* psp;         /* [nr][3] product species (-1 = unused slot)      */
+  const double* pnu;      /* [nr][3] product stoichiometric coefficients     */
+  const double* eff;      /* [nr][ns] third-body efficiencies (types 1-3)    */
+  double r_eos;           /* gas constant of the EOS and energy equation (FLINT Runiv 8314.51) */
+  double r_thermo;        /* gas constant of NASA-7 -> cp,h,s and Kc (8314.46261815324) */
+  double p_ref;           /* standard pressure of Kc, Pa (101325)            */
+} flint_mech_desc;
+
+/* Integrator options of the batched 0D reactor. */
+typedef struct {
+  double rtol;            /* relative tolerance (all components)            */
+  double atol;            /* absolute tolerance (all components)            */
+  int max_steps;          /* internal step limit per cell (bounded loop)    */
+  int max_order;          /* BDF order limit, 1..5                           */
+  int constant_volume;    /* 0 = constant pressure (default), 1 = constant volume */
+  int reserved;
+  double tmin, tmax;      /* valid temperature range; outside -> T_OUT_OF_RANGE */
+} flint_reactor_opts;
+
+/* ------------------------------------------------------------ life cycle */
+/* Replaces read_idealgas_thermo + read_chemistry + Assign_Mechanism for an
+ * analytic mechanism: copies the description to device memory owned by *out. */
+int flint_mech_create(const flint_mech_desc* desc, flint_mech_t* out);
+/* Replaces free_chemistry_data (Lib_Chemistry_data.f90:168). */
+int flint_mech_destroy(flint_mech_t mech);
+/* Text of the last error on the calling thread ("" if none). */
+const char* flint_last_error(void);
+/* Library version string. */
+const char* flint_version(void);
+/* Species / reaction counts of a handle. */
+int flint_mech_sizes(flint_mech_t mech, int* ns, int* nr);
+
+/* -------------------------------------------------------------- thermo */
+/* Mixture cp [J/kg/K] and h [J/kg] for N cells (NASA-7, f_cp / H of
+ * Lib_ThermoTransport.f90:251-271, :40-52).  Either output may be NULL. */
+int flint_thermo_batch(flint_mech_t mech, int64_t n, int layout, const double* T,
+                       const double* Y, double* cp, double* h, void* stream);
+
+/* ----------------------------------------------------------- source term */
+/* Net mass production rates wdot [kg/m^3/s] of N cells at (T, p, Y), plus the
+ * mixture cp and h (either may be NULL).  Replaces the per-cell
+ * chemistry_source loop of a CFD caller (Lib_Chemistry_wdot.f90:6-20). */
+int flint_wdot_batch(flint_mech_t mech, int64_t n, int layout, const double* T,
+                     const double* p, const double* Y, double* wdot, double* cp,
+                     double* h, void* stream);
+
+/* chemistry_source(roi, temp, omegadot) over N cells, cell-major rho_i input
+ * (Fortran (ns, N)).  Negative rho_i are clamped to zero in place, as the
+ * reference mechanisms do (WD.f90:19, Lib_Chemistry_rhs.f90:37-39). */
+int flint_chemistry_source_batch(flint_mech_t mech, int64_t n, double* roi,
+                                 const double* T, double* omegadot, void* stream);
+
+/* wdot and the analytic Jacobian of the constant-pressure reactor right-hand
+ * side, J = d(dY/dt, dT/dt)/d(Y, T), (ns+1)^2 per cell stored column-major
+ * per cell: jac[cell*(ns+1)^2 + col*(ns+1) + row] (Fortran (ns+1, ns+1, N)). */
+int flint_wdot_jac_batch(flint_mech_t mech, int64_t n, int layout, const double* T,
+                         const double* p, const double* Y, double* wdot, double* jac,
+                         void* stream);
+
+/* Constant-pressure reactor right-hand side f = (dY/dt, dT/dt), cell-major
+ * (ns+1) per cell. */
+int flint_rhs_constp_batch(flint_mech_t mech, int64_t n, const double* T, const double* p,
+                           const double* Y, double* f, void* stream);
+
+/* ---------------------------------------------------------------- reactor */
+/* Advance N independent 0D reactors over their own dt (setup_odesolver +
+ * run_odesolver of OSlo as called at test-batchF.f90:81,105) with a batched
+ * variable-order BDF / Newton integrator and dense LU of the (ns+1) system.
+ * T and Y (cell-major) are updated in place; status[cell] gets FLINT_CELL_*,
+ * nsteps[cell] the internal steps taken (either may be NULL). */
+int flint_reactor_advance(flint_mech_t mech, int64_t n, double* T, const double* p,
+                          double* Y, const double* dt, const flint_reactor_opts* opts,
+                          int* status, int* nsteps, void* stream);
+
+/* Default options: rtol 1e-8, atol 1e-14, 20000 steps, order 5, constant p. */
+void flint_reactor_default_opts(flint_reactor_opts* opts);
+
+/* ------------------------------------------------------------ host forms */
+int flint_wdot_batch_host(flint_mech_t mech, int64_t n, int layout, const double* T,
+                          const double* p, const double* Y, double* wdot, double* cp,
+                          double* h);
+int flint_wdot_jac_batch_host(flint_mech_t mech, int64_t n, int layout, const double* T,
+                              const double* p, const double* Y, double* wdot, double* jac);
+int flint_reactor_advance_host(flint_mech_t mech, int64_t n, double* T, const double* p,
+                               double* Y, const double* dt, const flint_reactor_opts* opts,
+                               int* status, int* nsteps);
+
+/* Number of kernels the library launched since load (instrumentation). */
+int64_t flint_kernel_launch_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FLINT_GPU_H */

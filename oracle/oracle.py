@@ -1,0 +1,115 @@
+"""ctypes wrapper of the FP64 CPU oracle (oracle/flint_oracle.c).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and
+bench.py's CPU-baseline leg, never by the flint_gb300 package.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+from flint_gb300.native import MechDesc, ReactorOpts, mech_desc, ptr
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+SO = os.path.join(HERE, "_build", "liboracle.so")
+
+_lib = None
+
+
+def build():
+    subprocess.run(["make", "-s", "-C", HERE], check=True)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(SO) or os.path.getmtime(SO) < os.path.getmtime(os.path.join(HERE, "flint_oracle.c")):
+            build()
+        L = C.CDLL(SO)
+        dp, vp, i64 = C.POINTER(C.c_double), C.c_void_p, C.c_int64
+        md = C.POINTER(MechDesc)
+        L.orc_species_thermo.argtypes = [md, C.c_double, vp, vp, vp, vp]
+        L.orc_rate_constants.argtypes = [md, C.c_double, vp, vp, vp, vp]
+        L.orc_wdot_cell.argtypes = [md, C.c_double, C.c_double, vp, vp, vp, vp, vp]
+        L.orc_rhs_constp_cell.argtypes = [md, C.c_double, C.c_double, vp, vp]
+        L.orc_jac_cell.argtypes = [md, C.c_double, C.c_double, vp, vp, vp, vp]
+        L.orc_wdot_batch.argtypes = [md, i64, C.c_int, vp, vp, vp, vp, vp, vp, vp, C.c_int]
+        L.orc_wdot_jac_batch.argtypes = [md, i64, C.c_int, vp, vp, vp, vp, vp, vp, C.c_int]
+        L.orc_reactor_advance.argtypes = [md, i64, vp, vp, vp, vp, C.POINTER(ReactorOpts), vp, vp, C.c_int]
+        L.orc_max_threads.restype = C.c_int
+        _lib = L
+    return _lib
+
+
+def _vp(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+class Oracle:
+    """Oracle bound to one mechanism."""
+
+    def __init__(self, mech):
+        self.mech = mech
+        self.desc, self._keep = mech_desc(mech)
+        self.ns, self.nr = mech.ns, mech.nr
+        self.L = lib()
+
+    def species_thermo(self, T):
+        ns = self.ns
+        out = [np.zeros(ns) for _ in range(4)]
+        self.L.orc_species_thermo(C.byref(self.desc), float(T), *[_vp(o) for o in out])
+        return out  # cpR, hRT, sR, dcpR
+
+    def rate_constants(self, T):
+        nr = self.nr
+        out = [np.zeros(nr) for _ in range(4)]
+        self.L.orc_rate_constants(C.byref(self.desc), float(T), *[_vp(o) for o in out])
+        return out  # kf, Kc, k0, fcent
+
+    def rhs(self, T, p, Y):
+        f = np.zeros(self.ns + 1)
+        Y = np.ascontiguousarray(Y, dtype=np.float64)
+        self.L.orc_rhs_constp_cell(C.byref(self.desc), float(T), float(p), _vp(Y), _vp(f))
+        return f
+
+    def jac(self, T, p, Y):
+        n = self.ns + 1
+        f = np.zeros(n); J = np.zeros(n * n); Js = np.zeros(n * n)
+        Y = np.ascontiguousarray(Y, dtype=np.float64)
+        self.L.orc_jac_cell(C.byref(self.desc), float(T), float(p), _vp(Y), _vp(f), _vp(J), _vp(Js))
+        return f, J.reshape(n, n).T.copy(), Js.reshape(n, n).T.copy()  # J[row, col]
+
+    def wdot_batch(self, T, p, Y, layout=0, nthreads=0):
+        T = np.ascontiguousarray(T, dtype=np.float64); p = np.ascontiguousarray(p, dtype=np.float64)
+        Y = np.ascontiguousarray(Y, dtype=np.float64)
+        n = T.shape[0]
+        w = np.zeros(n * self.ns); ws = np.zeros(n * self.ns); cp = np.zeros(n); h = np.zeros(n)
+        self.L.orc_wdot_batch(C.byref(self.desc), n, layout, _vp(T), _vp(p), _vp(Y), _vp(w), _vp(ws),
+                              _vp(cp), _vp(h), nthreads)
+        return w, ws, cp, h
+
+    def wdot_jac_batch(self, T, p, Y, layout=0, nthreads=0, scale=True):
+        T = np.ascontiguousarray(T, dtype=np.float64); p = np.ascontiguousarray(p, dtype=np.float64)
+        Y = np.ascontiguousarray(Y, dtype=np.float64)
+        n = T.shape[0]
+        nn = (self.ns + 1) ** 2
+        w = np.zeros(n * self.ns); J = np.zeros(n * nn); Js = np.zeros(n * nn) if scale else None
+        self.L.orc_wdot_jac_batch(C.byref(self.desc), n, layout, _vp(T), _vp(p), _vp(Y), _vp(w), _vp(J),
+                                  _vp(Js), nthreads)
+        return w, J, Js
+
+    def reactor_advance(self, T, p, Y, dt, opts, nthreads=0):
+        T = np.array(T, dtype=np.float64); p = np.ascontiguousarray(p, dtype=np.float64)
+        Y = np.array(Y, dtype=np.float64); dt = np.ascontiguousarray(dt, dtype=np.float64)
+        n = T.shape[0]
+        st = np.zeros(n, dtype=np.int32); ns_ = np.zeros(n, dtype=np.int32)
+        self.L.orc_reactor_advance(C.byref(self.desc), n, _vp(T), _vp(p), _vp(Y), _vp(dt), C.byref(opts),
+                                   _vp(st), _vp(ns_), nthreads)
+        return T, Y, st, ns_
+
+    @staticmethod
+    def max_threads():
+        return lib().orc_max_threads()

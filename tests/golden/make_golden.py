@@ -1,0 +1,156 @@
+"""Generate the committed golden fixtures and mechanism data from the FLINT tree.
+
+Run once in a container where the reference tree is mounted:
+
+    python tests/golden/make_golden.py /root/reference
+
+It writes, from the reference's own input files only (nothing is computed here
+except unit conversion of YAML rate parameters into the IR):
+
+* tests/golden/wd_arrhenius.json   sampled rows of test/WD/INPUT/chemistry-Arrhenius.dat
+* tests/golden/pelucchi_troe.json  sampled rows of test/Pelucchi/INPUT/chemistry-Troe.dat
+* tests/golden/pelucchi_lind.json  sampled rows of test/Pelucchi/INPUT/chemistry-Lindemann.dat
+* tests/golden/pelucchi_thermo.json sampled rows of test/Pelucchi/INPUT/thermo.dat
+* tests/golden/mech_pelucchi.json  the Pelucchi YAML as a mechanism IR
+* tests/golden/wd_info.json        WD chemistry-info.txt stoichiometry + phase.txt
+* flint_gb300/data/mech_c1.json    the 2-step CH4/air mechanism: WD reactions 1-2
+                                   (test/WD/INPUT/WD.yaml) with NASA-7 data of CH4, O2,
+                                   CO, CO2, H2O (TSR-Rich-31.yaml) and N2 (troyes.yaml),
+                                   molar masses from the phase.txt files
+* flint_gb300/data/chon_species.json  names + compositions of the C/H/O/N species in
+                                   the in-tree YAML files (species pool of the
+                                   synthetic mechanisms)
+
+The GPU machine never reads the reference tree; it reads these files.
+"""
+from __future__ import annotations
+
+import glob
+import json
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, REPO)
+
+from flint_gb300 import mech as M  # noqa: E402
+from flint_gb300 import yamlsub  # noqa: E402
+
+
+def read_tecplot_points(path):
+    """Tecplot ASCII POINT zones -> list of (zone title, rows ndarray)."""
+    zones, cur = [], None
+    with open(path) as f:
+        for ln in f:
+            s = ln.strip()
+            if s.startswith("ZONE"):
+                cur = [s.split('"')[1], []]
+                zones.append(cur)
+            elif s and cur is not None and (s[0].isdigit() or s[0] in "+-."):
+                cur[1].append([float(x) for x in s.split()])
+    return [(z, np.array(r)) for z, r in zones]
+
+
+def sample_rows(rows, temps):
+    out = []
+    for T in temps:
+        i = int(round(T - rows[0, 0]))
+        assert rows[i, 0] == T, (T, rows[i, 0])
+        out.append(rows[i].tolist())
+    return out
+
+
+def main(ref):
+    test = os.path.join(ref, "test")
+    gold = HERE
+    data = os.path.join(REPO, "flint_gb300", "data")
+    os.makedirs(data, exist_ok=True)
+
+    # ---- WD rate table (kf, kb per reaction; T = 1..15000) -------------------
+    wd = read_tecplot_points(os.path.join(test, "WD/INPUT/chemistry-Arrhenius.dat"))
+    temps = sorted(set([300.0, 500.0, 999.0, 1000.0, 1001.0, 1500.0, 2000.0, 2500.0, 3000.0, 5000.0]
+                       + [float(t) for t in range(250, 3001, 125)]))
+    json.dump({"source": "test/WD/INPUT/chemistry-Arrhenius.dat",
+               "columns": ["T", "kf", "kb"],
+               "zones": [{"zone": z, "rows": sample_rows(r, temps)} for z, r in wd]},
+              open(os.path.join(gold, "wd_arrhenius.json"), "w"), indent=0)
+
+    # ---- Pelucchi falloff + thermo tables ------------------------------------
+    P = os.path.join(test, "Pelucchi/INPUT")
+    temps_p = sorted(set([float(t) for t in range(300, 3000, 97)] + [999.0, 1000.0, 1001.0, 2999.0]))
+    for fname, key, cols in (("chemistry-Troe.dat", "pelucchi_troe", ["T", "k_inf", "k_0", "k_c", "F_cent"]),
+                             ("chemistry-Lindemann.dat", "pelucchi_lind", ["T", "k_inf", "k_0", "k_c"])):
+        zs = read_tecplot_points(os.path.join(P, fname))
+        json.dump({"source": "test/Pelucchi/INPUT/" + fname, "columns": cols,
+                   "zones": [{"zone": z, "rows": sample_rows(r, temps_p)} for z, r in zs]},
+                  open(os.path.join(gold, key + ".json"), "w"), indent=0)
+    zs = read_tecplot_points(os.path.join(P, "thermo.dat"))
+    json.dump({"source": "test/Pelucchi/INPUT/thermo.dat", "columns": ["T", "Cp", "Enthalpy", "Entropy", "dCp"],
+               "zones": [{"zone": z, "rows": sample_rows(r, temps_p)} for z, r in zs]},
+              open(os.path.join(gold, "pelucchi_thermo.json"), "w"), indent=0)
+    mp = M.from_yaml(os.path.join(P, "pelucchi.yaml"), phase_mw=M.read_phase_txt(os.path.join(P, "phase.txt")))
+    with open(os.path.join(gold, "mech_pelucchi.json"), "w") as f:
+        f.write(mp.to_json())
+
+    # ---- WD chemistry-info (general-loop stoichiometry) ----------------------
+    info = open(os.path.join(test, "WD/INPUT/chemistry-info.txt")).read().splitlines()
+    json.dump({"source": "test/WD/INPUT/chemistry-info.txt + phase.txt",
+               "info_lines": info,
+               "phase": M.read_phase_txt(os.path.join(test, "WD/INPUT/phase.txt"))},
+              open(os.path.join(gold, "wd_info.json"), "w"), indent=0)
+
+    # ---- C1 mechanism ---------------------------------------------------------
+    rich = yamlsub.load(os.path.join(test, "TSR-Rich-31/INPUT/TSR-Rich-31.yaml"))
+    troy = yamlsub.load(os.path.join(test, "Troyes/INPUT/troyes.yaml"))
+    wdy = yamlsub.load(os.path.join(test, "WD/INPUT/WD.yaml"))
+    mw = M.read_phase_txt(os.path.join(test, "WD/INPUT/phase.txt"))
+    mw.update({"N2": M.read_phase_txt(os.path.join(P, "phase.txt"))["N2"]})
+    spd = {s["name"]: s for s in rich["species"]}
+    spd["N2"] = [s for s in troy["species"] if s["name"] == "N2"][0]
+    names = ["CH4", "O2", "CO", "CO2", "H2O", "N2"]
+    species = []
+    for n in names:
+        th = spd[n]["thermo"]
+        tr = th["temperature-ranges"]
+        species.append(M.Species(n, mw[n], dict(spd[n]["composition"]), float(tr[0]), float(tr[1]),
+                                 float(tr[2]), [float(x) for x in th["data"][0]],
+                                 [float(x) for x in th["data"][1]]))
+    # WD reactions 1-2 with the IR unit conversion of from_yaml
+    conc_f, eaf = M._unit_factors(wdy["units"])
+    reactions = []
+    for r in wdy["reactions"][:2]:
+        eq = r["equation"]
+        lhs, arrow, rhs = M._ARROW_RE.split(eq)
+        reac, _, _ = M._parse_side(lhs)
+        prod, _, _ = M._parse_side(rhs)
+        orders = {k: float(v) for k, v in r["orders"].items()}
+        forder = sum(orders.get(k, v) for k, v in reac.items())
+        A, b, E = M._rate(r["rate-constant"], conc_f, eaf, forder)
+        # WD.f90:31-34 writes the orders as default-real (single precision)
+        # literals, coi(1)**0.70: the compiled exponent is float32(0.70).
+        orders = {k: float(np.float32(v)) for k, v in orders.items()}
+        reactions.append(M.Reaction(eq, M.TYPE_ELEMENTARY, reac, prod, orders, arrow != "=>", A, b, E))
+    c1 = M.Mechanism("CH4-air-2step", species, reactions, ["C", "H", "O", "N"])
+    with open(os.path.join(data, "mech_c1.json"), "w") as f:
+        f.write(c1.to_json())
+
+    # ---- C/H/O/N species pool -------------------------------------------------
+    pool = {}
+    for fy in sorted(glob.glob(os.path.join(test, "*/INPUT/*.yaml"))):
+        d = yamlsub.load(fy)
+        for s in d["species"]:
+            comp = s["composition"]
+            if set(comp) <= {"C", "H", "O", "N"} and s["name"] not in pool:
+                pool[s["name"]] = {k: int(v) for k, v in comp.items()}
+    order = [s for s in rich["phases"][0]["species"]] + sorted(k for k in pool if k not in rich["phases"][0]["species"])
+    json.dump({"source": "C/H/O/N species of test/*/INPUT/*.yaml (TSR-Rich-31 order first)",
+               "species": [{"name": n, "composition": pool[n]} for n in order]},
+              open(os.path.join(data, "chon_species.json"), "w"), indent=1)
+    print("wrote fixtures")
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")

@@ -1,0 +1,48 @@
+"""CPU-side checks of the C-ABI library: it loads and exports every entry point
+declared in include/flint_gpu.h (no compute call: there is no GPU here)."""
+import ctypes
+import os
+import re
+
+import pytest
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    txt = open(os.path.join(REPO, "include", "flint_gpu.h")).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    return sorted(set(re.findall(r"\b(flint_[a-z0-9_]+)\s*\(", txt)))
+
+
+def test_header_declares_entry_points():
+    syms = declared_symbols()
+    for s in ("flint_mech_create", "flint_wdot_batch", "flint_wdot_jac_batch", "flint_reactor_advance",
+              "flint_chemistry_source_batch", "flint_last_error"):
+        assert s in syms
+
+
+def test_library_exports_every_declared_symbol():
+    from flint_gb300 import native
+    if not os.path.exists(native.LIB_PATH):
+        from flint_gb300 import build
+        build.build_all()
+    lib = ctypes.CDLL(native.LIB_PATH)
+    missing = [s for s in declared_symbols() if not hasattr(lib, s)]
+    assert not missing, missing
+
+
+def test_fortran_interface_binds_declared_symbols():
+    f90 = open(os.path.join(REPO, "include", "flint_gpu.f90")).read()
+    bound = set(re.findall(r"bind\(C,\s*name='(flint_[a-z0-9_]+)'\)", f90))
+    assert bound, "no bind(C) interfaces"
+    assert bound <= set(declared_symbols())
+
+
+def test_error_reporting_without_gpu():
+    """Argument checks run on the host and report through flint_last_error."""
+    from flint_gb300 import native
+    L = native.lib()
+    rc = L.flint_mech_create(None, None)
+    assert rc == 1
+    assert b"NULL" in L.flint_last_error()

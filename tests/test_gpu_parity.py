@@ -1,0 +1,180 @@
+"""GPU parity: the CUDA library through the C-ABI against the FP64 oracle.
+
+Tolerances: net production rates and Jacobian entries agree with the oracle to
+1e-12 relative to the absolute sum of their terms (the scale the oracle
+accumulates); mixture cp and h to 1e-13 relative.  The reactor is compared by
+its own tolerance: both the GPU and the oracle run against a
+tighter-tolerance oracle solution.
+"""
+import numpy as np
+import pytest
+
+from flint_gb300 import mechgen
+from flint_gb300.api import Chemistry, CELL_MAJOR, SPECIES_MAJOR
+from flint_gb300.mech import Mechanism
+from oracle.oracle import Oracle
+from flint_gb300.native import reactor_opts
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+RTOL_WDOT = 1e-12
+
+
+def cuda(*arrs):
+    return [torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in arrs]
+
+
+def wdot_err(w, w_ref, scale):
+    return np.max(np.abs(w - w_ref) / (scale + 1e-300)) if w.size else 0.0
+
+
+@pytest.fixture(scope="module")
+def c1():
+    return Chemistry.from_config("c1")
+
+
+@pytest.fixture(scope="module")
+def c2():
+    return Chemistry.from_config("c2")
+
+
+@pytest.mark.parametrize("n", [65536, 1, 33, 1000])
+def test_c1_wdot_cp_h(c1, n):
+    orc = Oracle(c1.mech)
+    T, p, Y = mechgen.c1_states(n)
+    w_o, ws_o, cp_o, h_o = orc.wdot_batch(T, p, Y)
+    Tt, pt, Yt = cuda(T, p, Y)
+    cp, h = torch.empty_like(Tt), torch.empty_like(Tt)
+    w, _, _ = c1.wdot(Tt, pt, Yt, cp=cp, h=h)
+    torch.cuda.synchronize()
+    assert wdot_err(w.cpu().numpy().ravel(), w_o, ws_o) < RTOL_WDOT
+    np.testing.assert_allclose(cp.cpu().numpy(), cp_o, rtol=1e-13)
+    hs = np.abs(h_o) + cp_o * T
+    assert np.max(np.abs(h.cpu().numpy() - h_o) / hs) < 1e-13
+
+
+def test_c1_species_major_layout(c1):
+    orc = Oracle(c1.mech)
+    T, p, Y = mechgen.c1_states(4099, seed=77)
+    w_o, ws_o, _, _ = orc.wdot_batch(T, p, Y)
+    Tt, pt, Ys = cuda(T, p, Y.T.copy())
+    w, _, _ = c1.wdot(Tt, pt, Ys, layout=SPECIES_MAJOR)
+    torch.cuda.synchronize()
+    assert wdot_err(w.cpu().numpy().T.ravel(), w_o, ws_o) < RTOL_WDOT
+
+
+def test_c1_host_path(c1):
+    orc = Oracle(c1.mech)
+    T, p, Y = mechgen.c1_states(2048, seed=5)
+    w_o, ws_o, cp_o, _ = orc.wdot_batch(T, p, Y)
+    w, cp, _ = c1.wdot(T, p, Y)
+    assert wdot_err(w.ravel(), w_o, ws_o) < RTOL_WDOT
+    np.testing.assert_allclose(cp, cp_o, rtol=1e-13)
+
+
+def test_c1_chemistry_source_clamps(c1):
+    """chemistry_source(roi, T): negative partial densities clamp to 0 in place."""
+    T, p, Y = mechgen.c1_states(512, seed=9)
+    orc = Oracle(c1.mech)
+    W = np.array([s.mw for s in c1.mech.species])
+    rho = p / (c1.mech.r_eos * T * (Y / W).sum(1))
+    roi = rho[:, None] * Y
+    roi[::7, 1] = -1e-3  # negative O2 partial density
+    roi_t, Tt = cuda(roi, T)
+    w = c1.chemistry_source(roi_t, Tt)
+    torch.cuda.synchronize()
+    roi_c = np.clip(roi, 0, None)
+    assert (roi_t.cpu().numpy() >= 0).all()
+    rho_c = roi_c.sum(1)
+    Yc = roi_c / rho_c[:, None]
+    pc = rho_c * c1.mech.r_eos * T * (Yc / W).sum(1)
+    w_o, ws_o, _, _ = orc.wdot_batch(T, pc, Yc)
+    assert wdot_err(w.cpu().numpy().ravel(), w_o, ws_o) < 1e-11
+
+
+@pytest.mark.parametrize("cfg", ["c2", "pelucchi"])
+def test_wdot_and_jacobian(cfg):
+    if cfg == "pelucchi":
+        import os
+        mech = Mechanism.load(os.path.join(os.path.dirname(__file__), "golden", "mech_pelucchi.json"))
+        T, p, Y = mechgen.c2_states(1500, mech, seed=11)
+    else:
+        mech = mechgen.load("c2")
+        T, p, Y = mechgen.c2_states(3000, mech)
+    chem = Chemistry(mech)
+    orc = Oracle(mech)
+    w_o, ws_o, _, _ = orc.wdot_batch(T, p, Y)
+    _, J_o, Js_o = orc.wdot_jac_batch(T, p, Y)
+    Tt, pt, Yt = cuda(T, p, Y)
+    w, _, _ = chem.wdot(Tt, pt, Yt)
+    w2 = torch.empty_like(Yt)
+    _, J = chem.wdot_jac(Tt, pt, Yt, wdot=w2)
+    torch.cuda.synchronize()
+    assert wdot_err(w.cpu().numpy().ravel(), w_o, ws_o) < RTOL_WDOT
+    assert wdot_err(w2.cpu().numpy().ravel(), w_o, ws_o) < RTOL_WDOT
+    Jg = J.cpu().numpy().ravel()
+    err = np.abs(Jg - J_o) / (Js_o + 1e-300)
+    assert err.max() < RTOL_WDOT, err.max()
+
+
+def test_empty_batch(c2):
+    Tt = torch.empty(0, dtype=torch.float64, device="cuda")
+    Yt = torch.empty((0, c2.ns), dtype=torch.float64, device="cuda")
+    w, _, _ = c2.wdot(Tt, Tt, Yt)
+    torch.cuda.synchronize()
+    assert w.shape == (0, c2.ns)
+
+
+def _reactor_case(n, seed=3):
+    mech = mechgen.load("c2")
+    T, p, Y, dt = mechgen.c3_states(n, mech, seed=seed)
+    return mech, T, p, Y, dt
+
+
+def test_reactor_vs_oracle():
+    mech, T, p, Y, dt = _reactor_case(384)
+    chem = Chemistry(mech)
+    orc = Oracle(mech)
+    opts = reactor_opts()
+    T_o, Y_o, st_o, ns_o = orc.reactor_advance(T, p, Y, dt, opts)
+    T_x, Y_x, st_x, _ = orc.reactor_advance(T, p, Y, dt, reactor_opts(rtol=1e-12, atol=1e-18, max_steps=400000))
+    Tt, pt, Yt, dtt = cuda(T, p, Y, dt)
+    st, nst = chem.reactor_advance(Tt, pt, Yt, dtt)
+    torch.cuda.synchronize()
+    st, nst = st.cpu().numpy(), nst.cpu().numpy()
+    Tg, Yg = Tt.cpu().numpy(), Yt.cpu().numpy()
+    assert (st == 0).all() and (st_o == 0).all() and (st_x == 0).all()
+    # same algorithm: step counts agree closely
+    assert np.abs(nst - ns_o).max() <= max(3, 0.05 * ns_o.max())
+    # both within their tolerance of the tight solution (weighted by rtol*|y|+atol)
+    for Tv, Yv in ((Tg, Yg), (T_o, Y_o)):
+        errT = np.abs(Tv - T_x) / (1e-8 * np.abs(T_x))
+        errY = np.abs(Yv - Y_x) / (1e-8 * np.abs(Y_x) + 1e-14)
+        assert errT.max() < 200 and errY.max() < 2000, (errT.max(), errY.max())
+    # GPU and oracle agree to the integrator tolerance
+    assert np.max(np.abs(Tg - T_o) / T_o) < 1e-6
+    assert np.max(np.abs(Yg - Y_o)) < 1e-6
+
+
+def test_reactor_status_codes():
+    mech, T, p, Y, dt = _reactor_case(8, seed=4)
+    T[1] = np.nan            # NaN input
+    T[2] = 7000.0            # out of range
+    dt[3] = 0.0              # nothing to do
+    p[4] = -1.0              # bad pressure
+    chem = Chemistry(mech)
+    Tt, pt, Yt, dtt = cuda(T, p, Y, dt)
+    Y3 = Y[3].copy()
+    st, nst = chem.reactor_advance(Tt, pt, Yt, dtt)
+    torch.cuda.synchronize()
+    st = st.cpu().numpy()
+    assert st[1] == 2 and st[2] == 1 and st[3] == 0 and st[4] == 2
+    assert np.array_equal(Yt.cpu().numpy()[3], Y3)
+    # bounded work: a tiny step limit reports MAX_STEPS
+    mech, T, p, Y, dt = _reactor_case(4, seed=5)
+    Tt, pt, Yt, dtt = cuda(T, p, Y, dt)
+    st, nst = chem.reactor_advance(Tt, pt, Yt, dtt, max_steps=5)
+    torch.cuda.synchronize()
+    assert (st.cpu().numpy() == 3).all() and (nst.cpu().numpy() == 5).all()
