@@ -1,0 +1,365 @@
+"""Benchmark: batched stiff 0D constant-pressure reactor advance on one GB300.
+
+Workload (the reactor configuration of the metric): the seeded synthetic
+31-species / 160-reaction mechanism (12 third-body, 6 Troe), 262,144 cells with
+T0 ~ U(900,1600) K, p ~ U(1,20) atm, phi ~ U(0.5,2) CH4/air, per-cell
+dt = 10^U(-6,-4) s, rtol 1e-8, atol 1e-14.  One step = one advance of every
+cell over its own dt (one cell-step per cell); the state is reset from the
+initial copy at the start of each step.
+
+Metric: cell-steps/s (higher is better).
+  value  device-timed (inputs resident in HBM), CUDA events on the launch stream,
+         L2 flushed (256 MiB write) between timed steps.
+  e2e    the same through the public API with pinned host buffers: per step
+         H2D of T, p, Y, dt, the advance, D2H of T, Y and the status word.
+  roofline  the reactor kernel against the FP64 pipe: FP64 ops per launch from
+         the live work counters x per-event op counts (profiles/), over the
+         kernel's event-timed duration; peak = DFMA throughput measured in this
+         run by the library's probe kernel.
+  cpu_baseline  the FP64 oracle (OpenMP, all host cores) on a bounded sample.
+
+--impl reference times the oracle port of the reference path (FLINT's Fortran
+cannot be built: no Fortran compiler exists on these machines) on the same
+workload and prints the same JSON line with "impl": "reference".
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+import numpy as np  # noqa: E402
+
+CELLS = 262144
+METRIC = "cell-steps/s on 1 GB300: surrogate+fallback vs plain FP64 at stated T/Y error"
+# FP64 pipe ops (DADD + DMUL + 2*DFMA, thread level) per event of the reactor
+# kernel on the 31-species mechanism, from ncu counts of the standalone
+# source-term / Jacobian kernels (profiles/fp64_ops_per_event.md) plus the
+# dense LU counts of a 32x32 system.
+FP64_OPS = {"rhs": 18500.0, "jac": 36000.0, "lu": 22900.0, "solve": 2100.0}
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """Samples nvidia-smi clocks and throttle reasons during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 7:
+                continue
+            try:
+                sm.append(float(f[0])); smax.append(float(f[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[3:7]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_baseline(mech, T, p, Y, dt, target_s=12.0):
+    """Oracle reactor on all host cores over a bounded sample; cells/s."""
+    from oracle.oracle import Oracle
+    from flint_gb300.native import reactor_opts
+    orc = Oracle(mech)
+    cores = Oracle.max_threads()
+    opts = reactor_opts()
+    n = 256
+    while True:
+        t0 = time.perf_counter()
+        orc.reactor_advance(T[:n], p[:n], Y[:n], dt[:n], opts)
+        el = time.perf_counter() - t0
+        if el > 0.25 * target_s or n >= len(T):
+            break
+        n = min(len(T), int(n * max(2.0, 0.3 * target_s / max(el, 1e-3))))
+    return {"value": n / el, "unit": "cell-steps/s", "cores": cores, "kind": "port",
+            "sample": f"{n} of the {len(T)} cells (first n), FP64 oracle BDF, {el:.1f} s"}
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    from flint_gb300 import mechgen
+    mech = mechgen.load("c2")
+    T, p, Y, dt = mechgen.c3_states(args.cells, mech)
+    vals = []
+    for i in range(args.warmup + args.steps):
+        r = cpu_baseline(mech, T, p, Y, dt, target_s=args.ref_seconds)
+        if i >= args.warmup:
+            vals.append(r["value"])
+    v = statistics.mean(vals)
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "cell-steps/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * args.cells / v,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded)",
+            "config": {"workload": "reactor-c3: 31sp/160r BDF, 262144 cells, rtol 1e-8 atol 1e-14",
+                       "cells": args.cells, "note": "each step times a bounded sample and scales per cell"},
+            "cpu_baseline": {"value": v, "unit": "cell-steps/s", "cores": r["cores"], "kind": "port",
+                             "sample": r["sample"]},
+            "e2e": {"value": v, "unit": "cell-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def run_ours(args):
+    import torch
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+        torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    from flint_gb300 import mechgen
+    from flint_gb300.api import Chemistry, reactor_stats, kernel_launches
+    from flint_gb300 import native
+    mech = mechgen.load("c2")
+    n = args.cells
+    T0, p0, Y0, dt0 = mechgen.c3_states(n, mech, seed=1003 + rank)
+    chem = Chemistry(mech)
+    Td0 = torch.from_numpy(T0).to(dev)
+    Yd0 = torch.from_numpy(Y0).to(dev)
+    pd = torch.from_numpy(p0).to(dev)
+    dtd = torch.from_numpy(dt0).to(dev)
+    Td, Yd = Td0.clone(), Yd0.clone()
+    st = torch.empty(n, dtype=torch.int32, device=dev)
+    nst = torch.empty(n, dtype=torch.int32, device=dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream()
+
+    def step():
+        Td.copy_(Td0)
+        Yd.copy_(Yd0)
+        chem.reactor_advance(Td, pd, Yd, dtd, status=st, nsteps=nst)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+
+    def barrier():
+        if ws > 1:
+            torch.distributed.barrier()
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    times = []
+    launches0 = kernel_launches()
+    stats = []
+    barrier()
+    torch.cuda.synchronize()
+    wall0 = time.perf_counter()
+    for _ in range(args.steps):
+        flush.zero_()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        step()
+        e1.record(stream)
+        e1.synchronize()
+        times.append(e0.elapsed_time(e1) / 1e3)
+        stats.append(reactor_stats(chem))
+    torch.cuda.synchronize()
+    barrier()
+    wall = time.perf_counter() - wall0
+    clk = clocks.stop()
+    launches = kernel_launches() - launches0
+    status = st.cpu().numpy()
+    steps_per_cell = nst.cpu().numpy()
+    t_step = statistics.mean(times)
+    if ws > 1:
+        tt = torch.tensor([t_step], device=dev, dtype=torch.float64)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        t_step = float(tt.item())
+    value = n * ws / t_step
+
+    # ---- end to end through the public API with pinned host buffers --------
+    Th = torch.from_numpy(T0).pin_memory()
+    ph = torch.from_numpy(p0).pin_memory()
+    Yh = torch.from_numpy(Y0).pin_memory()
+    dth = torch.from_numpy(dt0).pin_memory()
+    To = torch.empty_like(Th).pin_memory()
+    Yo = torch.empty_like(Yh).pin_memory()
+    so = torch.empty(n, dtype=torch.int32).pin_memory()
+    Te, pe, Ye, dte = (torch.empty_like(x, device=dev) for x in (Th, ph, Yh, dth))
+    h2d = sum(x.numel() * x.element_size() for x in (Th, ph, Yh, dth))
+    d2h = sum(x.numel() * x.element_size() for x in (To, Yo, so))
+    e2e_times = []
+    for i in range(args.warmup + args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        Te.copy_(Th, non_blocking=True); pe.copy_(ph, non_blocking=True)
+        Ye.copy_(Yh, non_blocking=True); dte.copy_(dth, non_blocking=True)
+        chem.reactor_advance(Te, pe, Ye, dte, status=st, nsteps=nst)
+        To.copy_(Te, non_blocking=True); Yo.copy_(Ye, non_blocking=True); so.copy_(st, non_blocking=True)
+        torch.cuda.synchronize()
+        if i >= args.warmup:
+            e2e_times.append(time.perf_counter() - t0)
+    e2e_t = statistics.mean(e2e_times)
+    if ws > 1:
+        tt = torch.tensor([e2e_t], device=dev, dtype=torch.float64)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        e2e_t = float(tt.item())
+    assert np.array_equal(so.numpy(), status), "e2e run disagrees with the device-timed run"
+
+    # ---- roofline: FP64 pipe ------------------------------------------------
+    s = stats[-1]
+    ops = (s["rhs"] * FP64_OPS["rhs"] + s["jac_lu"] * (FP64_OPS["jac"] + FP64_OPS["lu"])
+           + s["newton"] * FP64_OPS["solve"])
+    peak = chem_peak_fp64()
+    achieved = ops / t_step / 1e12
+    roof = {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+            "frac": achieved / peak if peak else None, "traffic": None,
+            "kernel": "k_reactor", "peak_source": "DFMA probe kernel measured in this run (MEASURED_PEAKS.json has no FP64 figure)",
+            "ops_per_launch": ops, "events_per_launch": s}
+    line = {"metric": METRIC, "value": value, "unit": "cell-steps/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded states, seeded synthetic mechanism)",
+            "config": {"workload": "reactor-c3: 31sp/160r constant-p BDF/Newton, 262144 cells, rtol 1e-8 atol 1e-14",
+                       "cells_per_gpu": n, "mechanism": "synthetic-31sp-160r (12 third-body, 6 Troe)",
+                       "path": "plain FP64 integrator", "l2": "flushed (256 MiB write) between timed steps"},
+            "e2e": {"value": n * ws / e2e_t, "unit": "cell-steps/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h},
+            "gpu_launches": launches, "clocks": clk, "roofline": roof,
+            "cell_status": {str(k): int(v) for k, v in zip(*np.unique(status, return_counts=True))},
+            "internal_steps_per_cell": {"mean": float(steps_per_cell.mean()), "max": int(steps_per_cell.max())},
+            "wall_s_timed": wall}
+    if rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(mech, T0, p0, Y0, dt0)
+    if rank == 0:
+        print(json.dumps(line))
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+def run_kernel_workload(args):
+    """Source-term workloads: c1-wdot (65,536 states, 2-step CH4/air: wdot, cp, h)
+    and c2-wdotjac (1,048,576 states, 31 species: wdot + 32x32 Jacobian).
+    Metric states/s, device-timed, L2 flushed between steps."""
+    import torch
+    from flint_gb300 import mechgen
+    from flint_gb300.api import Chemistry, kernel_launches
+    dev = torch.device("cuda", 0)
+    if args.workload == "c1-wdot":
+        n = args.cells or 65536
+        T, p, Y = mechgen.c1_states(n)
+        chem = Chemistry.from_config("c1")
+    else:
+        n = args.cells or 1048576
+        chem = Chemistry.from_config("c2")
+        T, p, Y = mechgen.c2_states(n, chem.mech)
+    Td, pd, Yd = (torch.from_numpy(a).to(dev) for a in (T, p, Y))
+    w = torch.empty_like(Yd)
+    cp, h = torch.empty_like(Td), torch.empty_like(Td)
+    jac = torch.empty((n, chem.ns + 1, chem.ns + 1), dtype=torch.float64, device=dev) \
+        if args.workload == "c2-wdotjac" else None
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream()
+
+    def step():
+        if jac is None:
+            chem.wdot(Td, pd, Yd, wdot=w, cp=cp, h=h)
+        else:
+            chem.wdot_jac(Td, pd, Yd, wdot=w, jac=jac)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    l0 = kernel_launches()
+    times = []
+    for _ in range(args.steps):
+        flush.zero_()
+        e0 = torch.cuda.Event(enable_timing=True); e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream); step(); e1.record(stream); e1.synchronize()
+        times.append(e0.elapsed_time(e1) / 1e3)
+    t = statistics.mean(times)
+    nv = chem.ns + 1
+    bytes_per_state = 8 * (2 + 2 * chem.ns) + (8 * nv * nv if jac is not None else 16)
+    print(json.dumps({"workload": args.workload, "metric": "states/s", "value": n / t, "unit": "states/s",
+                      "ms_per_step": t * 1e3, "states": n, "steps": args.steps, "warmup": args.warmup,
+                      "gpu_launches": kernel_launches() - l0,
+                      "hbm_gbs_algorithmic": n * bytes_per_state / t / 1e9,
+                      "bytes_per_state": bytes_per_state}))
+
+
+def chem_peak_fp64():
+    """FP64 FMA throughput of this GPU [TFLOP/s], measured by the library's probe kernel."""
+    import ctypes as C
+    from flint_gb300 import native
+    L = native.lib()
+    out = C.c_double(0.0)
+    if L.flint_probe_fp64_peak(C.byref(out)) != 0:
+        return None
+    return out.value
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cells", type=int, default=None)
+    ap.add_argument("--workload", default="reactor", choices=["reactor", "c1-wdot", "c2-wdot", "c2-wdotjac"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--ref-seconds", type=float, default=10.0)
+    args = ap.parse_args()
+    if args.workload != "reactor":
+        run_kernel_workload(args)
+        return
+    args.cells = args.cells or CELLS
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

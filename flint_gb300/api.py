@@ -169,6 +169,13 @@ class Chemistry:
         return st, nst
 
 
+def reactor_stats(chem):
+    """Counters of the last reactor launch: rhs, jac_lu, newton, steps, rejected."""
+    out = (C.c_int64 * 5)()
+    native.check(chem.L.flint_reactor_stats(chem.h, out), "flint_reactor_stats")
+    return dict(zip(("rhs", "jac_lu", "newton", "steps", "rejected"), list(out)))
+
+
 def kernel_launches():
     """Kernels launched by the library in this process."""
     return native.lib().flint_kernel_launch_count()

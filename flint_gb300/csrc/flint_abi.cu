@@ -308,6 +308,21 @@ int flint_reactor_advance(flint_mech_t h, int64_t n, double* T, const double* p,
   return e == cudaSuccess ? FLINT_OK : cuda_fail(e, "flint_reactor_advance");
 }
 
+int flint_reactor_stats(flint_mech_t h, int64_t out[5]) {
+  if (!h || !out) return fail(FLINT_ERR_ARG, "NULL argument");
+  unsigned long long c[6];
+  cudaError_t e = cudaMemcpy(c, h->dcounter, sizeof c, cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_fail(e, "flint_reactor_stats");
+  for (int i = 0; i < 5; ++i) out[i] = (int64_t)c[i + 1];
+  return FLINT_OK;
+}
+
+int flint_probe_fp64_peak(double* tflops) {
+  if (!tflops) return fail(FLINT_ERR_ARG, "NULL argument");
+  cudaError_t e = probe_fp64(tflops);
+  return e == cudaSuccess ? FLINT_OK : cuda_fail(e, "flint_probe_fp64_peak");
+}
+
 // ------------------------------------------------------------------ host forms
 int flint_wdot_batch_host(flint_mech_t h, int64_t n, int layout, const double* T, const double* p, const double* Y,
                           double* wdot, double* cp, double* hm) {

@@ -8,6 +8,7 @@
 namespace flint {
 
 void count_launch();
+cudaError_t probe_fp64(double* tflops);
 int device_sms();
 
 cudaError_t launch_wdot(const uint8_t* img, const ImageLayout& L, int64_t n, int layout, const double* T,

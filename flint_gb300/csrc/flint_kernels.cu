@@ -203,6 +203,47 @@ k_thermo(const uint8_t* __restrict__ img, ImageLayout L, int64_t n, int layout, 
   }
 }
 
+// ---------------------------------------------------------------- FP64 probe
+// Independent FMA chains: the FP64 pipe's throughput, the denominator of the
+// FP64 roofline the benchmarks report.
+__global__ void k_dfma_probe(double* out, int iters, double a, double b) {
+  double x0 = threadIdx.x * 1e-3, x1 = x0 + 1.0, x2 = x0 + 2.0, x3 = x0 + 3.0;
+  double x4 = x0 + 4.0, x5 = x0 + 5.0, x6 = x0 + 6.0, x7 = x0 + 7.0;
+  for (int i = 0; i < iters; ++i) {
+    x0 = fma(x0, a, b); x1 = fma(x1, a, b); x2 = fma(x2, a, b); x3 = fma(x3, a, b);
+    x4 = fma(x4, a, b); x5 = fma(x5, a, b); x6 = fma(x6, a, b); x7 = fma(x7, a, b);
+  }
+  out[(int64_t)blockIdx.x * blockDim.x + threadIdx.x] = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+}
+
+cudaError_t probe_fp64(double* tflops) {
+  const int blocks = device_sms() * 8, threads = 256, iters = 2048;
+  double* buf = nullptr;
+  cudaError_t e = cudaMalloc(&buf, (size_t)blocks * threads * sizeof(double));
+  if (e != cudaSuccess) return e;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  k_dfma_probe<<<blocks, threads>>>(buf, 64, 0.999, 1e-3);
+  float best = 1e30f;
+  for (int rep = 0; rep < 3; ++rep) {
+    cudaEventRecord(e0);
+    k_dfma_probe<<<blocks, threads>>>(buf, iters, 0.999, 1e-3);
+    cudaEventRecord(e1);
+    cudaEventSynchronize(e1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (ms < best) best = ms;
+  }
+  count_launch();
+  e = cudaGetLastError();
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(buf);
+  *tflops = 2.0 * 8.0 * iters * (double)blocks * threads / (best * 1e-3) / 1e12;
+  return e;
+}
+
 // ---------------------------------------------------------------- launchers
 static int g_sms = 0;
 

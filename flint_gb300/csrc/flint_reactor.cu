@@ -30,7 +30,8 @@ constexpr int REACTOR_THREADS = 256;
 
 struct BdfL { double l[6][6]; };
 
-__host__ __device__ inline void bdf_coeffs(BdfL& B) {
+// l^(q)_j = coefficient of x^j in prod_{i=1..q} (1 + x/i)  (Nordsieck BDF of order q).
+static void bdf_coeffs(BdfL& B) {
   for (int q = 0; q < 6; ++q)
     for (int j = 0; j < 6; ++j) B.l[q][j] = 0.0;
   for (int q = 1; q <= 5; ++q) {
@@ -40,6 +41,13 @@ __host__ __device__ inline void bdf_coeffs(BdfL& B) {
       for (int j = i; j >= 1; --j) l[j] += l[j - 1] / (double)i;
   }
 }
+
+__constant__ BdfL c_bdf;
+
+// Work counters of the last reactor launch (device side, summed per cell):
+// [0] work-stealing cursor, [1] RHS evaluations, [2] Jacobian + LU refreshes,
+// [3] Newton iterations (LU solves), [4] accepted steps, [5] rejected attempts.
+constexpr int NCOUNTERS = 6;
 
 __device__ inline double wrms(double v, double w, bool act, int nv) {
   double t = act ? v * w : 0.0;
@@ -110,9 +118,9 @@ k_reactor(const uint8_t* __restrict__ img, ImageLayout L, int64_t n, double* __r
   const int ns = m.ns, nv = ns + 1;
   const bool act = lane < nv;
   const int ld = s.ldj;
-  BdfL B;
-  bdf_coeffs(B);
+  const BdfL& B = c_bdf;
   const int qmax = o.max_order;
+  unsigned long long n_rhs = 0, n_jac = 0, n_newt = 0, n_rej = 0;
 
   while (true) {
     unsigned long long c0 = 0;
@@ -138,6 +146,7 @@ k_reactor(const uint8_t* __restrict__ img, ImageLayout L, int64_t n, double* __r
       for (int j = 0; j < 6; ++j) { z[j] = 0.0; zs[j] = 0.0; }
       CellOut co;
       auto rhs = [&](double yv) -> double {
+        ++n_rhs;
         const double Tv = __shfl_sync(FULL, yv, ns);
         warp_kinetics<false>(m, s, lane, lane < ns ? yv : 0.0, Tv, p, co);
         __syncwarp();
@@ -184,6 +193,7 @@ k_reactor(const uint8_t* __restrict__ img, ImageLayout L, int64_t n, double* __r
           const double ypred = z[0];
           if (!have_J || need_J || fabs(gamma / gammaJ - 1.0) > 0.3 || nst >= nstJ + 20) {
             const double Tv = __shfl_sync(FULL, ypred, ns);
+            ++n_jac;
             warp_kinetics<true>(m, s, lane, lane < ns ? ypred : 0.0, Tv, p, co);
             if (act) {
               double* row = s.Jr + lane * ld;
@@ -200,6 +210,7 @@ k_reactor(const uint8_t* __restrict__ img, ImageLayout L, int64_t n, double* __r
           double delp = 0.0;
           const double Eq = 1.0 / ((double)(q + 1) * l1 + 1.0);
           for (int mi = 0; mi < 3; ++mi) {
+            ++n_newt;
             f = rhs(yv);
             double bv = act ? gamma * f - z[1] / l1 - e : 0.0;
             bv = warp_lu_solve(s.Jr, ld, nv, lane, pivs, mystep, bv);
@@ -217,6 +228,7 @@ k_reactor(const uint8_t* __restrict__ img, ImageLayout L, int64_t n, double* __r
 #pragma unroll
             for (int j = 0; j < 6; ++j) z[j] = zs[j];
             ++ncf;
+            ++n_rej;
             if (ncf >= 10) { status = FLINT_CELL_NEWTON_FAIL; break; }
             if (!jfresh) { need_J = 1; continue; }
             const double eta = 0.25;
@@ -231,6 +243,7 @@ k_reactor(const uint8_t* __restrict__ img, ImageLayout L, int64_t n, double* __r
 #pragma unroll
             for (int j = 0; j < 6; ++j) z[j] = zs[j];
             ++nef;
+            ++n_rej;
             if (nef >= 7) { status = FLINT_CELL_ERRTEST_FAIL; break; }
             double eta;
             if (nef >= 3) {
@@ -306,6 +319,7 @@ k_reactor(const uint8_t* __restrict__ img, ImageLayout L, int64_t n, double* __r
           h *= eta;
         }
       }
+      if (lane == 0) atomicAdd(counter + 4, (unsigned long long)nst);
       y = z[0];
       if (lane < ns) Yg[cell * ns + lane] = y;
       else if (lane == ns) Tg[cell] = y;
@@ -315,6 +329,12 @@ k_reactor(const uint8_t* __restrict__ img, ImageLayout L, int64_t n, double* __r
       if (nsteps_g) nsteps_g[cell] = nst;
     }
     __syncwarp();
+  }
+  if (lane == 0) {
+    atomicAdd(counter + 1, n_rhs);
+    atomicAdd(counter + 2, n_jac);
+    atomicAdd(counter + 3, n_newt);
+    atomicAdd(counter + 5, n_rej);
   }
 }
 
@@ -336,7 +356,15 @@ cudaError_t launch_reactor(const uint8_t* img, const ImageLayout& L, int64_t n, 
   int64_t blocks = (warps_needed + REACTOR_THREADS / 32 - 1) / (REACTOR_THREADS / 32);
   int64_t full = (int64_t)device_sms() * per_sm;
   if (blocks > full) blocks = full;
-  e = cudaMemsetAsync(work_counter, 0, sizeof(unsigned long long), st);
+  static bool bdf_ready = false;
+  if (!bdf_ready) {
+    BdfL B;
+    bdf_coeffs(B);
+    e = cudaMemcpyToSymbol(c_bdf, &B, sizeof(B));
+    if (e != cudaSuccess) return e;
+    bdf_ready = true;
+  }
+  e = cudaMemsetAsync(work_counter, 0, NCOUNTERS * sizeof(unsigned long long), st);
   if (e != cudaSuccess) return e;
   k_reactor<<<(unsigned)blocks, REACTOR_THREADS, sm, st>>>(img, L, n, T, p, Y, dt, o, status, nsteps,
                                                             reinterpret_cast<unsigned long long*>(work_counter));

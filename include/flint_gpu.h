@@ -164,6 +164,13 @@ int flint_reactor_advance(flint_mech_t mech, int64_t n, double* T, const double*
                           double* Y, const double* dt, const flint_reactor_opts* opts,
                           int* status, int* nsteps, void* stream);
 
+/* Work counters of the last flint_reactor_advance on this handle (blocks until
+ * it has finished): out[0] RHS evaluations, out[1] Jacobian + LU refreshes,
+ * out[2] Newton iterations (one LU solve each), out[3] accepted steps,
+ * out[4] rejected step attempts.  No reference counterpart: instrumentation
+ * (the CVODE statistics test-batchCXX.cpp:25-48 prints are its nearest kin). */
+int flint_reactor_stats(flint_mech_t mech, int64_t out[5]);
+
 /* Default options: rtol 1e-8, atol 1e-14, 20000 steps, order 5, constant p. */
 void flint_reactor_default_opts(flint_reactor_opts* opts);
 
@@ -176,6 +183,11 @@ int flint_wdot_jac_batch_host(flint_mech_t mech, int64_t n, int layout, const do
 int flint_reactor_advance_host(flint_mech_t mech, int64_t n, double* T, const double* p,
                                double* Y, const double* dt, const flint_reactor_opts* opts,
                                int* status, int* nsteps);
+
+/* FP64 FMA throughput of the current GPU in TFLOP/s (FMA = 2 flops), timed on
+ * the default stream with an independent-FMA-chain kernel; the denominator of
+ * the FP64 roofline.  No reference counterpart: instrumentation. */
+int flint_probe_fp64_peak(double* tflops);
 
 /* Number of kernels the library launched since load (instrumentation). */
 int64_t flint_kernel_launch_count(void);
