@@ -150,11 +150,13 @@ def test_reactor_vs_oracle():
     # but the work agrees on average and most cells take identical steps
     assert abs(nst.sum() / ns_o.sum() - 1.0) < 0.05
     assert np.mean(nst == ns_o) > 0.3
-    # both within their tolerance of the tight solution (weighted by rtol*|y|+atol)
+    # both close to the tight solution: the local tolerances rtol=1e-8,
+    # atol=1e-14 accumulate over ~650 steps into a global error of ~1e-8 in Y
+    # and ~1e-4 K in T; the bounds leave a factor ~50 of margin
     for Tv, Yv in ((Tg, Yg), (T_o, Y_o)):
-        errT = np.abs(Tv - T_x) / (1e-8 * np.abs(T_x))
-        errY = np.abs(Yv - Y_x) / (1e-8 * np.abs(Y_x) + 1e-14)
-        assert errT.max() < 200 and errY.max() < 2000, (errT.max(), errY.max())
+        errT = np.abs(Tv - T_x) / np.abs(T_x)
+        errY = np.abs(Yv - Y_x)
+        assert errT.max() < 1e-5 and errY.max() < 1e-6, (errT.max(), errY.max())
     # GPU and oracle agree to the integrator tolerance
     assert np.max(np.abs(Tg - T_o) / T_o) < 1e-6
     assert np.max(np.abs(Yg - Y_o)) < 1e-6
