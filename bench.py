@@ -251,7 +251,7 @@ def run_ours(args):
 
     # ---- roofline: FP64 pipe ------------------------------------------------
     s = stats[-1]
-    ops = (s["rhs"] * FP64_OPS["rhs"] + s["jac_lu"] * (FP64_OPS["jac"] + FP64_OPS["lu"])
+    ops = (s["rhs"] * FP64_OPS["rhs"] + s["jac"] * FP64_OPS["jac"] + s["lu"] * FP64_OPS["lu"]
            + s["newton"] * FP64_OPS["solve"])
     peak = chem_peak_fp64()
     achieved = ops / t_step / 1e12

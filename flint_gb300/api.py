@@ -170,10 +170,10 @@ class Chemistry:
 
 
 def reactor_stats(chem):
-    """Counters of the last reactor launch: rhs, jac_lu, newton, steps, rejected."""
-    out = (C.c_int64 * 5)()
+    """Counters of the last reactor launch: rhs, jac, newton, steps, rejected, lu."""
+    out = (C.c_int64 * 6)()
     native.check(chem.L.flint_reactor_stats(chem.h, out), "flint_reactor_stats")
-    return dict(zip(("rhs", "jac_lu", "newton", "steps", "rejected"), list(out)))
+    return dict(zip(("rhs", "jac", "newton", "steps", "rejected", "lu"), list(out)))
 
 
 def kernel_launches():

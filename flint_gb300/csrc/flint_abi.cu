@@ -47,11 +47,15 @@ static int rup(int x, int m) { return (x + m - 1) / m * m; }
 using namespace flint;
 
 struct flint_mech_s {
+  void* table = nullptr;   // tabulated mechanism (flint_mech_create_tables)
   ImageLayout L;
   std::vector<uint8_t> himg;
   uint8_t* dimg = nullptr;
   unsigned int* dcounter = nullptr;
   int device = 0;
+  // saved-Jacobian scratch of the reactor, one slot per resident warp
+  double* djsave = nullptr;
+  int jslots = 0;
   // staging buffers of the *_host entry points (grow only)
   void* dstage = nullptr;
   size_t stage_bytes = 0;
@@ -80,6 +84,7 @@ static int pack(const flint_mech_desc* d, ImageLayout& L, std::vector<uint8_t>& 
     if (t != 0) {
       if (!d->eff) return fail(FLINT_ERR_ARG, "third-body reactions need efficiencies");
       if (t >= 2 && (!d->arrh0 || (t == 3 && !d->troe))) return fail(FLINT_ERR_ARG, "falloff data missing");
+    if (t >= 2 && !(d->arrh[3 * r] > 0.0)) return fail(FLINT_ERR_MECH, "reaction %d: falloff with A_inf <= 0", r);
       ++ntb;
     }
     for (int s = 0; s < 3; ++s) {
@@ -90,6 +95,9 @@ static int pack(const flint_mech_desc* d, ImageLayout& L, std::vector<uint8_t>& 
     }
   }
   if (ntb > 255) return fail(FLINT_ERR_MECH, "more than 255 third-body/falloff reactions");
+  int nfall = 0;
+  for (int r = 0; r < nr; ++r) nfall += d->rtype[r] >= 2;
+  if (nfall > 16) return fail(FLINT_ERR_MECH, "%d falloff reactions: this build supports up to 16", nfall);
   L = ImageLayout{};
   L.ns = ns; L.nr = nr; L.nsp = rup(ns, 32); L.nrpad = rup(std::max(nr, 1), 32); L.ntb = std::max(ntb, 1);
   L.r_eos = d->r_eos; L.r_thermo = d->r_thermo;
@@ -117,8 +125,11 @@ static int pack(const flint_mech_desc* d, ImageLayout& L, std::vector<uint8_t>& 
   L.o_A0 = sec(8 * P); L.o_b0 = sec(8 * P); L.o_E0 = sec(8 * P); L.o_tr = sec(8 * 4 * P);
   L.o_rnu = sec(8 * 3 * P); L.o_rord = sec(8 * 3 * P); L.o_pnu = sec(8 * 3 * P);
   L.o_rsp = sec(4 * 3 * P); L.o_psp = sec(4 * 3 * P); L.o_code = sec(4 * P); L.o_dnu = sec(8 * P);
+  L.o_pcode = sec(4 * P);
   L.o_eff = sec(8 * L.ntb * S);
   L.o_cstart = sec(4 * (S + 1)); L.o_lr = sec(4 * std::max(nlist, 1)); L.o_lnu = sec(8 * std::max(nlist, 1));
+  L.o_exptab = sec(8 * 64);
+  L.nfall = nfall;
   L.bytes = off;
   img.assign(off, 0);
   auto D = [&](int o) { return reinterpret_cast<double*>(img.data() + o); };
@@ -139,7 +150,11 @@ static int pack(const flint_mech_desc* d, ImageLayout& L, std::vector<uint8_t>& 
     int r = order[rr];
     int t = d->rtype[r];
     D(L.o_A)[rr] = d->arrh[3 * r]; D(L.o_b)[rr] = d->arrh[3 * r + 1]; D(L.o_E)[rr] = d->arrh[3 * r + 2];
-    if (t >= 2) { D(L.o_A0)[rr] = d->arrh0[3 * r]; D(L.o_b0)[rr] = d->arrh0[3 * r + 1]; D(L.o_E0)[rr] = d->arrh0[3 * r + 2]; }
+    if (t >= 2) {  // low-pressure limit relative to the high-pressure one
+      D(L.o_A0)[rr] = d->arrh0[3 * r] / d->arrh[3 * r];
+      D(L.o_b0)[rr] = d->arrh0[3 * r + 1] - d->arrh[3 * r + 1];
+      D(L.o_E0)[rr] = d->arrh0[3 * r + 2] - d->arrh[3 * r + 2];
+    }
     if (t == 3) for (int j = 0; j < 4; ++j) D(L.o_tr)[j * P + rr] = d->troe[4 * r + j];
     uint32_t w = (uint32_t)t | ((d->reversible[r] ? 1u : 0u) << 2);
     double dn = 0.0;
@@ -153,7 +168,13 @@ static int pack(const flint_mech_desc* d, ImageLayout& L, std::vector<uint8_t>& 
         w |= oc << (16 + 4 * s);
         dn -= nu;
       }
-      if (b >= 0) { D(L.o_pnu)[s * P + rr] = d->pnu[3 * r + s]; dn += d->pnu[3 * r + s]; }
+      if (b >= 0) {
+        double nu = d->pnu[3 * r + s];
+        D(L.o_pnu)[s * P + rr] = nu;
+        dn += nu;
+        uint32_t pc = nu == 1.0 ? 1 : nu == 2.0 ? 2 : nu == 3.0 ? 3 : nu == 0.0 ? 0 : 4;
+        reinterpret_cast<uint32_t*>(img.data() + L.o_pcode)[rr] |= pc << (4 * s);
+      }
     }
     if (t != 0) {
       w |= (uint32_t)tb << 8;
@@ -170,6 +191,8 @@ static int pack(const flint_mech_desc* d, ImageLayout& L, std::vector<uint8_t>& 
       for (auto& pr : lists[k]) { I(L.o_lr)[e] = pr.first; D(L.o_lnu)[e] = pr.second; ++e; }
   }
   I(L.o_cstart)[S] = e;
+  // 2^(j/64), rounded from extended precision, for the table-driven exp
+  for (int j = 0; j < 64; ++j) D(L.o_exptab)[j] = (double)exp2l((long double)j / 64.0L);
   return FLINT_OK;
 }
 
@@ -212,16 +235,44 @@ int flint_mech_create(const flint_mech_desc* desc, flint_mech_t* out) {
   return FLINT_OK;
 }
 
+int flint_mech_create_tables(const flint_table_desc* desc, flint_mech_t* out) {
+  if (!desc || !out) return fail(FLINT_ERR_ARG, "NULL argument");
+  *out = nullptr;
+  auto* h = new flint_mech_s();
+  std::string err;
+  int rc = table_create(desc, &h->table, err);
+  if (rc != FLINT_OK) { delete h; return fail(rc, "flint_mech_create_tables: %s", err.c_str()); }
+  h->L = ImageLayout{};
+  h->L.ns = table_ns(h->table);
+  h->L.nr = table_nr(h->table);
+  cudaGetDevice(&h->device);
+  *out = h;
+  return FLINT_OK;
+}
+
+int flint_rhs_native_batch(flint_mech_t h, int64_t n, const double* Z, double* F, void* stream) {
+  if (!h) return fail(FLINT_ERR_ARG, "NULL handle");
+  if (n < 0) return fail(FLINT_ERR_ARG, "negative cell count");
+  if (!h->table) return fail(FLINT_ERR_MECH, "flint_rhs_native_batch needs a tabulated mechanism");
+  if (n == 0) return FLINT_OK;
+  if (!Z || !F) return fail(FLINT_ERR_ARG, "NULL array");
+  cudaError_t e = table_run(h->table, n, 1, Z, nullptr, F, (cudaStream_t)stream);
+  return e == cudaSuccess ? FLINT_OK : cuda_fail(e, "flint_rhs_native_batch");
+}
+
 int flint_mech_destroy(flint_mech_t h) {
   if (!h) return FLINT_OK;
+  if (h->table) table_destroy(h->table);
   if (h->dimg) cudaFree(h->dimg);
   if (h->dcounter) cudaFree(h->dcounter);
   if (h->dstage) cudaFree(h->dstage);
+  if (h->djsave) cudaFree(h->djsave);
   delete h;
   return FLINT_OK;
 }
 
 int flint_mech_sizes(flint_mech_t h, int* ns, int* nr) {
+  // (tabulated handles report their species and total reaction counts too)
   if (!h) return fail(FLINT_ERR_ARG, "NULL handle");
   if (ns) *ns = h->L.ns;
   if (nr) *nr = h->L.nr;
@@ -230,6 +281,7 @@ int flint_mech_sizes(flint_mech_t h, int* ns, int* nr) {
 
 static int check_common(flint_mech_t h, int64_t n, int layout) {
   if (!h) return fail(FLINT_ERR_ARG, "NULL handle");
+  if (h->table) return fail(FLINT_ERR_MECH, "this entry point needs an analytic (NASA-7/Arrhenius) mechanism");
   if (n < 0) return fail(FLINT_ERR_ARG, "negative cell count");
   if (layout != FLINT_CELL_MAJOR && layout != FLINT_SPECIES_MAJOR) return fail(FLINT_ERR_ARG, "layout %d", layout);
   return FLINT_OK;
@@ -257,6 +309,13 @@ int flint_thermo_batch(flint_mech_t h, int64_t n, int layout, const double* T, c
 
 int flint_chemistry_source_batch(flint_mech_t h, int64_t n, double* roi, const double* T, double* omegadot,
                                  void* stream) {
+  if (h && h->table) {
+    if (n < 0) return fail(FLINT_ERR_ARG, "negative cell count");
+    if (n == 0) return FLINT_OK;
+    if (!roi || !T || !omegadot) return fail(FLINT_ERR_ARG, "NULL array");
+    cudaError_t e = table_run(h->table, n, 0, roi, T, omegadot, (cudaStream_t)stream);
+    return e == cudaSuccess ? FLINT_OK : cuda_fail(e, "flint_chemistry_source_batch");
+  }
   int rc = check_common(h, n, FLINT_CELL_MAJOR);
   if (rc) return rc;
   if (n == 0) return FLINT_OK;
@@ -303,18 +362,31 @@ int flint_reactor_advance(flint_mech_t h, int64_t n, double* T, const double* p,
   if (!(o.rtol > 0.0) || !(o.atol > 0.0) || o.max_steps < 1 || o.max_order < 1 || o.max_order > 5)
     return fail(FLINT_ERR_ARG, "reactor options out of range");
   if (o.constant_volume) return fail(FLINT_ERR_ARG, "constant-volume reactor is not in this build");
-  cudaError_t e = launch_reactor(h->dimg, h->L, n, T, p, Y, dt, o, status, nsteps, h->dcounter,
-                                 (cudaStream_t)stream);
+  if (!h->djsave) {
+    int slots = reactor_slots(h->L);
+    if (slots < 1) return fail(FLINT_ERR_MECH, "reactor kernel does not fit this mechanism (shared memory)");
+    cudaError_t ea = cudaMalloc(&h->djsave, (size_t)slots * reactor_slot_bytes());
+    if (ea != cudaSuccess) { h->djsave = nullptr; return fail(FLINT_ERR_NOMEM, "reactor scratch: %s", cudaGetErrorString(ea)); }
+    h->jslots = slots;
+  }
+  cudaError_t e = launch_reactor(h->dimg, h->L, n, T, p, Y, dt, o, status, nsteps, h->dcounter, h->djsave,
+                                 h->jslots, (cudaStream_t)stream);
   return e == cudaSuccess ? FLINT_OK : cuda_fail(e, "flint_reactor_advance");
 }
 
-int flint_reactor_stats(flint_mech_t h, int64_t out[5]) {
+int flint_reactor_stats(flint_mech_t h, int64_t out[6]) {
   if (!h || !out) return fail(FLINT_ERR_ARG, "NULL argument");
-  unsigned long long c[6];
+  unsigned long long c[7];
   cudaError_t e = cudaMemcpy(c, h->dcounter, sizeof c, cudaMemcpyDeviceToHost);
   if (e != cudaSuccess) return cuda_fail(e, "flint_reactor_stats");
-  for (int i = 0; i < 5; ++i) out[i] = (int64_t)c[i + 1];
+  for (int i = 0; i < 6; ++i) out[i] = (int64_t)c[i + 1];
   return FLINT_OK;
+}
+
+int flint_selftest_exp(flint_mech_t h, int64_t n, const double* x, double* y, void* stream) {
+  if (!h || n < 0 || (n > 0 && (!x || !y))) return fail(FLINT_ERR_ARG, "bad argument");
+  cudaError_t e = launch_exp_selftest(h->dimg, h->L, n, x, y, (cudaStream_t)stream);
+  return e == cudaSuccess ? FLINT_OK : cuda_fail(e, "flint_selftest_exp");
 }
 
 int flint_probe_fp64_peak(double* tflops) {

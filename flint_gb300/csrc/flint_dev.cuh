@@ -43,14 +43,20 @@ struct ImageLayout {
   int o_mw, o_invmw, o_nasa;     // nasa: [16][nsp] : low a0..a6, high a0..a6, tmid, unused
   // reactions (nrpad each)
   int o_A, o_b, o_E, o_A0, o_b0, o_E0, o_tr;   // tr: [4][nrpad]
+  // falloff: the image stores the low-pressure limit relative to the high-
+  // pressure one, k0/kinf = A0r T^b0r exp(-E0r/T) with A0r = A0/A, b0r = b0-b,
+  // E0r = (Ea0-Ea)/R, so Pr = (k0/kinf) M costs one exp and no division.
   int o_rnu, o_rord, o_pnu;      // [3][nrpad]
   int o_rsp, o_psp;              // int32 [3][nrpad]
   int o_code;                    // uint32 [nrpad]
+  int o_pcode;                   // uint32 [nrpad]: product order codes, 4 bits per slot
   int o_dnu;                     // double [nrpad]
   int o_eff;                     // [ntb][nsp]
   int o_cstart;                  // int32 [nsp+1]
   int o_lr;                      // int32 [nlist]
   int o_lnu;                     // double [nlist]
+  int o_exptab;                  // double [64]: 2^(j/64)
+  int nfall;                     // falloff reactions (the last nfall after sorting; <= 16)
 };
 
 struct MechView {
@@ -61,10 +67,13 @@ struct MechView {
   const double *rnu, *rord, *pnu, *dnu;
   const int *rsp, *psp, *cstart, *lr;
   const uint32_t* code;
-  const double *eff, *lnu;
+  const uint32_t* pcode;
+  const double *eff, *lnu, *exptab;
+  int nfall;
 
   __host__ __device__ void bind(const ImageLayout& L, const uint8_t* base) {
-    ns = L.ns; nr = L.nr; nrpad = L.nrpad; nsp = L.nsp; ntb = L.ntb;
+    ns = L.ns; nr = L.nr; nrpad = L.nrpad; nsp = L.nsp; ntb = L.ntb; nfall = L.nfall;
+    exptab = (const double*)(base + L.o_exptab);
     r_eos = L.r_eos; r_thermo = L.r_thermo; lnpref_rth = L.lnpref_rth;
     mw = (const double*)(base + L.o_mw); invmw = (const double*)(base + L.o_invmw);
     nasa = (const double*)(base + L.o_nasa);
@@ -75,6 +84,7 @@ struct MechView {
     pnu = (const double*)(base + L.o_pnu); dnu = (const double*)(base + L.o_dnu);
     rsp = (const int*)(base + L.o_rsp); psp = (const int*)(base + L.o_psp);
     code = (const uint32_t*)(base + L.o_code);
+    pcode = (const uint32_t*)(base + L.o_pcode);
     eff = (const double*)(base + L.o_eff);
     cstart = (const int*)(base + L.o_cstart); lr = (const int*)(base + L.o_lr);
     lnu = (const double*)(base + L.o_lnu);
@@ -87,6 +97,30 @@ __device__ inline void stage_image(uint8_t* smem, const uint8_t* __restrict__ g,
   int4* dst = reinterpret_cast<int4*>(smem);
   for (int i = threadIdx.x; i < bytes / 16; i += blockDim.x) dst[i] = __ldg(src + i);
   __syncthreads();
+}
+
+// exp(x) by Tang's table-driven method (P. T. P. Tang, ACM TOMS 15(2), 1989):
+// x = (64 m + j) ln2/64 + r with |r| <= ln2/128, exp(x) = 2^m 2^(j/64) exp(r),
+// exp(r) - 1 by its degree-5 Taylor polynomial (truncation < 4e-17 relative).
+// ln2/64 is split into a 32-bit head and a tail (the classic fdlibm split of
+// ln2) so that n*head is exact.  2^(j/64) comes from the 64-entry table staged
+// with the mechanism.  10 FP64 operations; |x| >= 700, NaN and Inf take the
+// CUDA library path.  Accuracy is tested against CUDA's exp (tests/test_gpu_parity.py).
+__device__ __forceinline__ double fexp(double x, const double* __restrict__ tab) {
+  if (!(fabs(x) < 700.0)) return exp(x);
+  const double SHIFT = 6755399441055744.0;               // 1.5 * 2^52
+  const double INV_L = 92.33248261689366;                // 64 / ln2
+  const double L_HI = 0.01083042469326756;               // 0x1.62e42fee00000p-7
+  const double L_LO = 2.9815858269852933e-12;            // 0x1.a39ef35793c76p-39
+  double kd = fma(x, INV_L, SHIFT);
+  const int k = __double2loint(kd);
+  kd -= SHIFT;
+  double r = fma(kd, -L_HI, x);
+  r = fma(kd, -L_LO, r);
+  const double p = r * fma(r, fma(r, fma(r, fma(r, 1.0 / 120.0, 1.0 / 24.0), 1.0 / 6.0), 0.5), 1.0);
+  const double t = tab[k & 63];
+  const double res = fma(t, p, t);
+  return __hiloint2double(__double2hiint(res) + (k >> 6) * 1048576, __double2loint(res));
 }
 
 __device__ inline double warp_sum(double v) {
@@ -118,7 +152,7 @@ __device__ inline SpThermo nasa7(const MechView& m, int k, double T, double lnT,
 }
 
 // c^ord by order code (1..3 integral, 4 general) with the derivative d(c^ord)/dc.
-__device__ inline double powc(double c, int code, double ord, double* d) {
+__device__ inline double powc(double c, int code, double ord, double* d, const double* tab) {
   switch (code) {
     case 1: *d = 1.0; return c;
     case 2: *d = 2.0 * c; return c * c;
@@ -126,7 +160,7 @@ __device__ inline double powc(double c, int code, double ord, double* d) {
     case 4: {
       double cc = c > 0.0 ? c : 0.0;
       if (cc > 0.0) {
-        double pw = exp(ord * log(cc));
+        double pw = fexp(ord * log(cc), tab);
         *d = ord * pw / cc;
         return pw;
       }
@@ -137,25 +171,26 @@ __device__ inline double powc(double c, int code, double ord, double* d) {
   }
 }
 
-__device__ inline int ordcode_of(double nu) {
-  return nu == 1.0 ? 1 : (nu == 2.0 ? 2 : (nu == 3.0 ? 3 : (nu == 0.0 ? 0 : 4)));
-}
-
 // Per-warp scratch (doubles) used by the kinetics.
 struct WarpScratch {
   double* c;      // [nsp]
   double* hRT;    // [nsp]
   double* gRT;    // [nsp]
   double* q;      // [nrpad] rates of progress
+  double* fo;     // [8][32] falloff pre-pass values (aliases Jr in Jacobian mode)
   // Jacobian mode only
   double* dq;     // [8][nrpad]: 6 sparse partials (3 reactant, 3 product slots), tb coef, dq/dT
   double* Jr;     // [n][ldj] rows (species rows then T row), ldj = nsp+1 (odd stride)
   int ldj;
 };
 
+// Layout: c, hRT, gRT [nsp each], q [nrpad], then either the Jacobian area
+// dq [8][nrpad] + Jr [(nsp+1)^2] or (source terms only) the falloff area [8][32].
+// The falloff pre-pass of a source-term evaluation inside a Jacobian carve
+// uses the dq area (dead between Jacobian evaluations); a Jacobian evaluation
+// uses Jr (written only after the rates of progress are done).
 __host__ __device__ inline int scratch_doubles(int nsp, int nrpad, bool jac) {
-  int base = 3 * nsp + nrpad;
-  if (jac) base += 8 * nrpad + (nsp + 1) * (nsp + 1);
+  int base = 3 * nsp + nrpad + (jac ? 8 * nrpad + (nsp + 1) * (nsp + 1) : 8 * 32);
   return (base + 1) & ~1;   // keep 16-byte alignment
 }
 
@@ -164,6 +199,7 @@ __device__ inline WarpScratch carve(double* p, int nsp, int nrpad, bool jac) {
   s.c = p; s.hRT = p + nsp; s.gRT = p + 2 * nsp; s.q = p + 3 * nsp;
   s.ldj = nsp + 1;
   if (jac) { s.dq = s.q + nrpad; s.Jr = s.dq + 8 * nrpad; } else { s.dq = nullptr; s.Jr = nullptr; }
+  s.fo = s.q + nrpad;
   return s;
 }
 
@@ -183,19 +219,19 @@ struct Falloff { double keff, dlnkeff, dkeff_dM; };
 
 __device__ inline Falloff falloff_eval(const MechView& m, int r, int type, double kinf, double dlnkinf,
                                        double M, double T, double lnT, double invT) {
-  double k0 = m.A0[r] * exp(m.b0[r] * lnT - m.E0[r] * invT);
-  double dlnk0 = (m.b0[r] + m.E0[r] * invT) * invT;
-  double kratio = k0 / kinf;
+  const double* tab = m.exptab;
+  double kratio = m.A0[r] * fexp(m.b0[r] * lnT - m.E0[r] * invT, tab);
+  double dlnPr = (m.b0[r] + m.E0[r] * invT) * invT;
   double Pr = kratio * M;
   double F = 1.0, G = 0.0, dlnF_T = 0.0;
   if (type == 3) {
     const int P = m.nrpad;
     double a = m.tr[r], T3 = m.tr[P + r], T1 = m.tr[2 * P + r], T2 = m.tr[3 * P + r];
-    double e3 = exp(-T / T3), e1 = exp(-T / T1);
+    double e3 = fexp(-T / T3, tab), e1 = fexp(-T / T1, tab);
     double Fc = (1.0 - a) * e3 + a * e1;
     double dFc = -(1.0 - a) / T3 * e3 - a / T1 * e1;
     if (T2 != 0.0) {
-      double e2 = exp(-T2 * invT);
+      double e2 = fexp(-T2 * invT, tab);
       Fc += e2;
       dFc += T2 * invT * invT * e2;
     }
@@ -206,7 +242,7 @@ __device__ inline Falloff falloff_eval(const MechView& m, int r, int type, doubl
     double den = nn - 0.14 * x;
     double f1 = x / den;
     double opf = 1.0 + f1 * f1;
-    F = exp(2.302585092994045684 * (logFc / opf));
+    F = fexp(2.302585092994045684 * (logFc / opf), tab);
     double Aq = 2.0 * logFc * f1 / (opf * opf * den * den);
     G = -Aq * nn;
     dlnF_T = (1.0 / opf + Aq * (0.67 * nn - 1.27 * x)) * dFc / Fc;
@@ -214,7 +250,6 @@ __device__ inline Falloff falloff_eval(const MechView& m, int r, int type, doubl
   double opr = 1.0 + Pr;
   Falloff o;
   o.keff = kinf * (Pr / opr) * F;
-  double dlnPr = dlnk0 - dlnkinf;
   o.dlnkeff = dlnkinf + dlnPr / opr + G * dlnPr + dlnF_T;
   o.dkeff_dM = kinf * F / opr * (1.0 / opr + G) * kratio;
   return o;
@@ -248,14 +283,103 @@ __device__ void warp_kinetics(const MechView& m, const WarpScratch& s, int lane,
     s.c[lane] = ck; s.hRT[lane] = hr; s.gRT[lane] = gr;
   }
   __syncwarp();
-  // reaction-parallel: rates of progress
+  const double* tab = m.exptab;
+  // ---- falloff pre-pass: the last nfall reactions (<= 16) -----------------
+  // The transcendentals of all falloff reactions are spread over the lanes:
+  // pass 1 evaluates k_inf, k_0 and the three Fcent exponentials of every
+  // falloff reaction (5 jobs each), pass 2 forms M, Pr and Fcent on lane i,
+  // pass 3 takes log10 of Fcent (lane i) and Pr (lane nfall + i) together,
+  // pass 4 blends (Lindemann / Troe, Lib_Chemistry_falloff.f90:12-80).
+  const int NF = m.nfall, f0 = m.nr - NF;
+  double* fo = JAC ? s.Jr : s.fo;     // [8][32]
+  if (NF > 0) {
+    for (int jb = lane; jb < 5 * NF; jb += WARP) {
+      const int i = jb / 5, kind = jb - 5 * i, r = f0 + i;
+      const int P = m.nrpad;
+      double arg = 0.0, pre = 1.0;
+      const bool troe = rx_type(m.code[r]) == 3;
+      switch (kind) {
+        case 0: arg = m.b[r] * lnT - m.E[r] * invT; pre = m.A[r]; break;
+        case 1: arg = m.b0[r] * lnT - m.E0[r] * invT; pre = m.A0[r]; break;   // k0 / kinf
+        case 2: arg = troe ? -T / m.tr[P + r] : 0.0; break;
+        case 3: arg = troe ? -T / m.tr[2 * P + r] : 0.0; break;
+        default: {
+          const double T2 = m.tr[3 * P + r];
+          arg = (troe && T2 != 0.0) ? -T2 * invT : 0.0;
+          pre = (troe && T2 != 0.0) ? 1.0 : 0.0;
+        }
+      }
+      fo[kind * WARP + i] = pre * fexp(arg, tab);
+    }
+    __syncwarp();
+    double Pr = 1.0, Fc = 1.0, dFc = 0.0, kinf = 0.0, kratio = 0.0, dlnkinf = 0.0, dlnPr = 0.0;
+    bool troe = false;
+    if (lane < NF) {
+      const int r = f0 + lane, P = m.nrpad;
+      const uint32_t w = m.code[r];
+      troe = rx_type(w) == 3;
+      const double* effrow = m.eff + rx_tbrow(w) * nsp;
+      double M = 0.0;
+      for (int k = 0; k < ns; ++k) M += effrow[k] * s.c[k];
+      kinf = fo[lane];
+      kratio = fo[WARP + lane];
+      Pr = kratio * M;
+      if (JAC) {
+        dlnkinf = (m.b[r] + m.E[r] * invT) * invT;
+        dlnPr = (m.b0[r] + m.E0[r] * invT) * invT;
+      }
+      if (troe) {
+        const double a = m.tr[r];
+        const double e3 = fo[2 * WARP + lane], e1 = fo[3 * WARP + lane], e2 = fo[4 * WARP + lane];
+        Fc = (1.0 - a) * e3 + a * e1 + e2;
+        if (JAC) {
+          const double T3 = m.tr[P + r], T1 = m.tr[2 * P + r], T2 = m.tr[3 * P + r];
+          dFc = -(1.0 - a) / T3 * e3 - a / T1 * e1 + (T2 != 0.0 ? T2 * invT * invT * e2 : 0.0);
+        }
+      }
+    }
+    const double Pr_src = __shfl_sync(FULL, Pr, lane >= NF && lane < 2 * NF ? lane - NF : 0);
+    double lg_in = lane < NF ? Fc : (lane < 2 * NF ? Pr_src : 1.0);
+    lg_in = lg_in > 1e-300 ? lg_in : 1e-300;
+    const double lg = log10(lg_in);
+    const double logPr = __shfl_sync(FULL, lg, lane < NF ? lane + NF : 0);
+    double Fb = 1.0, G = 0.0, dlnF_T = 0.0, fexp_arg = 0.0;
+    double opf = 1.0, x = 0.0, nn = 0.0, logFc = 0.0, den = 1.0, f1 = 0.0;
+    if (lane < NF && troe) {
+      logFc = lg;
+      const double cc = -0.4 - 0.67 * logFc;
+      nn = 0.75 - 1.27 * logFc;
+      x = logPr + cc;
+      den = nn - 0.14 * x;
+      f1 = x / den;
+      opf = 1.0 + f1 * f1;
+      fexp_arg = 2.302585092994045684 * (logFc / opf);
+    }
+    Fb = fexp(fexp_arg, tab);
+    if (lane < NF) {
+      if (!troe) Fb = 1.0;
+      const double iopr = 1.0 / (1.0 + Pr);
+      fo[5 * WARP + lane] = kinf * (Pr * iopr) * Fb;
+      if (JAC) {
+        if (troe) {
+          const double Aq = 2.0 * logFc * f1 / (opf * opf * den * den);
+          G = -Aq * nn;
+          dlnF_T = (1.0 / opf + Aq * (0.67 * nn - 1.27 * x)) * dFc / Fc;
+        }
+        fo[6 * WARP + lane] = dlnkinf + dlnPr * iopr + G * dlnPr + dlnF_T;
+        fo[7 * WARP + lane] = kinf * Fb * iopr * (iopr + G) * kratio;
+      }
+    }
+    __syncwarp();
+  }
+  // ---- reaction-parallel: rates of progress --------------------------------
   for (int r = lane; r < nrpad; r += WARP) {
     double q = 0.0;
     if (r < m.nr) {
       const uint32_t w = m.code[r];
       const int type = rx_type(w);
       const bool rev = rx_rev(w);
-      double kf = m.A[r] * exp(m.b[r] * lnT - m.E[r] * invT);
+      double kf = m.A[r] * fexp(m.b[r] * lnT - m.E[r] * invT, tab);
       double dlnkf = (m.b[r] + m.E[r] * invT) * invT;
       double pwf[MAXSIDE], dpf[MAXSIDE], pwr[MAXSIDE], dpr[MAXSIDE];
       double Pf = 1.0, Pr = 0.0;
@@ -263,7 +387,7 @@ __device__ void warp_kinetics(const MechView& m, const WarpScratch& s, int lane,
       for (int sl = 0; sl < MAXSIDE; ++sl) {
         int sp = m.rsp[sl * nrpad + r];
         int oc = rx_ordcode(w, sl);
-        if (sp >= 0) pwf[sl] = powc(s.c[sp], oc, m.rord[sl * nrpad + r], &dpf[sl]);
+        if (sp >= 0) pwf[sl] = powc(s.c[sp], oc, m.rord[sl * nrpad + r], &dpf[sl], tab);
         else { pwf[sl] = 1.0; dpf[sl] = 0.0; }
         Pf *= pwf[sl];
       }
@@ -278,7 +402,7 @@ __device__ void warp_kinetics(const MechView& m, const WarpScratch& s, int lane,
             double nu = m.pnu[sl * nrpad + r];
             dG += nu * s.gRT[sp];
             if (JAC) dH += nu * s.hRT[sp];
-            pwr[sl] = powc(s.c[sp], ordcode_of(nu), nu, &dpr[sl]);
+            pwr[sl] = powc(s.c[sp], (m.pcode[r] >> (4 * sl)) & 0xf, nu, &dpr[sl], tab);
           } else { pwr[sl] = 1.0; dpr[sl] = 0.0; }
           Pr *= pwr[sl];
           int sq = m.rsp[sl * nrpad + r];
@@ -290,20 +414,18 @@ __device__ void warp_kinetics(const MechView& m, const WarpScratch& s, int lane,
         }
         const double dn = m.dnu[r];
         // 1/Kc = exp(dG - dnu ln(p_ref/RT))
-        invKc = exp(dG - dn * lnC0);
+        invKc = fexp(dG - dn * lnC0, tab);
         dlnKc = (dH - dn) * invT;
       }
-      double Mfac = 1.0, keff = kf, dlnkeff = dlnkf, dkdM = 0.0, M = 0.0;
-      const double* effrow = nullptr;
-      if (type != 0) {
-        effrow = m.eff + rx_tbrow(w) * nsp;
+      double Mfac = 1.0, keff = kf, dlnkeff = dlnkf, dkdM = 0.0;
+      if (type == 1) {
+        const double* effrow = m.eff + rx_tbrow(w) * nsp;
+        double M = 0.0;
         for (int k = 0; k < ns; ++k) M += effrow[k] * s.c[k];
-        if (type == 1) {
-          Mfac = M;
-        } else {
-          Falloff fo = falloff_eval(m, r, type, kf, dlnkf, M, T, lnT, invT);
-          keff = fo.keff; dlnkeff = fo.dlnkeff; dkdM = fo.dkeff_dM;
-        }
+        Mfac = M;
+      } else if (type >= 2) {
+        const int i = r - f0;
+        keff = fo[5 * WARP + i]; dlnkeff = fo[6 * WARP + i]; dkdM = fo[7 * WARP + i];
       }
       double fwd = Mfac * keff * Pf;
       double rvs = rev ? Mfac * keff * invKc * Pr : 0.0;

@@ -1,6 +1,7 @@
 // flint_host.h -- internal host-side declarations shared by the .cu files.
 #pragma once
 #include <cstdint>
+#include <string>
 #include <cuda_runtime.h>
 #include "flint_dev.cuh"
 #include "../../include/flint_gpu.h"
@@ -9,6 +10,8 @@ namespace flint {
 
 void count_launch();
 cudaError_t probe_fp64(double* tflops);
+cudaError_t launch_exp_selftest(const uint8_t* img, const ImageLayout& L, int64_t n, const double* x, double* y,
+                                cudaStream_t st);
 int device_sms();
 
 cudaError_t launch_wdot(const uint8_t* img, const ImageLayout& L, int64_t n, int layout, const double* T,
@@ -21,8 +24,18 @@ cudaError_t launch_wdot_jac(const uint8_t* img, const ImageLayout& L, int64_t n,
                             const double* p, const double* Y, double* wdot, double* jac, cudaStream_t st);
 cudaError_t launch_rhs(const uint8_t* img, const ImageLayout& L, int64_t n, const double* T, const double* p,
                        const double* Y, double* f, cudaStream_t st);
+int reactor_slots(const ImageLayout& L);
+size_t reactor_slot_bytes();
 cudaError_t launch_reactor(const uint8_t* img, const ImageLayout& L, int64_t n, double* T, const double* p,
                            double* Y, const double* dt, const flint_reactor_opts& o, int* status, int* nsteps,
-                           unsigned int* work_counter, cudaStream_t st);
+                           unsigned int* work_counter, double* jsave, int slots, cudaStream_t st);
+
+// tabulated (reference general-loop) path, flint_table.cu
+int table_create(const flint_table_desc* d, void** out, std::string& err);
+void table_destroy(void* th);
+int table_ns(void* th);
+int table_nr(void* th);
+cudaError_t table_run(void* th, int64_t n, int rhs, const double* roi, const double* T, double* out,
+                      cudaStream_t st);
 
 }  // namespace flint

@@ -81,12 +81,12 @@ k_wdot_small(const uint8_t* __restrict__ img, ImageLayout L, int64_t n, int layo
     for (int r = 0; r < m.nr; ++r) {
       const uint32_t w = m.code[r];
       const int type = rx_type(w);
-      double kf = m.A[r] * exp(m.b[r] * lnT - m.E[r] * invT);
+      double kf = m.A[r] * fexp(m.b[r] * lnT - m.E[r] * invT, m.exptab);
       double Pf = 1.0, d;
 #pragma unroll
       for (int sl = 0; sl < MAXSIDE; ++sl) {
         int sp = m.rsp[sl * P + r];
-        if (sp >= 0) Pf *= powc(CS(sp), rx_ordcode(w, sl), m.rord[sl * P + r], &d);
+        if (sp >= 0) Pf *= powc(CS(sp), rx_ordcode(w, sl), m.rord[sl * P + r], &d, m.exptab);
       }
       double rvsf = 0.0;
       if (rx_rev(w)) {
@@ -97,12 +97,12 @@ k_wdot_small(const uint8_t* __restrict__ img, ImageLayout L, int64_t n, int layo
           if (sp >= 0) {
             double nu = m.pnu[sl * P + r];
             dG += nu * GS(sp);
-            Pr *= powc(CS(sp), ordcode_of(nu), nu, &d);
+            Pr *= powc(CS(sp), (m.pcode[r] >> (4 * sl)) & 0xf, nu, &d, m.exptab);
           }
           int sq = m.rsp[sl * P + r];
           if (sq >= 0) dG -= m.rnu[sl * P + r] * GS(sq);
         }
-        rvsf = exp(dG - m.dnu[r] * lnC0) * Pr;
+        rvsf = fexp(dG - m.dnu[r] * lnC0, m.exptab) * Pr;
       }
       double keff = kf, Mfac = 1.0;
       if (type != 0) {
@@ -201,6 +201,27 @@ k_thermo(const uint8_t* __restrict__ img, ImageLayout L, int64_t n, int layout, 
     if (cpo) cpo[i] = cpm * m.r_thermo;
     if (ho) ho[i] = hm * m.r_thermo * T;
   }
+}
+
+// ---------------------------------------------------------------- exp self-test
+__global__ void k_exp_selftest(const uint8_t* __restrict__ img, ImageLayout L, int64_t n,
+                               const double* __restrict__ x, double* __restrict__ y) {
+  extern __shared__ __align__(16) uint8_t smem[];
+  stage_image(smem, img, L.bytes);
+  MechView m;
+  m.bind(L, smem);
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    y[2 * i] = fexp(x[i], m.exptab);
+    y[2 * i + 1] = exp(x[i]);
+  }
+}
+
+cudaError_t launch_exp_selftest(const uint8_t* img, const ImageLayout& L, int64_t n, const double* x, double* y,
+                                cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  k_exp_selftest<<<256, 256, L.bytes, st>>>(img, L, n, x, y);
+  count_launch();
+  return cudaGetLastError();
 }
 
 // ---------------------------------------------------------------- FP64 probe

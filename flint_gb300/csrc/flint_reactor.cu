@@ -20,7 +20,9 @@
 // failure with a stale matrix; step and order chosen every q+1 steps from the
 // order q-1, q, q+1 error estimates.  The Newton matrix I - gamma*J is factored
 // in shared memory by a row-per-lane LU with partial pivoting that records the
-// pivot order instead of swapping rows.
+// pivot order instead of swapping rows.  Step-size factors eta = (c*dsm)^(-1/(q+1))
+// are heuristics and are evaluated in FP32 (the oracle does the same); every
+// quantity of the solution itself stays FP64.
 #include "flint_dev.cuh"
 #include "flint_host.h"
 
@@ -45,9 +47,19 @@ static void bdf_coeffs(BdfL& B) {
 __constant__ BdfL c_bdf;
 
 // Work counters of the last reactor launch (device side, summed per cell):
-// [0] work-stealing cursor, [1] RHS evaluations, [2] Jacobian + LU refreshes,
-// [3] Newton iterations (LU solves), [4] accepted steps, [5] rejected attempts.
-constexpr int NCOUNTERS = 6;
+// [0] work-stealing cursor, [1] RHS evaluations, [2] Jacobian evaluations,
+// [3] Newton iterations (LU solves), [4] accepted steps, [5] rejected attempts,
+// [6] LU factorizations.
+constexpr int NCOUNTERS = 7;
+// Jacobian reuse (the CVODE policy): the Newton matrix I - gamma*J is rebuilt
+// and factored when gamma moved by more than DGMAX or MSBP steps passed; the
+// Jacobian itself is re-evaluated only every MSBJ steps or after a Newton
+// failure with a stale Jacobian.  Between evaluations the last Jacobian is kept
+// in a per-warp slot of global scratch (one slot per resident warp).
+constexpr double DGMAX = 0.3;
+constexpr int MSBP = 20;
+constexpr int MSBJ = 50;
+constexpr int JSLOT = 32 * 32;   // doubles per saved-Jacobian slot
 
 __device__ inline double wrms(double v, double w, bool act, int nv) {
   double t = act ? v * w : 0.0;
@@ -105,7 +117,7 @@ __global__ void __launch_bounds__(REACTOR_THREADS)
 k_reactor(const uint8_t* __restrict__ img, ImageLayout L, int64_t n, double* __restrict__ Tg,
           const double* __restrict__ pg, double* __restrict__ Yg, const double* __restrict__ dtg,
           flint_reactor_opts o, int* __restrict__ status_g, int* __restrict__ nsteps_g,
-          unsigned long long* __restrict__ counter) {
+          unsigned long long* __restrict__ counter, double* __restrict__ jsave) {
   extern __shared__ __align__(16) uint8_t smem[];
   stage_image(smem, img, L.bytes);
   MechView m;
@@ -120,7 +132,8 @@ k_reactor(const uint8_t* __restrict__ img, ImageLayout L, int64_t n, double* __r
   const int ld = s.ldj;
   const BdfL& B = c_bdf;
   const int qmax = o.max_order;
-  unsigned long long n_rhs = 0, n_jac = 0, n_newt = 0, n_rej = 0;
+  unsigned long long n_rhs = 0, n_jac = 0, n_newt = 0, n_rej = 0, n_lu = 0;
+  double* Jg = jsave + (size_t)(blockIdx.x * (blockDim.x >> 5) + wid) * JSLOT;
 
   while (true) {
     unsigned long long c0 = 0;
@@ -160,7 +173,7 @@ k_reactor(const uint8_t* __restrict__ img, ImageLayout L, int64_t n, double* __r
       z[1] = h * f;
       int q = 1;
       double t = 0.0;
-      int ialth = 2, have_J = 0, jfresh = 0, nstJ = 0, have_eprev = 0, last = 0;
+      int ialth = 2, have_J = 0, jfresh = 0, nstJ = 0, nstP = 0, have_eprev = 0, last = 0;
       double gammaJ = 0.0, crate = 1.0, etamax = 1.0e4;
       int mystep = 0;
 
@@ -191,17 +204,24 @@ k_reactor(const uint8_t* __restrict__ img, ImageLayout L, int64_t n, double* __r
           const double l1 = B.l[q][1];
           const double gamma = h / l1;
           const double ypred = z[0];
-          if (!have_J || need_J || fabs(gamma / gammaJ - 1.0) > 0.3 || nst >= nstJ + 20) {
-            const double Tv = __shfl_sync(FULL, ypred, ns);
-            ++n_jac;
-            warp_kinetics<true>(m, s, lane, lane < ns ? ypred : 0.0, Tv, p, co);
-            if (act) {
-              double* row = s.Jr + lane * ld;
-              for (int j = 0; j < nv; ++j) row[j] = (j == lane ? 1.0 : 0.0) - gamma * row[j];
+          if (!have_J || need_J || fabs(gamma / gammaJ - 1.0) > DGMAX || nst >= nstP + MSBP) {
+            double* row = s.Jr + lane * ld;
+            if (!have_J || need_J || nst >= nstJ + MSBJ) {
+              const double Tv = __shfl_sync(FULL, ypred, ns);
+              ++n_jac;
+              warp_kinetics<true>(m, s, lane, lane < ns ? ypred : 0.0, Tv, p, co);
+              if (act)
+                for (int j = 0; j < nv; ++j) Jg[j * 32 + lane] = row[j];
+              have_J = 1; jfresh = 1; nstJ = nst; need_J = 0;
+            } else if (act) {
+              for (int j = 0; j < nv; ++j) row[j] = Jg[j * 32 + lane];
             }
+            if (act)
+              for (int j = 0; j < nv; ++j) row[j] = (j == lane ? 1.0 : 0.0) - gamma * row[j];
             __syncwarp();
+            ++n_lu;
             warp_lu(s.Jr, ld, nv, lane, pivs, mystep);
-            have_J = 1; jfresh = 1; gammaJ = gamma; nstJ = nst; crate = 1.0; need_J = 0;
+            gammaJ = gamma; nstP = nst; crate = 1.0;
           }
           const double gamrat = gamma / gammaJ;
           e = 0.0;
@@ -250,7 +270,7 @@ k_reactor(const uint8_t* __restrict__ img, ImageLayout L, int64_t n, double* __r
               eta = 0.1;
               if (q > 1) q = 1;
             } else {
-              eta = 1.0 / (pow(1.2 * dsm, 1.0 / (q + 1)) + 1e-6);
+              eta = 1.0 / ((double)powf((float)(1.2 * dsm), 1.0f / (float)(q + 1)) + 1e-6);
               if (eta > 0.9) eta = 0.9;
               if (eta < 0.1) eta = 0.1;
             }
@@ -273,7 +293,7 @@ k_reactor(const uint8_t* __restrict__ img, ImageLayout L, int64_t n, double* __r
         double eta = 1.0;
         if (ialth <= 0) {
           const double l1 = B.l[q][1];
-          const double etaq = 1.0 / (pow(1.2 * dsm, 1.0 / (q + 1)) + 1.2e-6);
+          const double etaq = 1.0 / ((double)powf((float)(1.2 * dsm), 1.0f / (float)(q + 1)) + 1.2e-6);
           double etadn = 0.0, etaup = 0.0;
           if (q > 1) {
             double fact = 1.0;
@@ -282,12 +302,12 @@ k_reactor(const uint8_t* __restrict__ img, ImageLayout L, int64_t n, double* __r
 #pragma unroll
             for (int j = 2; j <= 5; ++j) if (j == q) zq = z[j];
             const double ddn = wrms(zq, ewt, act, nv) * fact / ((double)q * B.l[q - 1][1]);
-            etadn = 1.0 / (pow(1.3 * ddn, 1.0 / q) + 1.3e-6);
+            etadn = 1.0 / ((double)powf((float)(1.3 * ddn), 1.0f / (float)q) + 1.3e-6);
           }
           if (q < qmax && have_eprev) {
             const double Kq = 1.0 + 1.0 / ((double)(q + 1) * l1);
             const double dup = wrms(e - eprev, ewt, act, nv) / (Kq * (double)(q + 2) * B.l[q + 1][1]);
-            etaup = 1.0 / (pow(1.4 * dup, 1.0 / (q + 2)) + 1.4e-6);
+            etaup = 1.0 / ((double)powf((float)(1.4 * dup), 1.0f / (float)(q + 2)) + 1.4e-6);
           }
           int newq = q;
           eta = etaq;
@@ -335,6 +355,7 @@ k_reactor(const uint8_t* __restrict__ img, ImageLayout L, int64_t n, double* __r
     atomicAdd(counter + 2, n_jac);
     atomicAdd(counter + 3, n_newt);
     atomicAdd(counter + 5, n_rej);
+    atomicAdd(counter + 6, n_lu);
   }
 }
 
@@ -342,9 +363,19 @@ size_t reactor_smem(const ImageLayout& L) {
   return L.bytes + (REACTOR_THREADS / 32) * (scratch_doubles(L.nsp, L.nrpad, true) * sizeof(double) + 32 * sizeof(int));
 }
 
+int reactor_slots(const ImageLayout& L) {
+  size_t sm = reactor_smem(L);
+  if (cudaFuncSetAttribute(k_reactor, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) != cudaSuccess) return 0;
+  int per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_reactor, REACTOR_THREADS, sm);
+  return per_sm * device_sms() * (REACTOR_THREADS / 32);
+}
+
+size_t reactor_slot_bytes() { return JSLOT * sizeof(double); }
+
 cudaError_t launch_reactor(const uint8_t* img, const ImageLayout& L, int64_t n, double* T, const double* p,
                            double* Y, const double* dt, const flint_reactor_opts& o, int* status, int* nsteps,
-                           unsigned int* work_counter, cudaStream_t st) {
+                           unsigned int* work_counter, double* jsave, int slots, cudaStream_t st) {
   if (n <= 0) return cudaSuccess;
   size_t sm = reactor_smem(L);
   cudaError_t e = cudaFuncSetAttribute(k_reactor, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
@@ -356,6 +387,8 @@ cudaError_t launch_reactor(const uint8_t* img, const ImageLayout& L, int64_t n, 
   int64_t blocks = (warps_needed + REACTOR_THREADS / 32 - 1) / (REACTOR_THREADS / 32);
   int64_t full = (int64_t)device_sms() * per_sm;
   if (blocks > full) blocks = full;
+  if (blocks * (REACTOR_THREADS / 32) > slots) blocks = slots / (REACTOR_THREADS / 32);
+  if (blocks < 1) return cudaErrorInvalidValue;
   static bool bdf_ready = false;
   if (!bdf_ready) {
     BdfL B;
@@ -367,7 +400,7 @@ cudaError_t launch_reactor(const uint8_t* img, const ImageLayout& L, int64_t n, 
   e = cudaMemsetAsync(work_counter, 0, NCOUNTERS * sizeof(unsigned long long), st);
   if (e != cudaSuccess) return e;
   k_reactor<<<(unsigned)blocks, REACTOR_THREADS, sm, st>>>(img, L, n, T, p, Y, dt, o, status, nsteps,
-                                                            reinterpret_cast<unsigned long long*>(work_counter));
+                                                            reinterpret_cast<unsigned long long*>(work_counter), jsave);
   count_launch();
   return cudaGetLastError();
 }

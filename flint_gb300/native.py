@@ -33,6 +33,19 @@ class MechDesc(C.Structure):
                 ("r_eos", C.c_double), ("r_thermo", C.c_double), ("p_ref", C.c_double)]
 
 
+class TableDesc(C.Structure):
+    """flint_table_desc: FLINT's tabulated module arrays (Fortran layout)."""
+    _fields_ = [("ns", C.c_int), ("nr_arrh", C.c_int), ("nr_troe", C.c_int), ("nr_lind", C.c_int),
+                ("tmin", C.c_int), ("tmax", C.c_int), ("ti1", C.c_int), ("ti2", C.c_int),
+                ("wm", _dp), ("cp_tab", _dp), ("h_tab", _dp), ("kf_tab", _dp), ("kb_tab", _dp),
+                ("kinf_troe", _dp), ("k0_troe", _dp), ("kc_troe", _dp), ("fcent_troe", _dp),
+                ("kinf_lind", _dp), ("k0_lind", _dp), ("kc_lind", _dp),
+                ("ni1_arrh", _dp), ("ni2_arrh", _dp), ("eps_arrh", _dp),
+                ("ni1_troe", _dp), ("ni2_troe", _dp), ("eps_troe", _dp),
+                ("ni1_lind", _dp), ("ni2_lind", _dp), ("eps_lind", _dp),
+                ("runiv", C.c_double)]
+
+
 class ReactorOpts(C.Structure):
     """flint_reactor_opts."""
     _fields_ = [("rtol", C.c_double), ("atol", C.c_double), ("max_steps", C.c_int),
@@ -96,6 +109,9 @@ def lib():
     L.flint_reactor_default_opts.argtypes = [C.POINTER(ReactorOpts)]
     L.flint_reactor_stats.argtypes = [vp, C.POINTER(C.c_int64)]
     L.flint_probe_fp64_peak.argtypes = [C.POINTER(C.c_double)]
+    L.flint_selftest_exp.argtypes = [vp, i64, vp, vp, vp]
+    L.flint_mech_create_tables.argtypes = [C.POINTER(TableDesc), C.POINTER(vp)]
+    L.flint_rhs_native_batch.argtypes = [vp, i64, vp, vp, vp]
     L.flint_wdot_batch_host.argtypes = [vp, i64, C.c_int, vp, vp, vp, vp, vp, vp]
     L.flint_wdot_jac_batch_host.argtypes = [vp, i64, C.c_int, vp, vp, vp, vp, vp]
     L.flint_reactor_advance_host.argtypes = [vp, i64, vp, vp, vp, vp, C.POINTER(ReactorOpts), vp, vp]

@@ -98,6 +98,40 @@ typedef struct {
   double p_ref;           /* standard pressure of Kc, Pa (101325)            */
 } flint_mech_desc;
 
+/* Tabulated mechanism: FLINT's own module arrays as read_idealgas_thermo and
+ * read_chemistry leave them (Lib_ThermoTransport.f90:10-23,
+ * Lib_Chemistry_data.f90:4-32), in their Fortran layout, 1-K rows.  A FLINT
+ * caller passes c_loc() of its arrays; flint_gb300.tables reads the same files
+ * in Python.  Rows run tmin..tmax (thermo) and ti1..ti2 (rates). */
+typedef struct {
+  int ns;
+  int nr_arrh, nr_troe, nr_lind;
+  int tmin, tmax;              /* thermo rows tmin..tmax                       */
+  int ti1, ti2;                /* rate-table rows ti1..ti2                     */
+  const double* wm;            /* [ns] molar mass                              */
+  const double* cp_tab;        /* cp_tab(tmin:tmax, ns)  J/kg/K                */
+  const double* h_tab;         /* h_tab(tmin:tmax, ns)   J/kg                  */
+  const double* kf_tab;        /* kf_tab(ti1:ti2, nr_arrh)                     */
+  const double* kb_tab;        /* kb_tab(ti1:ti2, nr_arrh)                     */
+  const double* kinf_troe;     /* (ti1:ti2, nr_troe), likewise k0, kc, Fcent    */
+  const double* k0_troe;
+  const double* kc_troe;
+  const double* fcent_troe;
+  const double* kinf_lind;     /* (ti1:ti2, nr_lind), likewise k0, kc           */
+  const double* k0_lind;
+  const double* kc_lind;
+  const double* ni1_arrh;      /* ni1_arrh_tab(ns+1, nr_arrh); row ns+1 = "M"   */
+  const double* ni2_arrh;
+  const double* eps_arrh;
+  const double* ni1_troe;      /* (ns+1, nr_troe)                               */
+  const double* ni2_troe;
+  const double* eps_troe;
+  const double* ni1_lind;      /* (ns+1, nr_lind)                               */
+  const double* ni2_lind;
+  const double* eps_lind;
+  double runiv;                /* Runiv of the EOS terms (8314.51)             */
+} flint_table_desc;
+
 /* Integrator options of the batched 0D reactor. */
 typedef struct {
   double rtol;            /* relative tolerance (all components)            */
@@ -113,6 +147,11 @@ typedef struct {
 /* Replaces read_idealgas_thermo + read_chemistry + Assign_Mechanism for an
  * analytic mechanism: copies the description to device memory owned by *out. */
 int flint_mech_create(const flint_mech_desc* desc, flint_mech_t* out);
+/* Replaces read_idealgas_thermo + read_chemistry + Assign_Mechanism for the
+ * reference's tabulated data (the `general` path, Lib_Chemistry_wdot.f90:96-220):
+ * copies the tables to device memory owned by *out.  Handles made this way
+ * serve flint_chemistry_source_batch and flint_rhs_native_batch. */
+int flint_mech_create_tables(const flint_table_desc* desc, flint_mech_t* out);
 /* Replaces free_chemistry_data (Lib_Chemistry_data.f90:168). */
 int flint_mech_destroy(flint_mech_t mech);
 /* Text of the last error on the calling thread ("" if none). */
@@ -137,10 +176,19 @@ int flint_wdot_batch(flint_mech_t mech, int64_t n, int layout, const double* T,
                      double* h, void* stream);
 
 /* chemistry_source(roi, temp, omegadot) over N cells, cell-major rho_i input
- * (Fortran (ns, N)).  Negative rho_i are clamped to zero in place, as the
- * reference mechanisms do (WD.f90:19, Lib_Chemistry_rhs.f90:37-39). */
+ * (Fortran (ns, N)).  Analytic handles clamp negative rho_i to zero in place, as
+ * the reference mechanisms do (WD.f90:19, Lib_Chemistry_rhs.f90:37-39);
+ * tabulated handles run the general loop on roi as given, as `general` does.
+ * For a tabulated handle, temperatures outside the rate table use its edge
+ * rows (the reference reads past the table there). */
 int flint_chemistry_source_batch(flint_mech_t mech, int64_t n, double* roi,
                                  const double* T, double* omegadot, void* stream);
+
+/* rhs_native(nz, time, Z, F) over N cells (Lib_Chemistry_rhs.f90:15-52):
+ * Z, F cell-major (ns+1) per cell, Z = (rho_1..rho_ns, T); constant-volume
+ * energy equation from the tabulated h and cp; F = -1 for a cell whose T is
+ * outside the thermo table or NaN, as the reference returns.  Tabulated handles. */
+int flint_rhs_native_batch(flint_mech_t mech, int64_t n, const double* Z, double* F, void* stream);
 
 /* wdot and the analytic Jacobian of the constant-pressure reactor right-hand
  * side, J = d(dY/dt, dT/dt)/d(Y, T), (ns+1)^2 per cell stored column-major
@@ -165,11 +213,12 @@ int flint_reactor_advance(flint_mech_t mech, int64_t n, double* T, const double*
                           int* status, int* nsteps, void* stream);
 
 /* Work counters of the last flint_reactor_advance on this handle (blocks until
- * it has finished): out[0] RHS evaluations, out[1] Jacobian + LU refreshes,
+ * it has finished): out[0] RHS evaluations, out[1] Jacobian evaluations,
  * out[2] Newton iterations (one LU solve each), out[3] accepted steps,
- * out[4] rejected step attempts.  No reference counterpart: instrumentation
- * (the CVODE statistics test-batchCXX.cpp:25-48 prints are its nearest kin). */
-int flint_reactor_stats(flint_mech_t mech, int64_t out[5]);
+ * out[4] rejected step attempts, out[5] LU factorizations.  No reference
+ * counterpart: instrumentation (the CVODE statistics test-batchCXX.cpp:25-48
+ * prints are its nearest kin). */
+int flint_reactor_stats(flint_mech_t mech, int64_t out[6]);
 
 /* Default options: rtol 1e-8, atol 1e-14, 20000 steps, order 5, constant p. */
 void flint_reactor_default_opts(flint_reactor_opts* opts);
@@ -188,6 +237,11 @@ int flint_reactor_advance_host(flint_mech_t mech, int64_t n, double* T, const do
  * the default stream with an independent-FMA-chain kernel; the denominator of
  * the FP64 roofline.  No reference counterpart: instrumentation. */
 int flint_probe_fp64_peak(double* tflops);
+
+/* Diagnostic: y[2i] = the kernels' table-driven exp(x[i]), y[2i+1] = CUDA's
+ * exp(x[i]) (device pointers).  No reference counterpart: lets tests bound the
+ * kernels' exp against the CUDA library. */
+int flint_selftest_exp(flint_mech_t mech, int64_t n, const double* x, double* y, void* stream);
 
 /* Number of kernels the library launched since load (instrumentation). */
 int64_t flint_kernel_launch_count(void);

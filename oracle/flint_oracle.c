@@ -508,7 +508,9 @@ static void jac_y(const rhs_ctx* cx, const double* y, double* J) {
   orc_jac_cell(cx->m, y[ns], cx->p, y, f, J, NULL);
 }
 
-/* One cell of the reactor.  Returns the FLINT_CELL_* status. */
+/* One cell of the reactor.  Returns the FLINT_CELL_* status.  The step-size
+ * factors eta = (c*dsm)^(-1/(q+1)) are heuristics evaluated in FP32, as the GPU
+ * does; the solution itself is FP64 throughout. */
 static int bdf_cell(const rhs_ctx* cx, int n, double* y, double tout, const flint_reactor_opts* o,
                     int* nsteps_out) {
   double z[6][MAXNS + 1], zs[6][MAXNS + 1];
@@ -534,7 +536,7 @@ static int bdf_cell(const rhs_ctx* cx, int n, double* y, double tout, const flin
   int ialth = 2;            /* steps until the next step-size / order decision */
   int have_J = 0, jfresh = 0;
   double gammaJ = 0.0;
-  int nstJ = 0;
+  int nstJ = 0, nstP = 0;
   double crate = 1.0;
   double etamax = 1.0e4;
   int have_eprev = 0;
@@ -566,12 +568,17 @@ static int bdf_cell(const rhs_ctx* cx, int n, double* y, double tout, const flin
       double l1 = L[q][1];
       double gamma = h / l1;
       for (int i = 0; i < n; ++i) ypred[i] = z[0][i];
-      if (!have_J || need_J || fabs(gamma / gammaJ - 1.0) > 0.3 || nst >= nstJ + 20) {
-        jac_y(cx, ypred, J);
+      /* Newton matrix refresh (gamma moved > 30 % or 20 steps) and Jacobian
+       * re-evaluation (50 steps or a failure with a stale one): CVODE's policy. */
+      if (!have_J || need_J || fabs(gamma / gammaJ - 1.0) > 0.3 || nst >= nstP + 20) {
+        if (!have_J || need_J || nst >= nstJ + 50) {
+          jac_y(cx, ypred, J);
+          have_J = 1; jfresh = 1; nstJ = nst; need_J = 0;
+        }
         for (int j = 0; j < n; ++j)
           for (int i = 0; i < n; ++i) Mlu[j * n + i] = (i == j ? 1.0 : 0.0) - gamma * J[j * n + i];
         lu_factor(n, Mlu, piv);
-        have_J = 1; jfresh = 1; gammaJ = gamma; nstJ = nst; crate = 1.0; need_J = 0;
+        gammaJ = gamma; nstP = nst; crate = 1.0;
       }
       double gamrat = gamma / gammaJ;
       /* Newton iteration on e = y - ypred */
@@ -612,7 +619,7 @@ static int bdf_cell(const rhs_ctx* cx, int n, double* y, double tout, const flin
           eta = 0.1;
           if (q > 1) q = 1;
         } else {
-          eta = 1.0 / (pow(1.2 * dsm, 1.0 / (q + 1)) + 1e-6);
+          eta = 1.0 / ((double)powf((float)(1.2 * dsm), 1.0f / (float)(q + 1)) + 1e-6);
           if (eta > 0.9) eta = 0.9;
           if (eta < 0.1) eta = 0.1;
         }
@@ -634,20 +641,20 @@ static int bdf_cell(const rhs_ctx* cx, int n, double* y, double tout, const flin
     double eta = 1.0;
     if (ialth <= 0) {
       double l1 = L[q][1];
-      double etaq = 1.0 / (pow(1.2 * dsm, 1.0 / (q + 1)) + 1.2e-6);
+      double etaq = 1.0 / ((double)powf((float)(1.2 * dsm), 1.0f / (float)(q + 1)) + 1.2e-6);
       double etadn = 0.0, etaup = 0.0;
       if (q > 1) {
         double fact = 1.0;
         for (int i = 2; i <= q; ++i) fact *= i;
         double ddn = wrms(n, z[q], ewt) * fact / ((double)q * L[q - 1][1]);
-        etadn = 1.0 / (pow(1.3 * ddn, 1.0 / q) + 1.3e-6);
+        etadn = 1.0 / ((double)powf((float)(1.3 * ddn), 1.0f / (float)q) + 1.3e-6);
       }
       if (q < qmax && have_eprev) {
         double d[MAXNS + 1];
         for (int i = 0; i < n; ++i) d[i] = e[i] - eprev[i];
         double Kq = 1.0 + 1.0 / ((double)(q + 1) * l1);
         double dup = wrms(n, d, ewt) / (Kq * (double)(q + 2) * L[q + 1][1]);
-        etaup = 1.0 / (pow(1.4 * dup, 1.0 / (q + 2)) + 1.4e-6);
+        etaup = 1.0 / ((double)powf((float)(1.4 * dup), 1.0f / (float)(q + 2)) + 1.4e-6);
       }
       int newq = q;
       eta = etaq;
@@ -713,8 +720,10 @@ void orc_reactor_advance(const flint_mech_desc* m, int64_t n, double* T, const d
 /* ------------------------------------------------------- TABLE mode (reference) */
 /* comp_ch_tabT: a + (b-a)*Tdiff on rows T_i, T_i+1 (Lib_Chemistry_data.f90:36-48). */
 static double lerp_tab(const double* tab, int row0, int nrows, int col, int Ti, double Tdiff) {
-  double a = tab[(int64_t)col * nrows + (Ti - row0)];
-  double b = tab[(int64_t)col * nrows + (Ti + 1 - row0)];
+  int row = Ti - row0;   /* edge rows outside the table (the reference reads past it) */
+  row = row < 0 ? 0 : (row > nrows - 2 ? nrows - 2 : row);
+  double a = tab[(int64_t)col * nrows + row];
+  double b = tab[(int64_t)col * nrows + row + 1];
   return a + (b - a) * Tdiff;
 }
 
@@ -818,8 +827,9 @@ void orc_rhs_native(const orc_table_mech* m, int nz, const double* Z, double* F)
   for (int s = 0; s < ns; ++s) {
     double hs = lerp_tab(m->h_tab, m->tmin, nrows, s, Ti, Tdiff);
     double cps = lerp_tab(m->cp_tab, m->tmin, nrows, s, Ti, Tdiff);
-    eiroi = eiroi + (hs - m->ri[s] * T) * droic[s];
-    rho_cv = rho_cv + roi[s] * (cps - m->ri[s]);
+    double ri = m->runiv / m->wm[s];   /* Ri_tab = Runiv/wm_tab, Load_ThermoTransport.f90:54 */
+    eiroi = eiroi + (hs - ri * T) * droic[s];
+    rho_cv = rho_cv + roi[s] * (cps - ri);
   }
   for (int s = 0; s < ns; ++s) F[s] = droic[s];
   F[nz - 1] = -eiroi / rho_cv;

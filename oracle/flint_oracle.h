@@ -60,24 +60,9 @@ void orc_reactor_advance(const flint_mech_desc* m, int64_t n, double* T, const d
                          double* Y, const double* dt, const flint_reactor_opts* o,
                          int* status, int* nsteps, int nthreads);
 
-/* Reference-restatement (TABLE mode) of FLINT's general loop and rhs_native. */
-typedef struct {
-  int ns;
-  int nr_arrh, nr_troe, nr_lind;
-  int tmin, tmax;            /* thermo table rows tmin..tmax                 */
-  int ti1, ti2;              /* rate table rows ti1..ti2                      */
-  const double* wm;          /* [ns]                                          */
-  const double* ri;          /* [ns] Runiv/wm                                 */
-  const double* cp_tab;      /* Fortran (tmin:tmax, ns): [s*(tmax-tmin+1) + (T-tmin)] */
-  const double* h_tab;
-  const double* kf_tab;      /* Fortran (ti1:ti2, nr_arrh)                    */
-  const double* kb_tab;
-  const double* kinf_troe, *k0_troe, *kc_troe, *fcent_troe;  /* (ti1:ti2, nr_troe) */
-  const double* kinf_lind, *k0_lind, *kc_lind;                /* (ti1:ti2, nr_lind) */
-  const double* ni1_arrh, *ni2_arrh, *eps_arrh;  /* Fortran (ns+1, nr_arrh)   */
-  const double* ni1_troe, *ni2_troe, *eps_troe;
-  const double* ni1_lind, *ni2_lind, *eps_lind;
-} orc_table_mech;
+/* Reference restatement of FLINT's general loop and rhs_native on the tabulated
+ * mechanism of include/flint_gpu.h (flint_table_desc). */
+typedef flint_table_desc orc_table_mech;
 
 /* general(roi, temp, omegadot), Lib_Chemistry_wdot.f90:96-220. */
 void orc_general(const orc_table_mech* m, const double* roi, double temp, double* omegadot);

@@ -11,7 +11,7 @@ import subprocess
 
 import numpy as np
 
-from flint_gb300.native import MechDesc, ReactorOpts, mech_desc, ptr
+from flint_gb300.native import MechDesc, ReactorOpts, TableDesc, mech_desc, ptr
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 SO = os.path.join(HERE, "_build", "liboracle.so")
@@ -40,6 +40,9 @@ def lib():
         L.orc_wdot_jac_batch.argtypes = [md, i64, C.c_int, vp, vp, vp, vp, vp, vp, C.c_int]
         L.orc_reactor_advance.argtypes = [md, i64, vp, vp, vp, vp, C.POINTER(ReactorOpts), vp, vp, C.c_int]
         L.orc_max_threads.restype = C.c_int
+        td = C.POINTER(TableDesc)
+        L.orc_general_batch.argtypes = [td, i64, vp, vp, vp, C.c_int]
+        L.orc_rhs_native_batch.argtypes = [td, i64, vp, vp, C.c_int]
         _lib = L
     return _lib
 
@@ -113,3 +116,26 @@ class Oracle:
     @staticmethod
     def max_threads():
         return lib().orc_max_threads()
+
+
+class TableOracle:
+    """Oracle of FLINT's general loop and rhs_native on a table dict."""
+
+    def __init__(self, t):
+        from flint_gb300.tables import table_desc
+        self.t = t
+        self.desc, self._keep = table_desc(t)
+        self.ns = t["ns"]
+        self.L = lib()
+
+    def general(self, roi, T, nthreads=0):
+        roi = np.ascontiguousarray(roi, dtype=np.float64); T = np.ascontiguousarray(T, dtype=np.float64)
+        out = np.zeros_like(roi)
+        self.L.orc_general_batch(C.byref(self.desc), T.shape[0], _vp(roi), _vp(T), _vp(out), nthreads)
+        return out
+
+    def rhs_native(self, Z, nthreads=0):
+        Z = np.ascontiguousarray(Z, dtype=np.float64)
+        F = np.zeros_like(Z)
+        self.L.orc_rhs_native_batch(C.byref(self.desc), Z.shape[0], _vp(Z), _vp(F), nthreads)
+        return F
