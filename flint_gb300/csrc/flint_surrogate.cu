@@ -1,0 +1,557 @@
+// flint_surrogate.cu -- learned reactor surrogate with a residual gate and an
+// FP64 integrator fallback.
+//
+// A cell (T0, p, Y0, dt) is mapped by an MLP (flint_mlp.cu) to (dY, dT) over dt.
+// The prediction is then made exactly conservative and checked:
+//   * element conservation: dY is projected onto the null space of the
+//     element matrix (mass fractions: sum_k a_ek dY_k / W_k = 0; total mass
+//     follows), P = I - B^T (B B^T)^-1 B;
+//   * energy conservation (adiabatic, constant p): T1 solves h(T1, Y1) = h(T0, Y0)
+//     by Newton on the NASA-7 enthalpy, started from the network's T0 + dT;
+// and the cell is accepted only if the residuals of the raw prediction are
+// small: |T1(h) - (T0 + dT_net)| (energy residual), the element residual
+// |B dY_net| (projection size), min Y1 (realizability), the input inside the
+// training domain, and (two networks) the ensemble disagreement.  Rejected
+// cells are compacted and re-solved by the BDF integrator (flint_reactor.cu)
+// from their original state, so every result is either a gated surrogate
+// step or an FP64 integrator step.
+//
+// Features (n_in = ns + 2): log10(max(Y_k, 1e-20)) of every species but the
+// bath species, T, log10 p, log10 dt; targets (n_out = ns + 1): dY_k, dT.
+// Both normalised by the training-set mean and standard deviation.
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+#include <algorithm>
+#include <cuda_bf16.h>
+
+#include "flint_host.h"
+
+namespace flint {
+
+struct GemmArgs;
+enum { EPI_STORE = 0, EPI_BIAS = 1, EPI_BIAS_GELU = 2, EPI_GELU_BWD = 3 };
+struct GemmArgs {
+  int M, N, K;
+  const void* A; int a_bf16; int64_t sa_m, sa_k;
+  const void* B; int b_bf16; int64_t sb_k, sb_n;
+  const float* bias;
+  float* C; int64_t ldc;
+  __nv_bfloat16* Cb; int64_t ldcb;
+  const float* Zprev; int64_t ldz;
+  int epi;
+  int accumulate;
+};
+cudaError_t launch_gemm(const GemmArgs& g, cudaStream_t st);
+cudaError_t launch_colsum(const float* dZ, int M, int N, int64_t ld, float* db, int acc, cudaStream_t st);
+cudaError_t launch_mse(const float* yhat, const float* y, int64_t total, float scale, float* grad, double* loss,
+                       cudaStream_t st);
+cudaError_t launch_adam(float* w, const float* gw, float* m1, float* m2, __nv_bfloat16* wb, int64_t n, float lr,
+                        float b1, float b2, float eps, float bc1, float bc2, float wd, cudaStream_t st);
+cudaError_t launch_to_bf16(const float* x, __nv_bfloat16* y, int64_t n, cudaStream_t st);
+
+constexpr int MAXL = 8;
+constexpr int SURR_THREADS = 128;
+
+struct Net {
+  int nl = 0;
+  int dims[MAXL + 1] = {0};
+  int64_t off_w[MAXL] = {0}, off_b[MAXL] = {0}, P = 0;
+  float *w = nullptr, *g = nullptr, *m1 = nullptr, *m2 = nullptr;
+  __nv_bfloat16* wb = nullptr;
+  int64_t step = 0;
+};
+
+struct Surrogate {
+  const uint8_t* mimg;      // analytic mechanism image (device)
+  ImageLayout L;
+  unsigned int* counter;    // reactor counters (device)
+  double* jsave;            // reactor scratch (device)
+  int jslots;
+  int ns, bath, n_in, n_out, nnets, H;
+  Net net[2];
+  float *xmean, *xstd, *ymean, *ystd;   // device, host copies below
+  std::vector<float> hxm, hxs, hym, hys;
+  double* proj;             // [ns][ns] projector (device)
+  double* Bm;               // [ne][ns] element rows divided by W (device)
+  int ne;
+  // workspaces
+  int64_t cap = 0;          // rows of the training / inference workspaces
+  float* Z[MAXL] = {nullptr};
+  __nv_bfloat16* A[MAXL] = {nullptr};
+  float *dz0 = nullptr, *dz1 = nullptr, *yhat = nullptr, *xf = nullptr, *yout2 = nullptr;
+  double* loss = nullptr;
+  // fallback compaction
+  int64_t* rej_idx = nullptr;
+  unsigned long long* rej_count = nullptr;
+  double *cT = nullptr, *cp = nullptr, *cY = nullptr, *cdt = nullptr;
+  int *cst = nullptr, *cns = nullptr;
+  int64_t last_accepted = 0, last_rejected = 0, last_fallback_steps = 0;
+};
+
+// ------------------------------------------------------------------ kernels
+__global__ void k_features(int64_t n, int ns, int bath, const double* __restrict__ T, const double* __restrict__ p,
+                           const double* __restrict__ Y, const double* __restrict__ dt,
+                           const float* __restrict__ xm, const float* __restrict__ xs, float* __restrict__ X) {
+  const int nin = ns + 2;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    float* x = X + i * nin;
+    int c = 0;
+    for (int k = 0; k < ns; ++k) {
+      if (k == bath) continue;
+      double y = Y[i * ns + k];
+      x[c] = (float)((log10(y > 1e-20 ? y : 1e-20) - xm[c]) / xs[c]);
+      ++c;
+    }
+    x[c] = (float)((T[i] - xm[c]) / xs[c]); ++c;
+    x[c] = (float)((log10(p[i]) - xm[c]) / xs[c]); ++c;
+    x[c] = (float)((log10(dt[i]) - xm[c]) / xs[c]);
+  }
+}
+
+__global__ void k_targets(int64_t n, int ns, const double* __restrict__ T0, const double* __restrict__ Y0,
+                          const double* __restrict__ T1, const double* __restrict__ Y1, const float* __restrict__ ym,
+                          const float* __restrict__ ys, float* __restrict__ Yt) {
+  const int nout = ns + 1;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    for (int k = 0; k < ns; ++k) Yt[i * nout + k] = (float)((Y1[i * ns + k] - Y0[i * ns + k] - ym[k]) / ys[k]);
+    Yt[i * nout + ns] = (float)((T1[i] - T0[i] - ym[ns]) / ys[ns]);
+  }
+}
+
+struct GateParams {
+  double max_dT_resid, max_elem_resid, min_Y, max_ens_dT, max_ens_dY;
+  double Tlo, Thi, lpl, lph, ldl, ldh;
+};
+
+// Post-processing and gate, one thread per cell.  Accepted cells are written
+// in place; rejected ones are listed for the fallback (their T, Y untouched).
+__global__ void __launch_bounds__(SURR_THREADS)
+k_post(const uint8_t* __restrict__ img, ImageLayout L, int64_t n, int64_t base, double* __restrict__ T,
+       const double* __restrict__ p, double* __restrict__ Y, const double* __restrict__ dt,
+       const float* __restrict__ yn, const float* __restrict__ yn2, const float* __restrict__ ym,
+       const float* __restrict__ ys, const double* __restrict__ proj, const double* __restrict__ Bm, int ne,
+       GateParams gp, int* __restrict__ status, int* __restrict__ nsteps, int64_t* __restrict__ rej_idx,
+       unsigned long long* __restrict__ rej_count) {
+  extern __shared__ __align__(16) uint8_t smem[];
+  stage_image(smem, img, L.bytes);
+  MechView m;
+  m.bind(L, smem);
+  const int ns = m.ns, nout = ns + 1;
+  double* sP = reinterpret_cast<double*>(smem + L.bytes);
+  for (int i = threadIdx.x; i < ns * ns; i += blockDim.x) sP[i] = proj[i];
+  double* sB = sP + ns * ns;
+  for (int i = threadIdx.x; i < ne * ns; i += blockDim.x) sB[i] = Bm[i];
+  __syncthreads();
+  double dY[32], Y1[32];
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t cell = base + i;
+    const double T0 = T[cell], dti = dt[cell], pc = p[cell];
+    bool ok = isfinite(T0) && isfinite(pc) && pc > 0.0 && isfinite(dti) && dti > 0.0;
+    ok = ok && T0 >= gp.Tlo && T0 <= gp.Thi;
+    const double lp = log10(pc), ld = log10(dti);
+    ok = ok && lp >= gp.lpl && lp <= gp.lph && ld >= gp.ldl && ld <= gp.ldh;
+    double dTn = 0.0, ens = 0.0, ensT = 0.0;
+    for (int k = 0; k < ns; ++k) {
+      dY[k] = (double)ym[k] + (double)ys[k] * (double)yn[i * nout + k];
+      if (yn2) {
+        double d2 = (double)ym[k] + (double)ys[k] * (double)yn2[i * nout + k];
+        ens = fmax(ens, fabs(d2 - dY[k]));
+        dY[k] = 0.5 * (dY[k] + d2);
+      }
+    }
+    dTn = (double)ym[ns] + (double)ys[ns] * (double)yn[i * nout + ns];
+    if (yn2) {
+      double d2 = (double)ym[ns] + (double)ys[ns] * (double)yn2[i * nout + ns];
+      ensT = fabs(d2 - dTn);
+      dTn = 0.5 * (dTn + d2);
+    }
+    // element residual of the raw prediction
+    double er = 0.0;
+    for (int e = 0; e < ne; ++e) {
+      double s = 0.0;
+      for (int k = 0; k < ns; ++k) s += sB[e * ns + k] * dY[k];
+      er = fmax(er, fabs(s));
+    }
+    // projection and realizability
+    double ymin = 1.0;
+    for (int k = 0; k < ns; ++k) {
+      double s = 0.0;
+      for (int j = 0; j < ns; ++j) s += sP[k * ns + j] * dY[j];
+      Y1[k] = Y[cell * ns + k] + s;
+      ymin = fmin(ymin, Y1[k]);
+    }
+    // energy: h(T1, Y1) = h(T0, Y0), Newton from the network's temperature
+    double h0 = 0.0;
+    {
+      const double lnT = log(T0), invT = 1.0 / T0;
+      for (int k = 0; k < ns; ++k) h0 += Y[cell * ns + k] * nasa7(m, k, T0, lnT, invT).hRT * m.invmw[k];
+      h0 *= T0;
+    }
+    double T1 = T0 + dTn;
+    bool conv = isfinite(T1) && T1 > 200.0 && T1 < 6000.0;
+    for (int it = 0; it < 8 && conv; ++it) {
+      const double lnT = log(T1), invT = 1.0 / T1;
+      double h = 0.0, cpm = 0.0;
+      for (int k = 0; k < ns; ++k) {
+        SpThermo th = nasa7(m, k, T1, lnT, invT);
+        h += Y1[k] * th.hRT * m.invmw[k];
+        cpm += Y1[k] * th.cpR * m.invmw[k];
+      }
+      const double dT = (h * T1 - h0) / cpm;
+      T1 -= dT;
+      if (!(T1 > 200.0 && T1 < 6000.0)) conv = false;
+      if (fabs(dT) < 1e-10 * T1) break;
+    }
+    ok = ok && conv && fabs(T1 - (T0 + dTn)) <= gp.max_dT_resid && er <= gp.max_elem_resid && ymin >= gp.min_Y;
+    if (yn2) ok = ok && ensT <= gp.max_ens_dT && ens <= gp.max_ens_dY;
+    if (ok) {
+      for (int k = 0; k < ns; ++k) Y[cell * ns + k] = Y1[k] > 0.0 ? Y1[k] : 0.0;
+      T[cell] = T1;
+      if (status) status[cell] = FLINT_CELL_OK;
+      if (nsteps) nsteps[cell] = 0;
+    } else {
+      unsigned long long slot = atomicAdd(rej_count, 1ull);
+      rej_idx[slot] = cell;
+    }
+  }
+}
+
+__global__ void k_gather(int64_t m, const int64_t* __restrict__ idx, int ns, const double* __restrict__ T,
+                         const double* __restrict__ p, const double* __restrict__ Y, const double* __restrict__ dt,
+                         double* __restrict__ cT, double* __restrict__ cp, double* __restrict__ cY, double* __restrict__ cdt) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t c = idx[i];
+    cT[i] = T[c]; cp[i] = p[c]; cdt[i] = dt[c];
+    for (int k = 0; k < ns; ++k) cY[i * ns + k] = Y[c * ns + k];
+  }
+}
+
+__global__ void k_scatter(int64_t m, const int64_t* __restrict__ idx, int ns, double* __restrict__ T,
+                          double* __restrict__ Y, const double* __restrict__ cT, const double* __restrict__ cY,
+                          const int* __restrict__ cst, const int* __restrict__ cns, int* __restrict__ status,
+                          int* __restrict__ nsteps) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t c = idx[i];
+    T[c] = cT[i];
+    for (int k = 0; k < ns; ++k) Y[c * ns + k] = cY[i * ns + k];
+    if (status) status[c] = cst[i] == FLINT_CELL_OK ? FLINT_CELL_SURROGATE_REJECTED : cst[i];
+    if (nsteps) nsteps[c] = cns[i];
+  }
+}
+
+static int blocks_for(int64_t n, int threads) {
+  int64_t b = (n + threads - 1) / threads;
+  int64_t cap = (int64_t)device_sms() * 8;
+  return (int)std::max<int64_t>(1, std::min(b, cap));
+}
+
+// ------------------------------------------------------------------ host side
+static cudaError_t net_forward(Surrogate* s, Net& nt, int64_t n, const float* X, float* out, bool keep,
+                               cudaStream_t st) {
+  cudaError_t e = cudaSuccess;
+  for (int l = 0; l < nt.nl && !e; ++l) {
+    GemmArgs g{};
+    g.M = (int)n; g.N = nt.dims[l + 1]; g.K = nt.dims[l];
+    if (l == 0) { g.A = X; g.a_bf16 = 0; } else { g.A = s->A[l - 1]; g.a_bf16 = 1; }
+    g.sa_m = g.K; g.sa_k = 1;
+    g.B = nt.wb + nt.off_w[l]; g.b_bf16 = 1; g.sb_k = 1; g.sb_n = g.K;
+    g.bias = nt.w + nt.off_b[l];
+    if (l < nt.nl - 1) {
+      g.epi = EPI_BIAS_GELU;
+      g.C = keep ? s->Z[l] : nullptr; g.ldc = g.N;
+      g.Cb = s->A[l]; g.ldcb = g.N;
+    } else {
+      g.epi = EPI_BIAS;
+      g.C = out; g.ldc = g.N;
+    }
+    e = launch_gemm(g, st);
+  }
+  return e;
+}
+
+static int alloc_ws(Surrogate* s, int64_t cap) {
+  if (cap <= s->cap) return 0;
+  auto fr = [](void* p) { if (p) cudaFree(p); };
+  for (int l = 0; l < MAXL; ++l) { fr(s->Z[l]); fr(s->A[l]); s->Z[l] = nullptr; s->A[l] = nullptr; }
+  fr(s->dz0); fr(s->dz1); fr(s->yhat); fr(s->xf); fr(s->yout2); fr(s->rej_idx);
+  fr(s->cT); fr(s->cp); fr(s->cY); fr(s->cdt); fr(s->cst); fr(s->cns);
+  const int W = std::max(s->H, std::max(s->n_in, s->n_out));
+  cudaError_t e = cudaSuccess;
+  for (int l = 0; l < s->net[0].nl - 1 && !e; ++l) {
+    e = cudaMalloc(&s->Z[l], cap * s->H * sizeof(float));
+    if (!e) e = cudaMalloc(&s->A[l], cap * s->H * sizeof(__nv_bfloat16));
+  }
+  if (!e) e = cudaMalloc(&s->dz0, cap * W * sizeof(float));
+  if (!e) e = cudaMalloc(&s->dz1, cap * W * sizeof(float));
+  if (!e) e = cudaMalloc(&s->yhat, cap * s->n_out * sizeof(float));
+  if (!e) e = cudaMalloc(&s->yout2, cap * s->n_out * sizeof(float));
+  if (!e) e = cudaMalloc(&s->xf, cap * s->n_in * sizeof(float));
+  if (!e) e = cudaMalloc(&s->rej_idx, cap * sizeof(int64_t));
+  if (!e) e = cudaMalloc(&s->cT, cap * sizeof(double));
+  if (!e) e = cudaMalloc(&s->cp, cap * sizeof(double));
+  if (!e) e = cudaMalloc(&s->cdt, cap * sizeof(double));
+  if (!e) e = cudaMalloc(&s->cY, cap * s->ns * sizeof(double));
+  if (!e) e = cudaMalloc(&s->cst, cap * sizeof(int));
+  if (!e) e = cudaMalloc(&s->cns, cap * sizeof(int));
+  if (e) return FLINT_ERR_NOMEM;
+  s->cap = cap;
+  return 0;
+}
+
+static void net_free(Net& nt) {
+  cudaFree(nt.w); cudaFree(nt.g); cudaFree(nt.m1); cudaFree(nt.m2); cudaFree(nt.wb);
+  nt = Net();
+}
+
+void surrogate_free(Surrogate* s) {
+  if (!s) return;
+  for (int i = 0; i < 2; ++i) net_free(s->net[i]);
+  auto fr = [](void* p) { if (p) cudaFree(p); };
+  for (int l = 0; l < MAXL; ++l) { fr(s->Z[l]); fr(s->A[l]); }
+  fr(s->dz0); fr(s->dz1); fr(s->yhat); fr(s->xf); fr(s->yout2); fr(s->rej_idx); fr(s->rej_count);
+  fr(s->cT); fr(s->cp); fr(s->cY); fr(s->cdt); fr(s->cst); fr(s->cns); fr(s->loss);
+  fr(s->xmean); fr(s->xstd); fr(s->ymean); fr(s->ystd); fr(s->proj); fr(s->Bm);
+  delete s;
+}
+
+// Net layout: dims, then per layer W[dims[l+1]][dims[l]] followed by b[dims[l+1]].
+static int net_init(Net& nt, int nl, const int* dims, const float* w0) {
+  nt.nl = nl;
+  int64_t off = 0;
+  for (int l = 0; l <= nl; ++l) nt.dims[l] = dims[l];
+  for (int l = 0; l < nl; ++l) {
+    nt.off_w[l] = off; off += (int64_t)dims[l + 1] * dims[l];
+    nt.off_b[l] = off; off += dims[l + 1];
+  }
+  nt.P = off;
+  cudaError_t e = cudaMalloc(&nt.w, off * sizeof(float));
+  if (!e) e = cudaMalloc(&nt.g, off * sizeof(float));
+  if (!e) e = cudaMalloc(&nt.m1, off * sizeof(float));
+  if (!e) e = cudaMalloc(&nt.m2, off * sizeof(float));
+  if (!e) e = cudaMalloc(&nt.wb, off * sizeof(__nv_bfloat16));
+  if (!e) e = cudaMemcpy(nt.w, w0, off * sizeof(float), cudaMemcpyHostToDevice);
+  if (!e) e = cudaMemset(nt.m1, 0, off * sizeof(float));
+  if (!e) e = cudaMemset(nt.m2, 0, off * sizeof(float));
+  if (!e) e = launch_to_bf16(nt.w, nt.wb, off, nullptr);
+  if (!e) e = cudaDeviceSynchronize();
+  return e ? FLINT_ERR_CUDA : 0;
+}
+
+int surrogate_create(const uint8_t* mimg, const ImageLayout& L, unsigned int* counter, const flint_surrogate_desc* d,
+                     Surrogate** out, std::string& err) {
+  if (d->n_layers < 2 || d->n_layers > MAXL) { err = "n_layers out of range"; return FLINT_ERR_ARG; }
+  if (L.ns > 31 || L.ns < 2) { err = "surrogate supports 2..31 species"; return FLINT_ERR_MECH; }
+  if (d->bath < 0 || d->bath >= L.ns) { err = "bath species index"; return FLINT_ERR_ARG; }
+  if (d->n_nets < 1 || d->n_nets > 2) { err = "n_nets must be 1 or 2"; return FLINT_ERR_ARG; }
+  if (!d->weights || !d->x_mean || !d->x_std || !d->y_mean || !d->y_std || !d->elem) { err = "NULL array"; return FLINT_ERR_ARG; }
+  auto* s = new Surrogate();
+  s->mimg = mimg; s->L = L; s->counter = counter; s->jsave = nullptr; s->jslots = 0;
+  s->ns = L.ns; s->bath = d->bath; s->n_in = L.ns + 2; s->n_out = L.ns + 1; s->H = d->hidden;
+  s->nnets = d->n_nets; s->ne = d->n_elements;
+  std::vector<int> dims(d->n_layers + 1);
+  dims[0] = s->n_in;
+  for (int l = 1; l < d->n_layers; ++l) dims[l] = d->hidden;
+  dims[d->n_layers] = s->n_out;
+  int64_t P = 0;
+  for (int l = 0; l < d->n_layers; ++l) P += (int64_t)dims[l + 1] * dims[l] + dims[l + 1];
+  for (int i = 0; i < s->nnets; ++i) {
+    if (net_init(s->net[i], d->n_layers, dims.data(), d->weights + i * P)) {
+      surrogate_free(s); err = "weight buffers"; return FLINT_ERR_NOMEM;
+    }
+  }
+  s->hxm.assign(d->x_mean, d->x_mean + s->n_in); s->hxs.assign(d->x_std, d->x_std + s->n_in);
+  s->hym.assign(d->y_mean, d->y_mean + s->n_out); s->hys.assign(d->y_std, d->y_std + s->n_out);
+  // projector P = I - B^T (B B^T)^-1 B with B[e][k] = a_ek / W_k
+  const int ns = s->ns, ne = s->ne;
+  std::vector<double> Bm((size_t)ne * ns), BBt((size_t)ne * ne, 0.0), Pm((size_t)ns * ns, 0.0);
+  std::vector<double> W(ns);
+  cudaMemcpy(W.data(), mimg + L.o_mw, ns * sizeof(double), cudaMemcpyDeviceToHost);
+  for (int e = 0; e < ne; ++e)
+    for (int k = 0; k < ns; ++k) Bm[e * ns + k] = d->elem[e * ns + k] / W[k];
+  for (int a = 0; a < ne; ++a)
+    for (int b = 0; b < ne; ++b)
+      for (int k = 0; k < ns; ++k) BBt[a * ne + b] += Bm[a * ns + k] * Bm[b * ns + k];
+  // invert BBt (small, Gauss-Jordan with partial pivoting); zero rows (absent elements) are skipped
+  std::vector<double> inv((size_t)ne * ne, 0.0);
+  for (int a = 0; a < ne; ++a) inv[a * ne + a] = 1.0;
+  std::vector<int> active(ne, 1);
+  for (int c = 0; c < ne; ++c) {
+    int piv = -1; double best = 0.0;
+    for (int r = c; r < ne; ++r) if (fabs(BBt[r * ne + c]) > best) { best = fabs(BBt[r * ne + c]); piv = r; }
+    if (piv < 0 || best < 1e-300) { active[c] = 0; continue; }
+    for (int j = 0; j < ne; ++j) { std::swap(BBt[c * ne + j], BBt[piv * ne + j]); std::swap(inv[c * ne + j], inv[piv * ne + j]); }
+    double dv = BBt[c * ne + c];
+    for (int j = 0; j < ne; ++j) { BBt[c * ne + j] /= dv; inv[c * ne + j] /= dv; }
+    for (int r = 0; r < ne; ++r) {
+      if (r == c) continue;
+      double f = BBt[r * ne + c];
+      for (int j = 0; j < ne; ++j) { BBt[r * ne + j] -= f * BBt[c * ne + j]; inv[r * ne + j] -= f * inv[c * ne + j]; }
+    }
+  }
+  for (int k = 0; k < ns; ++k)
+    for (int j = 0; j < ns; ++j) {
+      double v = (k == j) ? 1.0 : 0.0;
+      for (int a = 0; a < ne; ++a)
+        for (int b = 0; b < ne; ++b) v -= Bm[a * ns + k] * inv[a * ne + b] * Bm[b * ns + j];
+      Pm[k * ns + j] = v;
+    }
+  cudaError_t e = cudaMalloc(&s->xmean, s->n_in * 4);
+  if (!e) e = cudaMalloc(&s->xstd, s->n_in * 4);
+  if (!e) e = cudaMalloc(&s->ymean, s->n_out * 4);
+  if (!e) e = cudaMalloc(&s->ystd, s->n_out * 4);
+  if (!e) e = cudaMalloc(&s->proj, ns * ns * 8);
+  if (!e) e = cudaMalloc(&s->Bm, std::max(ne, 1) * ns * 8);
+  if (!e) e = cudaMalloc(&s->loss, 8);
+  if (!e) e = cudaMalloc(&s->rej_count, 8);
+  if (!e) e = cudaMemcpy(s->xmean, d->x_mean, s->n_in * 4, cudaMemcpyHostToDevice);
+  if (!e) e = cudaMemcpy(s->xstd, d->x_std, s->n_in * 4, cudaMemcpyHostToDevice);
+  if (!e) e = cudaMemcpy(s->ymean, d->y_mean, s->n_out * 4, cudaMemcpyHostToDevice);
+  if (!e) e = cudaMemcpy(s->ystd, d->y_std, s->n_out * 4, cudaMemcpyHostToDevice);
+  if (!e) e = cudaMemcpy(s->proj, Pm.data(), ns * ns * 8, cudaMemcpyHostToDevice);
+  if (!e && ne) e = cudaMemcpy(s->Bm, Bm.data(), ne * ns * 8, cudaMemcpyHostToDevice);
+  if (e) { surrogate_free(s); err = cudaGetErrorString(e); return FLINT_ERR_CUDA; }
+  *out = s;
+  return 0;
+}
+
+int surrogate_features(Surrogate* s, int64_t n, const double* T, const double* p, const double* Y, const double* dt,
+                       float* X, cudaStream_t st) {
+  if (n <= 0) return 0;
+  k_features<<<blocks_for(n, 256), 256, 0, st>>>(n, s->ns, s->bath, T, p, Y, dt, s->xmean, s->xstd, X);
+  count_launch();
+  return cudaGetLastError() ? FLINT_ERR_CUDA : 0;
+}
+
+int surrogate_targets(Surrogate* s, int64_t n, const double* T0, const double* Y0, const double* T1, const double* Y1,
+                      float* Yt, cudaStream_t st) {
+  if (n <= 0) return 0;
+  k_targets<<<blocks_for(n, 256), 256, 0, st>>>(n, s->ns, T0, Y0, T1, Y1, s->ymean, s->ystd, Yt);
+  count_launch();
+  return cudaGetLastError() ? FLINT_ERR_CUDA : 0;
+}
+
+int surrogate_predict(Surrogate* s, int net, int64_t n, const float* X, float* Yn, cudaStream_t st) {
+  if (net < 0 || net >= s->nnets) return FLINT_ERR_ARG;
+  for (int64_t b = 0; b < n; b += std::max<int64_t>(s->cap, 1)) {
+    if (alloc_ws(s, std::min<int64_t>(std::max<int64_t>(n, 1), 262144))) return FLINT_ERR_NOMEM;
+    int64_t m = std::min<int64_t>(s->cap, n - b);
+    if (net_forward(s, s->net[net], m, X + b * s->n_in, Yn + b * s->n_out, false, st)) return FLINT_ERR_CUDA;
+  }
+  return 0;
+}
+
+int surrogate_train_step(Surrogate* s, int net, int64_t n, const float* X, const float* Yt, float lr, double* loss_out,
+                         cudaStream_t st) {
+  if (net < 0 || net >= s->nnets || n <= 0) return FLINT_ERR_ARG;
+  if (alloc_ws(s, n)) return FLINT_ERR_NOMEM;
+  Net& nt = s->net[net];
+  if (net_forward(s, nt, n, X, s->yhat, true, st)) return FLINT_ERR_CUDA;
+  if (cudaMemsetAsync(s->loss, 0, 8, st)) return FLINT_ERR_CUDA;
+  const int nl = nt.nl;
+  float* dz = s->dz0;
+  float* dzn = s->dz1;
+  if (launch_mse(s->yhat, Yt, n * s->n_out, 1.0f / (float)(n * s->n_out), dz, s->loss, st)) return FLINT_ERR_CUDA;
+  for (int l = nl - 1; l >= 0; --l) {
+    const int N = nt.dims[l + 1], K = nt.dims[l];
+    GemmArgs g{};
+    g.M = N; g.N = K; g.K = (int)n;
+    g.A = dz; g.a_bf16 = 0; g.sa_m = 1; g.sa_k = N;
+    if (l == 0) { g.B = X; g.b_bf16 = 0; } else { g.B = s->A[l - 1]; g.b_bf16 = 1; }
+    g.sb_k = K; g.sb_n = 1;
+    g.C = nt.g + nt.off_w[l]; g.ldc = K; g.epi = EPI_STORE;
+    if (launch_gemm(g, st)) return FLINT_ERR_CUDA;
+    if (launch_colsum(dz, (int)n, N, N, nt.g + nt.off_b[l], 0, st)) return FLINT_ERR_CUDA;
+    if (l > 0) {
+      GemmArgs h{};
+      h.M = (int)n; h.N = K; h.K = N;
+      h.A = dz; h.a_bf16 = 0; h.sa_m = N; h.sa_k = 1;
+      h.B = nt.wb + nt.off_w[l]; h.b_bf16 = 1; h.sb_k = K; h.sb_n = 1;
+      h.C = dzn; h.ldc = K; h.epi = EPI_GELU_BWD; h.Zprev = s->Z[l - 1]; h.ldz = K;
+      if (launch_gemm(h, st)) return FLINT_ERR_CUDA;
+      std::swap(dz, dzn);
+    }
+  }
+  nt.step += 1;
+  const float b1 = 0.9f, b2 = 0.999f;
+  const float bc1 = 1.f - powf(b1, (float)nt.step), bc2 = 1.f - powf(b2, (float)nt.step);
+  if (launch_adam(nt.w, nt.g, nt.m1, nt.m2, nt.wb, nt.P, lr, b1, b2, 1e-8f, bc1, bc2, 0.f, st)) return FLINT_ERR_CUDA;
+  if (loss_out) {
+    if (cudaMemcpyAsync(loss_out, s->loss, 8, cudaMemcpyDeviceToHost, st)) return FLINT_ERR_CUDA;
+    if (cudaStreamSynchronize(st)) return FLINT_ERR_CUDA;
+  }
+  return 0;
+}
+
+int surrogate_state(Surrogate* s, int net, float* host, int64_t* step, int get) {
+  if (net < 0 || net >= s->nnets) return FLINT_ERR_ARG;
+  Net& nt = s->net[net];
+  const int64_t P = nt.P;
+  cudaError_t e;
+  if (get) {
+    e = cudaMemcpy(host, nt.w, P * 4, cudaMemcpyDeviceToHost);
+    if (!e) e = cudaMemcpy(host + P, nt.m1, P * 4, cudaMemcpyDeviceToHost);
+    if (!e) e = cudaMemcpy(host + 2 * P, nt.m2, P * 4, cudaMemcpyDeviceToHost);
+    if (step) *step = nt.step;
+  } else {
+    e = cudaMemcpy(nt.w, host, P * 4, cudaMemcpyHostToDevice);
+    if (!e) e = cudaMemcpy(nt.m1, host + P, P * 4, cudaMemcpyHostToDevice);
+    if (!e) e = cudaMemcpy(nt.m2, host + 2 * P, P * 4, cudaMemcpyHostToDevice);
+    if (!e) e = launch_to_bf16(nt.w, nt.wb, P, nullptr);
+    if (!e) e = cudaDeviceSynchronize();
+    if (step) nt.step = *step;
+  }
+  return e ? FLINT_ERR_CUDA : 0;
+}
+
+int64_t surrogate_nparams(Surrogate* s) { return s->net[0].P; }
+
+int surrogate_advance(Surrogate* s, int64_t n, double* T, const double* p, double* Y, const double* dt,
+                      const flint_reactor_opts& o, const flint_surrogate_gate* gate, int* status, int* nsteps,
+                      double* jsave, int jslots, cudaStream_t st) {
+  s->last_accepted = s->last_rejected = 0;
+  if (n <= 0) return 0;
+  const int64_t CH = 262144;
+  if (alloc_ws(s, std::min<int64_t>(n, CH))) return FLINT_ERR_NOMEM;
+  GateParams gp;
+  gp.max_dT_resid = gate->max_dT_resid; gp.max_elem_resid = gate->max_elem_resid; gp.min_Y = gate->min_Y;
+  gp.max_ens_dT = gate->max_ens_dT; gp.max_ens_dY = gate->max_ens_dY;
+  gp.Tlo = gate->T_lo; gp.Thi = gate->T_hi; gp.lpl = gate->log10p_lo; gp.lph = gate->log10p_hi;
+  gp.ldl = gate->log10dt_lo; gp.ldh = gate->log10dt_hi;
+  const size_t psm = s->L.bytes + (size_t)(s->ns * s->ns + std::max(s->ne, 1) * s->ns) * sizeof(double);
+  cudaFuncSetAttribute(k_post, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)psm);
+  for (int64_t b = 0; b < n; b += s->cap) {
+    const int64_t m = std::min<int64_t>(s->cap, n - b);
+    if (surrogate_features(s, m, T + b, p + b, Y + b * s->ns, dt + b, s->xf, st)) return FLINT_ERR_CUDA;
+    if (net_forward(s, s->net[0], m, s->xf, s->yhat, false, st)) return FLINT_ERR_CUDA;
+    if (s->nnets > 1 && net_forward(s, s->net[1], m, s->xf, s->yout2, false, st)) return FLINT_ERR_CUDA;
+    if (cudaMemsetAsync(s->rej_count, 0, 8, st)) return FLINT_ERR_CUDA;
+    k_post<<<blocks_for(m, SURR_THREADS), SURR_THREADS, psm, st>>>(
+        s->mimg, s->L, m, b, T, p, Y, dt, s->yhat, s->nnets > 1 ? s->yout2 : nullptr, s->ymean, s->ystd, s->proj,
+        s->Bm, s->ne, gp, status, nsteps, s->rej_idx, s->rej_count);
+    count_launch();
+    if (cudaGetLastError()) return FLINT_ERR_CUDA;
+    unsigned long long nrej = 0;
+    if (cudaMemcpyAsync(&nrej, s->rej_count, 8, cudaMemcpyDeviceToHost, st) || cudaStreamSynchronize(st))
+      return FLINT_ERR_CUDA;
+    s->last_rejected += (int64_t)nrej;
+    s->last_accepted += m - (int64_t)nrej;
+    if (nrej == 0) continue;
+    k_gather<<<blocks_for((int64_t)nrej, 256), 256, 0, st>>>((int64_t)nrej, s->rej_idx, s->ns, T, p, Y, dt, s->cT,
+                                                             s->cp, s->cY, s->cdt);
+    count_launch();
+    cudaError_t e = launch_reactor(s->mimg, s->L, (int64_t)nrej, s->cT, s->cp, s->cY, s->cdt, o, s->cst, s->cns,
+                                   s->counter, jsave, jslots, st);
+    if (e) return FLINT_ERR_CUDA;
+    k_scatter<<<blocks_for((int64_t)nrej, 256), 256, 0, st>>>((int64_t)nrej, s->rej_idx, s->ns, T, Y, s->cT, s->cY,
+                                                              s->cst, s->cns, status, nsteps);
+    count_launch();
+    if (cudaGetLastError()) return FLINT_ERR_CUDA;
+  }
+  return 0;
+}
+
+void surrogate_counts(Surrogate* s, int64_t* acc, int64_t* rej) { *acc = s->last_accepted; *rej = s->last_rejected; }
+
+}  // namespace flint
