@@ -23,12 +23,15 @@
 // pivot order instead of swapping rows.  Step-size factors eta = (c*dsm)^(-1/(q+1))
 // are heuristics and are evaluated in FP32 (the oracle does the same); every
 // quantity of the solution itself stays FP64.
+#include <mutex>
+
 #include "flint_dev.cuh"
 #include "flint_host.h"
 
 namespace flint {
 
 constexpr int REACTOR_THREADS = 256;
+constexpr int MAX_DEVICES = 64;
 
 struct BdfL { double l[6][6]; };
 
@@ -389,13 +392,22 @@ cudaError_t launch_reactor(const uint8_t* img, const ImageLayout& L, int64_t n, 
   if (blocks > full) blocks = full;
   if (blocks * (REACTOR_THREADS / 32) > slots) blocks = slots / (REACTOR_THREADS / 32);
   if (blocks < 1) return cudaErrorInvalidValue;
-  static bool bdf_ready = false;
-  if (!bdf_ready) {
-    BdfL B;
-    bdf_coeffs(B);
-    e = cudaMemcpyToSymbol(c_bdf, &B, sizeof(B));
-    if (e != cudaSuccess) return e;
-    bdf_ready = true;
+  // the BDF coefficient table lives in __constant__ memory, one copy per device
+  static std::mutex bdf_mu;
+  static bool bdf_ready[MAX_DEVICES] = {false};
+  int dev = 0;
+  e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= MAX_DEVICES) return cudaErrorInvalidDevice;
+  {
+    std::lock_guard<std::mutex> lk(bdf_mu);
+    if (!bdf_ready[dev]) {
+      BdfL B;
+      bdf_coeffs(B);
+      e = cudaMemcpyToSymbol(c_bdf, &B, sizeof(B));
+      if (e != cudaSuccess) return e;
+      bdf_ready[dev] = true;
+    }
   }
   e = cudaMemsetAsync(work_counter, 0, NCOUNTERS * sizeof(unsigned long long), st);
   if (e != cudaSuccess) return e;
