@@ -374,6 +374,24 @@ int flint_reactor_advance(flint_mech_t h, int64_t n, double* T, const double* p,
   return e == cudaSuccess ? FLINT_OK : cuda_fail(e, "flint_reactor_advance");
 }
 
+int flint_reactor_advance_noalloc(flint_mech_t h, int64_t n, double* T, const double* p, double* Y, const double* dt,
+                                  const flint_reactor_opts* opts, int* status, int* nsteps, void* stream) {
+  int rc = check_common(h, n, FLINT_CELL_MAJOR);
+  if (rc) return rc;
+  if (n == 0) return FLINT_OK;
+  if (!T || !p || !Y || !dt) return fail(FLINT_ERR_ARG, "NULL array");
+  if ((int64_t)(h->L.ns + 1) * (h->L.ns + 1) > 32 * 32)
+    return fail(FLINT_ERR_MECH, "flint_reactor_advance_noalloc: %d unknowns exceed the 32 x 32 Jacobian slots of its "
+                                "static scratch (%zu bytes)", h->L.ns + 1, reactor_noalloc_bytes());
+  flint_reactor_opts o;
+  if (opts) o = *opts; else flint_reactor_default_opts(&o);
+  if (!(o.rtol > 0.0) || !(o.atol > 0.0) || o.max_steps < 1 || o.max_order < 1 || o.max_order > 5)
+    return fail(FLINT_ERR_ARG, "reactor options out of range");
+  if (o.constant_volume) return fail(FLINT_ERR_ARG, "constant-volume reactor is not in this build");
+  cudaError_t e = launch_reactor_noalloc(h->dimg, h->L, n, T, p, Y, dt, o, status, nsteps, (cudaStream_t)stream);
+  return e == cudaSuccess ? FLINT_OK : cuda_fail(e, "flint_reactor_advance_noalloc");
+}
+
 int flint_reactor_stats(flint_mech_t h, int64_t out[6]) {
   if (!h || !out) return fail(FLINT_ERR_ARG, "NULL argument");
   unsigned long long c[7];

@@ -30,6 +30,12 @@ cudaError_t launch_reactor(const uint8_t* img, const ImageLayout& L, int64_t n, 
                            double* Y, const double* dt, const flint_reactor_opts& o, int* status, int* nsteps,
                            unsigned int* work_counter, double* jsave, int slots, cudaStream_t st);
 
+size_t reactor_noalloc_bytes();
+int reactor_noalloc_slots();
+cudaError_t launch_reactor_noalloc(const uint8_t* img, const ImageLayout& L, int64_t n, double* T, const double* p,
+                                   double* Y, const double* dt, const flint_reactor_opts& o, int* status,
+                                   int* nsteps, cudaStream_t st);
+
 // tabulated (reference general-loop) path, flint_table.cu
 int table_create(const flint_table_desc* d, void** out, std::string& err);
 void table_destroy(void* th);

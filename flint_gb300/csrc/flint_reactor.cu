@@ -417,4 +417,57 @@ cudaError_t launch_reactor(const uint8_t* img, const ImageLayout& L, int64_t n, 
   return cudaGetLastError();
 }
 
+
+// ------------------------------------------------------- allocation-free entry
+// Some callers cannot let a library call cudaMalloc: CFD solvers that reserve
+// their whole device-memory budget for their own pool at start-up (a later
+// allocation by a library fails or fragments that pool) and codes whose
+// certification or real-time rules forbid device allocation after
+// initialisation.  flint_reactor_advance_noalloc serves them: the reactor's
+// scratch (its work-stealing and statistics counters and one saved-Jacobian
+// slot per resident warp) lives in this file-scope device array instead of
+// memory allocated by the handle.  Every GPU that loads the library holds it
+// until the process exits.
+constexpr int NOALLOC_SLOTS = 1280;                  // saved-Jacobian slots of 32 x 32 FP64
+constexpr size_t NOALLOC_COUNTER_BYTES = 256;        // counters, zeroed by every call
+constexpr size_t NOALLOC_BYTES = NOALLOC_COUNTER_BYTES + (size_t)NOALLOC_SLOTS * JSLOT * sizeof(double);
+static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_BYTES];
+
+// Host-side address of g_noalloc_scratch on each device: the symbol's name is
+// only a host stand-in, the kernel needs the device address, looked up once
+// per device (with that device current) by cudaGetSymbolAddress.
+static std::mutex g_noalloc_mu;
+static void* g_noalloc_addr[MAX_DEVICES] = {nullptr};
+
+static cudaError_t noalloc_scratch_address(void** out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= MAX_DEVICES) return cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> lk(g_noalloc_mu);
+  if (!g_noalloc_addr[dev]) {
+    void* ptr = nullptr;
+    e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+    if (e != cudaSuccess) return e;
+    g_noalloc_addr[dev] = ptr;
+  }
+  *out = g_noalloc_addr[dev];
+  return cudaSuccess;
+}
+
+size_t reactor_noalloc_bytes() { return NOALLOC_BYTES; }
+int reactor_noalloc_slots() { return NOALLOC_SLOTS; }
+
+cudaError_t launch_reactor_noalloc(const uint8_t* img, const ImageLayout& L, int64_t n, double* T, const double* p,
+                                   double* Y, const double* dt, const flint_reactor_opts& o, int* status,
+                                   int* nsteps, cudaStream_t st) {
+  void* base = nullptr;
+  cudaError_t e = noalloc_scratch_address(&base);
+  if (e != cudaSuccess) return e;
+  unsigned int* counters = reinterpret_cast<unsigned int*>(base);
+  double* jsave = reinterpret_cast<double*>(static_cast<unsigned char*>(base) + NOALLOC_COUNTER_BYTES);
+  // launch_reactor zeroes the counters on `st` and caps the grid to the slots
+  return launch_reactor(img, L, n, T, p, Y, dt, o, status, nsteps, counters, jsave, NOALLOC_SLOTS, st);
+}
+
 }  // namespace flint

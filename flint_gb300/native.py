@@ -107,6 +107,7 @@ def lib():
     L.flint_rhs_constp_batch.argtypes = [vp, i64, vp, vp, vp, vp, vp]
     L.flint_reactor_advance.argtypes = [vp, i64, vp, vp, vp, vp, C.POINTER(ReactorOpts), vp, vp, vp]
     L.flint_reactor_default_opts.argtypes = [C.POINTER(ReactorOpts)]
+    L.flint_reactor_advance_noalloc.argtypes = [vp, i64, vp, vp, vp, vp, C.POINTER(ReactorOpts), vp, vp, vp]
     L.flint_reactor_stats.argtypes = [vp, C.POINTER(C.c_int64)]
     L.flint_probe_fp64_peak.argtypes = [C.POINTER(C.c_double)]
     L.flint_selftest_exp.argtypes = [vp, i64, vp, vp, vp]

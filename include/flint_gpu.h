@@ -212,6 +212,23 @@ int flint_reactor_advance(flint_mech_t mech, int64_t n, double* T, const double*
                           double* Y, const double* dt, const flint_reactor_opts* opts,
                           int* status, int* nsteps, void* stream);
 
+/* flint_reactor_advance without any device allocation.  No counterpart in the
+ * reference.  For callers that must not have a library call cudaMalloc: CFD
+ * codes that hand their whole device memory to their own pool at start-up and
+ * codes whose rules forbid allocation after initialisation.  The scratch (work
+ * counters and one saved Jacobian per resident warp) is a static device array
+ * of 1280 slots of 32 x 32 doubles plus 256 bytes of counters (10 MiB + 256 B),
+ * which every GPU that loads the library holds until exit.  Mechanisms of up to
+ * 31 species fit; larger ones are rejected with FLINT_ERR_MECH.  The first call
+ * on a device looks the array's address up (cudaGetSymbolAddress) and uploads
+ * the BDF table, so make that first call before any stream capture.  Every
+ * call shares the one array and zeroes its counters: calls that overlap on the
+ * GPU (two streams, two threads) race and must be serialised by the caller.
+ * flint_reactor_stats does not report these calls. */
+int flint_reactor_advance_noalloc(flint_mech_t mech, int64_t n, double* T, const double* p,
+                                  double* Y, const double* dt, const flint_reactor_opts* opts,
+                                  int* status, int* nsteps, void* stream);
+
 /* Work counters of the last flint_reactor_advance on this handle (blocks until
  * it has finished): out[0] RHS evaluations, out[1] Jacobian evaluations,
  * out[2] Newton iterations (one LU solve each), out[3] accepted steps,
