@@ -392,6 +392,110 @@ int flint_reactor_advance_noalloc(flint_mech_t h, int64_t n, double* T, const do
   return e == cudaSuccess ? FLINT_OK : cuda_fail(e, "flint_reactor_advance_noalloc");
 }
 
+// ------------------------------------------------------------------ surrogate
+struct flint_surrogate_s {
+  flint_mech_t mech;
+  flint::Surrogate* s;
+};
+
+static int ensure_jsave(flint_mech_t h) {
+  if (h->djsave) return FLINT_OK;
+  int slots = reactor_slots(h->L);
+  if (slots < 1) return fail(FLINT_ERR_MECH, "reactor kernel does not fit this mechanism (shared memory)");
+  cudaError_t ea = cudaMalloc(&h->djsave, (size_t)slots * reactor_slot_bytes());
+  if (ea != cudaSuccess) { h->djsave = nullptr; return fail(FLINT_ERR_NOMEM, "reactor scratch: %s", cudaGetErrorString(ea)); }
+  h->jslots = slots;
+  return FLINT_OK;
+}
+
+int flint_surrogate_create(flint_mech_t mech, const flint_surrogate_desc* desc, flint_surrogate_t* out) {
+  if (!mech || !desc || !out) return fail(FLINT_ERR_ARG, "NULL argument");
+  if (mech->table) return fail(FLINT_ERR_MECH, "the surrogate needs an analytic mechanism");
+  *out = nullptr;
+  std::string err;
+  flint::Surrogate* s = nullptr;
+  int rc = surrogate_create(mech->dimg, mech->L, mech->dcounter, desc, &s, err);
+  if (rc) return fail(rc, "flint_surrogate_create: %s", err.c_str());
+  *out = new flint_surrogate_s{mech, s};
+  return FLINT_OK;
+}
+
+int flint_surrogate_destroy(flint_surrogate_t s) {
+  if (!s) return FLINT_OK;
+  surrogate_free(s->s);
+  delete s;
+  return FLINT_OK;
+}
+
+int64_t flint_surrogate_nparams(flint_surrogate_t s) { return s ? surrogate_nparams(s->s) : 0; }
+
+int flint_surrogate_features(flint_surrogate_t s, int64_t n, const double* T, const double* p, const double* Y,
+                             const double* dt, float* X, void* stream) {
+  if (!s || n < 0 || (n > 0 && (!T || !p || !Y || !dt || !X))) return fail(FLINT_ERR_ARG, "bad argument");
+  int rc = surrogate_features(s->s, n, T, p, Y, dt, X, (cudaStream_t)stream);
+  return rc ? fail(rc, "flint_surrogate_features failed") : FLINT_OK;
+}
+
+int flint_surrogate_targets(flint_surrogate_t s, int64_t n, const double* T0, const double* Y0, const double* T1,
+                            const double* Y1, float* Yt, void* stream) {
+  if (!s || n < 0 || (n > 0 && (!T0 || !Y0 || !T1 || !Y1 || !Yt))) return fail(FLINT_ERR_ARG, "bad argument");
+  int rc = surrogate_targets(s->s, n, T0, Y0, T1, Y1, Yt, (cudaStream_t)stream);
+  return rc ? fail(rc, "flint_surrogate_targets failed") : FLINT_OK;
+}
+
+int flint_surrogate_train_step(flint_surrogate_t s, int net, int64_t n, const float* X, const float* Yt, float lr,
+                               double* loss, void* stream) {
+  if (!s || n <= 0 || !X || !Yt) return fail(FLINT_ERR_ARG, "bad argument");
+  int rc = surrogate_train_step(s->s, net, n, X, Yt, lr, loss, (cudaStream_t)stream);
+  return rc ? fail(rc, "flint_surrogate_train_step failed") : FLINT_OK;
+}
+
+int flint_surrogate_predict(flint_surrogate_t s, int net, int64_t n, const float* X, float* Yn, void* stream) {
+  if (!s || n < 0 || (n > 0 && (!X || !Yn))) return fail(FLINT_ERR_ARG, "bad argument");
+  int rc = surrogate_predict(s->s, net, n, X, Yn, (cudaStream_t)stream);
+  return rc ? fail(rc, "flint_surrogate_predict failed") : FLINT_OK;
+}
+
+int flint_surrogate_state(flint_surrogate_t s, int net, float* host, int64_t* step, int get) {
+  if (!s || !host) return fail(FLINT_ERR_ARG, "bad argument");
+  int rc = surrogate_state(s->s, net, host, step, get);
+  return rc ? fail(rc, "flint_surrogate_state failed") : FLINT_OK;
+}
+
+int flint_surrogate_advance(flint_surrogate_t s, int64_t n, double* T, const double* p, double* Y, const double* dt,
+                            const flint_reactor_opts* opts, const flint_surrogate_gate* gate, int* status,
+                            int* nsteps, int64_t* counts, void* stream) {
+  if (!s || !gate) return fail(FLINT_ERR_ARG, "NULL argument");
+  int rc = check_common(s->mech, n, FLINT_CELL_MAJOR);
+  if (rc) return rc;
+  if (n == 0) return FLINT_OK;
+  if (!T || !p || !Y || !dt) return fail(FLINT_ERR_ARG, "NULL array");
+  flint_reactor_opts o;
+  if (opts) o = *opts; else flint_reactor_default_opts(&o);
+  if (!(o.rtol > 0.0) || !(o.atol > 0.0) || o.max_steps < 1 || o.max_order < 1 || o.max_order > 5)
+    return fail(FLINT_ERR_ARG, "reactor options out of range");
+  rc = ensure_jsave(s->mech);
+  if (rc) return rc;
+  rc = surrogate_advance(s->s, n, T, p, Y, dt, o, gate, status, nsteps, s->mech->djsave, s->mech->jslots,
+                         nullptr, (cudaStream_t)stream);
+  if (rc) return fail(rc, "flint_surrogate_advance failed: %s", cudaGetErrorString(cudaGetLastError()));
+  if (counts) surrogate_counts(s->s, &counts[0], &counts[1]);
+  return FLINT_OK;
+}
+
+int flint_surrogate_evaluate(flint_surrogate_t s, int64_t n, double* T, const double* p, double* Y,
+                             const double* dt, const flint_surrogate_gate* gate, double* metrics, void* stream) {
+  if (!s || !gate || !metrics) return fail(FLINT_ERR_ARG, "NULL argument");
+  int rc = check_common(s->mech, n, FLINT_CELL_MAJOR);
+  if (rc) return rc;
+  if (n == 0) return FLINT_OK;
+  if (!T || !p || !Y || !dt) return fail(FLINT_ERR_ARG, "NULL array");
+  flint_reactor_opts o;
+  flint_reactor_default_opts(&o);
+  rc = surrogate_advance(s->s, n, T, p, Y, dt, o, gate, nullptr, nullptr, nullptr, 0, metrics, (cudaStream_t)stream);
+  return rc ? fail(rc, "flint_surrogate_evaluate failed") : FLINT_OK;
+}
+
 int flint_reactor_stats(flint_mech_t h, int64_t out[6]) {
   if (!h || !out) return fail(FLINT_ERR_ARG, "NULL argument");
   unsigned long long c[7];

@@ -36,6 +36,25 @@ cudaError_t launch_reactor_noalloc(const uint8_t* img, const ImageLayout& L, int
                                    double* Y, const double* dt, const flint_reactor_opts& o, int* status,
                                    int* nsteps, cudaStream_t st);
 
+// learned surrogate, flint_surrogate.cu
+struct Surrogate;
+int surrogate_create(const uint8_t* mimg, const ImageLayout& L, unsigned int* counter, const flint_surrogate_desc* d,
+                     Surrogate** out, std::string& err);
+void surrogate_free(Surrogate* s);
+int64_t surrogate_nparams(Surrogate* s);
+int surrogate_features(Surrogate* s, int64_t n, const double* T, const double* p, const double* Y, const double* dt,
+                       float* X, cudaStream_t st);
+int surrogate_targets(Surrogate* s, int64_t n, const double* T0, const double* Y0, const double* T1, const double* Y1,
+                      float* Yt, cudaStream_t st);
+int surrogate_predict(Surrogate* s, int net, int64_t n, const float* X, float* Yn, cudaStream_t st);
+int surrogate_train_step(Surrogate* s, int net, int64_t n, const float* X, const float* Yt, float lr, double* loss,
+                         cudaStream_t st);
+int surrogate_state(Surrogate* s, int net, float* host, int64_t* step, int get);
+int surrogate_advance(Surrogate* s, int64_t n, double* T, const double* p, double* Y, const double* dt,
+                      const flint_reactor_opts& o, const flint_surrogate_gate* gate, int* status, int* nsteps,
+                      double* jsave, int jslots, double* metrics, cudaStream_t st);
+void surrogate_counts(Surrogate* s, int64_t* acc, int64_t* rej);
+
 // tabulated (reference general-loop) path, flint_table.cu
 int table_create(const flint_table_desc* d, void** out, std::string& err);
 void table_destroy(void* th);

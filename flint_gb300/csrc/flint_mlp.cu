@@ -18,16 +18,15 @@
 // Tiles: 64 x 64 per block, 4 warps of 32 x 32, K staged 32 at a time with rows
 // padded to 40 BF16 (80 bytes) so the fragment loads are bank-conflict free.
 #include <cstdint>
+#include <algorithm>
 #include <cuda_bf16.h>
 #include "flint_host.h"
+#include "flint_mlp.h"
 
 namespace flint {
 
 constexpr int GBM = 64, GBN = 64, GBK = 32, GKP = 40, GTHREADS = 128;
 
-enum { EPI_STORE = 0, EPI_BIAS = 1, EPI_BIAS_GELU = 2, EPI_GELU_BWD = 3 };
-
-// GELU, tanh form: 0.5 x (1 + tanh(sqrt(2/pi) (x + 0.044715 x^3))), in FP32.
 __device__ __forceinline__ float gelu_f(float x) {
   const float k0 = 0.7978845608028654f, k1 = 0.044715f;
   return 0.5f * x * (1.0f + tanhf(k0 * (x + k1 * x * x * x)));
@@ -38,18 +37,6 @@ __device__ __forceinline__ float gelu_grad(float x) {
   const float t = tanhf(u);
   return 0.5f * (1.0f + t) + 0.5f * x * (1.0f - t * t) * k0 * (1.0f + 3.0f * k1 * x * x);
 }
-
-struct GemmArgs {
-  int M, N, K;
-  const void* A; int a_bf16; int64_t sa_m, sa_k;
-  const void* B; int b_bf16; int64_t sb_k, sb_n;
-  const float* bias;                 // [N]
-  float* C; int64_t ldc;             // FP32 output (pre-activation or result)
-  __nv_bfloat16* Cb; int64_t ldcb;   // optional BF16 activation output
-  const float* Zprev; int64_t ldz;   // GELU_BWD: pre-activation of the previous layer
-  int epi;
-  int accumulate;                    // C += result (gradient accumulation)
-};
 
 __device__ __forceinline__ float ld_any(const void* p, int bf16, int64_t idx) {
   return bf16 ? __bfloat162float(static_cast<const __nv_bfloat16*>(p)[idx]) : static_cast<const float*>(p)[idx];
@@ -129,8 +116,10 @@ __global__ void __launch_bounds__(GTHREADS) k_gemm_bf16(GemmArgs g) {
         float v = acc[i][j][c];
         if (g.epi == EPI_BIAS || g.epi == EPI_BIAS_GELU) v += g.bias[n];
         if (g.epi == EPI_GELU_BWD) v *= gelu_grad(g.Zprev[(int64_t)m * g.ldz + n]);
-        float* cp = g.C + (int64_t)m * g.ldc + n;
-        if (g.C) *cp = g.accumulate ? *cp + v : v;
+        if (g.C) {
+          float* cp = g.C + (int64_t)m * g.ldc + n;
+          *cp = g.accumulate ? *cp + v : v;
+        }
         if (g.Cb) g.Cb[(int64_t)m * g.ldcb + n] = __float2bfloat16_rn(g.epi == EPI_BIAS_GELU ? gelu_f(v) : v);
       }
 }

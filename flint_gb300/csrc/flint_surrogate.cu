@@ -27,29 +27,9 @@
 #include <cuda_bf16.h>
 
 #include "flint_host.h"
+#include "flint_mlp.h"
 
 namespace flint {
-
-struct GemmArgs;
-enum { EPI_STORE = 0, EPI_BIAS = 1, EPI_BIAS_GELU = 2, EPI_GELU_BWD = 3 };
-struct GemmArgs {
-  int M, N, K;
-  const void* A; int a_bf16; int64_t sa_m, sa_k;
-  const void* B; int b_bf16; int64_t sb_k, sb_n;
-  const float* bias;
-  float* C; int64_t ldc;
-  __nv_bfloat16* Cb; int64_t ldcb;
-  const float* Zprev; int64_t ldz;
-  int epi;
-  int accumulate;
-};
-cudaError_t launch_gemm(const GemmArgs& g, cudaStream_t st);
-cudaError_t launch_colsum(const float* dZ, int M, int N, int64_t ld, float* db, int acc, cudaStream_t st);
-cudaError_t launch_mse(const float* yhat, const float* y, int64_t total, float scale, float* grad, double* loss,
-                       cudaStream_t st);
-cudaError_t launch_adam(float* w, const float* gw, float* m1, float* m2, __nv_bfloat16* wb, int64_t n, float lr,
-                        float b1, float b2, float eps, float bc1, float bc2, float wd, cudaStream_t st);
-cudaError_t launch_to_bf16(const float* x, __nv_bfloat16* y, int64_t n, cudaStream_t st);
 
 constexpr int MAXL = 8;
 constexpr int SURR_THREADS = 128;
@@ -133,7 +113,7 @@ k_post(const uint8_t* __restrict__ img, ImageLayout L, int64_t n, int64_t base, 
        const float* __restrict__ yn, const float* __restrict__ yn2, const float* __restrict__ ym,
        const float* __restrict__ ys, const double* __restrict__ proj, const double* __restrict__ Bm, int ne,
        GateParams gp, int* __restrict__ status, int* __restrict__ nsteps, int64_t* __restrict__ rej_idx,
-       unsigned long long* __restrict__ rej_count) {
+       unsigned long long* __restrict__ rej_count, double* __restrict__ metrics) {
   extern __shared__ __align__(16) uint8_t smem[];
   stage_image(smem, img, L.bytes);
   MechView m;
@@ -204,7 +184,17 @@ k_post(const uint8_t* __restrict__ img, ImageLayout L, int64_t n, int64_t base, 
       if (!(T1 > 200.0 && T1 < 6000.0)) conv = false;
       if (fabs(dT) < 1e-10 * T1) break;
     }
-    ok = ok && conv && fabs(T1 - (T0 + dTn)) <= gp.max_dT_resid && er <= gp.max_elem_resid && ymin >= gp.min_Y;
+    const double dTres = conv ? fabs(T1 - (T0 + dTn)) : 1e300;
+    if (metrics) {
+      // evaluation mode: every cell takes the surrogate result, the gate
+      // quantities are reported instead of applied
+      double* mt = metrics + i * 6;
+      mt[0] = dTres; mt[1] = er; mt[2] = ymin; mt[3] = ensT; mt[4] = ens; mt[5] = ok ? 1.0 : 0.0;
+      for (int k = 0; k < ns; ++k) Y[cell * ns + k] = Y1[k] > 0.0 ? Y1[k] : 0.0;
+      T[cell] = conv ? T1 : T0 + dTn;
+      continue;
+    }
+    ok = ok && conv && dTres <= gp.max_dT_resid && er <= gp.max_elem_resid && ymin >= gp.min_Y;
     if (yn2) ok = ok && ensT <= gp.max_ens_dT && ens <= gp.max_ens_dY;
     if (ok) {
       for (int k = 0; k < ns; ++k) Y[cell * ns + k] = Y1[k] > 0.0 ? Y1[k] : 0.0;
@@ -434,9 +424,10 @@ int surrogate_targets(Surrogate* s, int64_t n, const double* T0, const double* Y
 
 int surrogate_predict(Surrogate* s, int net, int64_t n, const float* X, float* Yn, cudaStream_t st) {
   if (net < 0 || net >= s->nnets) return FLINT_ERR_ARG;
-  for (int64_t b = 0; b < n; b += std::max<int64_t>(s->cap, 1)) {
-    if (alloc_ws(s, std::min<int64_t>(std::max<int64_t>(n, 1), 262144))) return FLINT_ERR_NOMEM;
-    int64_t m = std::min<int64_t>(s->cap, n - b);
+  if (n <= 0) return 0;
+  if (alloc_ws(s, std::min<int64_t>(n, 262144))) return FLINT_ERR_NOMEM;
+  for (int64_t b = 0; b < n; b += s->cap) {
+    const int64_t m = std::min<int64_t>(s->cap, n - b);
     if (net_forward(s, s->net[net], m, X + b * s->n_in, Yn + b * s->n_out, false, st)) return FLINT_ERR_CUDA;
   }
   return 0;
@@ -509,7 +500,7 @@ int64_t surrogate_nparams(Surrogate* s) { return s->net[0].P; }
 
 int surrogate_advance(Surrogate* s, int64_t n, double* T, const double* p, double* Y, const double* dt,
                       const flint_reactor_opts& o, const flint_surrogate_gate* gate, int* status, int* nsteps,
-                      double* jsave, int jslots, cudaStream_t st) {
+                      double* jsave, int jslots, double* metrics, cudaStream_t st) {
   s->last_accepted = s->last_rejected = 0;
   if (n <= 0) return 0;
   const int64_t CH = 262144;
@@ -529,9 +520,10 @@ int surrogate_advance(Surrogate* s, int64_t n, double* T, const double* p, doubl
     if (cudaMemsetAsync(s->rej_count, 0, 8, st)) return FLINT_ERR_CUDA;
     k_post<<<blocks_for(m, SURR_THREADS), SURR_THREADS, psm, st>>>(
         s->mimg, s->L, m, b, T, p, Y, dt, s->yhat, s->nnets > 1 ? s->yout2 : nullptr, s->ymean, s->ystd, s->proj,
-        s->Bm, s->ne, gp, status, nsteps, s->rej_idx, s->rej_count);
+        s->Bm, s->ne, gp, status, nsteps, s->rej_idx, s->rej_count, metrics ? metrics + b * 6 : nullptr);
     count_launch();
     if (cudaGetLastError()) return FLINT_ERR_CUDA;
+    if (metrics) continue;
     unsigned long long nrej = 0;
     if (cudaMemcpyAsync(&nrej, s->rej_count, 8, cudaMemcpyDeviceToHost, st) || cudaStreamSynchronize(st))
       return FLINT_ERR_CUDA;

@@ -1,0 +1,425 @@
+"""Learned surrogate of the reactor advance: data, training, checkpoints, gate.
+
+The network, its training step (forward, backward, Adam) and the gated
+surrogate + fallback advance all run in the CUDA library
+(``flint_surrogate_*`` in include/flint_gpu.h); this module drives them:
+
+* ``generate``   runs the FP64 GPU integrator on seeded reactor states and
+  returns (state, dt, outcome) samples;
+* ``fit_stats``  input / target normalisation from the training samples;
+* ``Surrogate``  the device handle (features, targets, train_step, predict,
+  advance, state get/set) plus ``save`` / ``load`` of checkpoints holding the
+  weights, the Adam moments, the Adam step, the data-sampler position and the
+  gate;
+* ``train``      Adam with cosine decay on device-resident samples;
+* ``calibrate``  gate thresholds from a held-out set judged by the integrator.
+
+Command line: ``python -m flint_gb300.surrogate train --out PATH`` trains the
+networks of the benchmark and writes PATH (a checkpoint) next to a JSON
+report.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import math
+import os
+import struct
+import time
+
+import numpy as np
+
+from . import native, mechgen
+from .api import Chemistry
+
+_fp = C.POINTER(C.c_float)
+_dp = C.POINTER(C.c_double)
+
+
+class SurrogateDesc(C.Structure):
+    _fields_ = [("n_layers", C.c_int), ("hidden", C.c_int), ("n_nets", C.c_int), ("bath", C.c_int),
+                ("n_elements", C.c_int), ("reserved", C.c_int), ("weights", _fp), ("x_mean", _fp),
+                ("x_std", _fp), ("y_mean", _fp), ("y_std", _fp), ("elem", _dp)]
+
+
+class SurrogateGate(C.Structure):
+    _fields_ = [("max_dT_resid", C.c_double), ("max_elem_resid", C.c_double), ("min_Y", C.c_double),
+                ("max_ens_dT", C.c_double), ("max_ens_dY", C.c_double), ("T_lo", C.c_double),
+                ("T_hi", C.c_double), ("log10p_lo", C.c_double), ("log10p_hi", C.c_double),
+                ("log10dt_lo", C.c_double), ("log10dt_hi", C.c_double)]
+
+
+GATE_KEYS = [f[0] for f in SurrogateGate._fields_]
+
+
+def _bind(L):
+    if getattr(L, "_surrogate_bound", False):
+        return
+    vp, i64 = C.c_void_p, C.c_int64
+    L.flint_surrogate_create.argtypes = [vp, C.POINTER(SurrogateDesc), C.POINTER(vp)]
+    L.flint_surrogate_destroy.argtypes = [vp]
+    L.flint_surrogate_nparams.argtypes = [vp]
+    L.flint_surrogate_nparams.restype = C.c_int64
+    L.flint_surrogate_features.argtypes = [vp, i64, vp, vp, vp, vp, vp, vp]
+    L.flint_surrogate_targets.argtypes = [vp, i64, vp, vp, vp, vp, vp, vp]
+    L.flint_surrogate_train_step.argtypes = [vp, C.c_int, i64, vp, vp, C.c_float, C.POINTER(C.c_double), vp]
+    L.flint_surrogate_predict.argtypes = [vp, C.c_int, i64, vp, vp, vp]
+    L.flint_surrogate_state.argtypes = [vp, C.c_int, _fp, C.POINTER(C.c_int64), C.c_int]
+    L.flint_surrogate_advance.argtypes = [vp, i64, vp, vp, vp, vp, C.POINTER(native.ReactorOpts),
+                                          C.POINTER(SurrogateGate), vp, vp, C.POINTER(C.c_int64), vp]
+    L.flint_surrogate_evaluate.argtypes = [vp, i64, vp, vp, vp, vp, C.POINTER(SurrogateGate), vp, vp]
+    L._surrogate_bound = True
+
+
+def layer_dims(ns, hidden=256, n_layers=5):
+    return [ns + 2] + [hidden] * (n_layers - 1) + [ns + 1]
+
+
+def init_weights(dims, seed):
+    """Uniform(-1/sqrt(fan_in), 1/sqrt(fan_in)) weights and biases, per layer W[out][in] then b[out]."""
+    rng = np.random.default_rng(seed)
+    parts = []
+    for i in range(len(dims) - 1):
+        bound = 1.0 / math.sqrt(dims[i])
+        parts.append(rng.uniform(-bound, bound, dims[i + 1] * dims[i]))
+        parts.append(rng.uniform(-bound, bound, dims[i + 1]))
+    return np.concatenate(parts).astype(np.float32)
+
+
+def _ptr(t):
+    return C.c_void_p(t.data_ptr())
+
+
+def _stream():
+    import torch
+    return C.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+# ------------------------------------------------------------------ data
+def generate(chem, n, seed, states=mechgen.fuel_air_states, **kw):
+    """Seeded reactor states advanced by the FP64 GPU integrator (device tensors).
+
+    Returns dict of T0, p, Y0, dt, T1, Y1 (torch, cuda) and the integrator
+    statuses; cells that fail are dropped."""
+    import torch
+    T0, p, Y0, dt = states(n, chem.mech, seed, **kw)
+    dev = torch.device("cuda")
+    T = torch.from_numpy(T0).to(dev)
+    Y = torch.from_numpy(Y0).to(dev)
+    P = torch.from_numpy(p).to(dev)
+    D = torch.from_numpy(dt).to(dev)
+    st, nst = chem.reactor_advance(T, P, Y, D)
+    torch.cuda.synchronize()
+    ok = (st == 0)
+    T0t, Y0t = torch.from_numpy(T0).to(dev), torch.from_numpy(Y0).to(dev)
+    return {"T0": T0t[ok].contiguous(), "p": P[ok].contiguous(), "Y0": Y0t[ok].contiguous(),
+            "dt": D[ok].contiguous(), "T1": T[ok].contiguous(), "Y1": Y[ok].contiguous(),
+            "nsteps": nst[ok].contiguous(), "n_failed": int((~ok).sum().item())}
+
+
+def fit_stats(d, bath):
+    """Normalisation: inputs (log10 Y but bath, T, log10 p, log10 dt) and targets (dY, dT).
+
+    Species targets share a floor of 5 % of the largest species spread so that
+    the loss weights mass-fraction errors in absolute terms."""
+    Y0 = d["Y0"].cpu().numpy(); Y1 = d["Y1"].cpu().numpy()
+    T0 = d["T0"].cpu().numpy(); T1 = d["T1"].cpu().numpy()
+    p = d["p"].cpu().numpy(); dt = d["dt"].cpu().numpy()
+    ns = Y0.shape[1]
+    keep = [k for k in range(ns) if k != bath]
+    X = np.hstack([np.log10(np.maximum(Y0[:, keep], 1e-20)), T0[:, None], np.log10(p)[:, None],
+                   np.log10(dt)[:, None]])
+    xm, xs = X.mean(0), X.std(0)
+    xs = np.where(xs > 1e-3, xs, 1.0)
+    dY = Y1 - Y0
+    dT = T1 - T0
+    ym = np.concatenate([dY.mean(0), [dT.mean()]])
+    sy = dY.std(0)
+    sy = np.maximum(sy, 0.05 * sy.max())
+    ys = np.concatenate([sy, [max(dT.std(), 1e-3)]])
+    dom = {"T_lo": float(T0.min()), "T_hi": float(T0.max()), "log10p_lo": float(np.log10(p).min()),
+           "log10p_hi": float(np.log10(p).max()), "log10dt_lo": float(np.log10(dt).min()),
+           "log10dt_hi": float(np.log10(dt).max())}
+    return {"x_mean": xm.astype(np.float32), "x_std": xs.astype(np.float32), "y_mean": ym.astype(np.float32),
+            "y_std": ys.astype(np.float32), "bath": int(bath), "domain": dom}
+
+
+DEFAULT_GATE = {"max_dT_resid": 1.0, "max_elem_resid": 1e-5, "min_Y": -1e-6, "max_ens_dT": 1.0, "max_ens_dY": 1e-4}
+
+
+# ---------------------------------------------------------------- handle
+class Surrogate:
+    """The device surrogate bound to an analytic mechanism handle."""
+
+    def __init__(self, chem: Chemistry, stats, weights=None, n_nets=1, hidden=256, n_layers=5, seed=0):
+        self.chem = chem
+        self.L = native.lib()
+        _bind(self.L)
+        self.stats = stats
+        self.ns = chem.ns
+        self.n_in, self.n_out = chem.ns + 2, chem.ns + 1
+        self.dims = layer_dims(chem.ns, hidden, n_layers)
+        self.hidden, self.n_layers, self.n_nets = hidden, n_layers, n_nets
+        if weights is None:
+            weights = np.concatenate([init_weights(self.dims, seed + i) for i in range(n_nets)])
+        self._w = np.ascontiguousarray(weights, dtype=np.float32)
+        E = chem.mech.element_matrix()
+        self._E = np.ascontiguousarray(E, dtype=np.float64)
+        self._keep = {k: np.ascontiguousarray(stats[k], dtype=np.float32) for k in ("x_mean", "x_std", "y_mean", "y_std")}
+        d = SurrogateDesc(n_layers, hidden, n_nets, int(stats["bath"]), E.shape[0], 0,
+                          self._w.ctypes.data_as(_fp), self._keep["x_mean"].ctypes.data_as(_fp),
+                          self._keep["x_std"].ctypes.data_as(_fp), self._keep["y_mean"].ctypes.data_as(_fp),
+                          self._keep["y_std"].ctypes.data_as(_fp), self._E.ctypes.data_as(_dp))
+        h = C.c_void_p()
+        native.check(self.L.flint_surrogate_create(chem.h, C.byref(d), C.byref(h)), "flint_surrogate_create")
+        self.h = h
+        self.P = int(self.L.flint_surrogate_nparams(h))
+        self.gate = dict(DEFAULT_GATE, **stats.get("domain", {}))
+        self.sampler_pos = 0
+        self.rng_state = None
+
+    def close(self):
+        if self.h:
+            self.L.flint_surrogate_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:  # noqa: BLE001
+            pass
+
+    # ---------------------------------------------------------- device ops
+    def features(self, T, p, Y, dt):
+        import torch
+        X = torch.empty((T.shape[0], self.n_in), dtype=torch.float32, device=T.device)
+        native.check(self.L.flint_surrogate_features(self.h, T.shape[0], _ptr(T), _ptr(p), _ptr(Y), _ptr(dt),
+                                                     _ptr(X), _stream()), "flint_surrogate_features")
+        return X
+
+    def targets(self, T0, Y0, T1, Y1):
+        import torch
+        Yt = torch.empty((T0.shape[0], self.n_out), dtype=torch.float32, device=T0.device)
+        native.check(self.L.flint_surrogate_targets(self.h, T0.shape[0], _ptr(T0), _ptr(Y0), _ptr(T1), _ptr(Y1),
+                                                    _ptr(Yt), _stream()), "flint_surrogate_targets")
+        return Yt
+
+    def train_step(self, X, Yt, lr, net=0, want_loss=False):
+        loss = C.c_double(0.0)
+        native.check(self.L.flint_surrogate_train_step(self.h, net, X.shape[0], _ptr(X), _ptr(Yt), float(lr),
+                                                       C.byref(loss) if want_loss else None, _stream()),
+                     "flint_surrogate_train_step")
+        return loss.value if want_loss else None
+
+    def predict(self, X, net=0):
+        import torch
+        Yn = torch.empty((X.shape[0], self.n_out), dtype=torch.float32, device=X.device)
+        native.check(self.L.flint_surrogate_predict(self.h, net, X.shape[0], _ptr(X), _ptr(Yn), _stream()),
+                     "flint_surrogate_predict")
+        return Yn
+
+    def get_state(self, net=0):
+        buf = np.zeros(3 * self.P, dtype=np.float32)
+        step = C.c_int64(0)
+        native.check(self.L.flint_surrogate_state(self.h, net, buf.ctypes.data_as(_fp), C.byref(step), 1),
+                     "flint_surrogate_state")
+        return buf, step.value
+
+    def set_state(self, buf, step, net=0):
+        buf = np.ascontiguousarray(buf, dtype=np.float32)
+        s = C.c_int64(int(step))
+        native.check(self.L.flint_surrogate_state(self.h, net, buf.ctypes.data_as(_fp), C.byref(s), 0),
+                     "flint_surrogate_state")
+
+    def advance(self, T, p, Y, dt, status=None, nsteps=None, gate=None, rtol=1e-8, atol=1e-14, max_steps=20000):
+        import torch
+        g = dict(self.gate, **(gate or {}))
+        gs = SurrogateGate(*[float(g[k]) for k in GATE_KEYS])
+        opts = native.reactor_opts(rtol, atol, max_steps)
+        n = T.shape[0]
+        if status is None:
+            status = torch.empty(n, dtype=torch.int32, device=T.device)
+        if nsteps is None:
+            nsteps = torch.empty(n, dtype=torch.int32, device=T.device)
+        counts = (C.c_int64 * 2)()
+        native.check(self.L.flint_surrogate_advance(self.h, n, _ptr(T), _ptr(p), _ptr(Y), _ptr(dt), C.byref(opts),
+                                                    C.byref(gs), _ptr(status), _ptr(nsteps), counts, _stream()),
+                     "flint_surrogate_advance")
+        return status, nsteps, (counts[0], counts[1])
+
+    def evaluate(self, T, p, Y, dt):
+        """Surrogate result for every cell (T, Y in place) and the gate metrics (n, 6)."""
+        import torch
+        gs = SurrogateGate(*[float(self.gate[k]) for k in GATE_KEYS])
+        M = torch.empty((T.shape[0], 6), dtype=torch.float64, device=T.device)
+        native.check(self.L.flint_surrogate_evaluate(self.h, T.shape[0], _ptr(T), _ptr(p), _ptr(Y), _ptr(dt),
+                                                     C.byref(gs), _ptr(M), _stream()), "flint_surrogate_evaluate")
+        return M
+
+    # ---------------------------------------------------------- checkpoints
+    def save(self, path, extra=None):
+        """Checkpoint: JSON header (dims, stats, gate, Adam steps, sampler state) + FP32 blobs."""
+        nets = [self.get_state(i) for i in range(self.n_nets)]
+        hdr = {"format": "flint-surrogate-1", "ns": self.ns, "dims": self.dims, "hidden": self.hidden,
+               "n_layers": self.n_layers, "n_nets": self.n_nets, "P": self.P,
+               "steps": [s for _, s in nets], "bath": int(self.stats["bath"]),
+               "domain": self.stats.get("domain", {}), "gate": self.gate, "sampler_pos": self.sampler_pos,
+               "rng_state": self.rng_state, "extra": extra or {}}
+        blob = b"".join(self._keep[k].tobytes() for k in ("x_mean", "x_std", "y_mean", "y_std"))
+        blob += b"".join(b.tobytes() for b, _ in nets)
+        h = json.dumps(hdr).encode()
+        with open(path, "wb") as f:
+            f.write(struct.pack("<Q", len(h)))
+            f.write(h)
+            f.write(blob)
+
+    @classmethod
+    def load(cls, chem, path, weights_only=False):
+        with open(path, "rb") as f:
+            (hl,) = struct.unpack("<Q", f.read(8))
+            hdr = json.loads(f.read(hl))
+            data = np.frombuffer(f.read(), dtype=np.float32)
+        ns = hdr["ns"]
+        o = 0
+        stats = {"bath": hdr["bath"], "domain": hdr["domain"]}
+        for k, n in (("x_mean", ns + 2), ("x_std", ns + 2), ("y_mean", ns + 1), ("y_std", ns + 1)):
+            stats[k] = data[o:o + n].copy(); o += n
+        P = hdr["P"]
+        states = [data[o + 3 * P * i:o + 3 * P * (i + 1)].copy() for i in range(hdr["n_nets"])]
+        w0 = np.concatenate([s[:P] for s in states])
+        s = cls(chem, stats, weights=w0, n_nets=hdr["n_nets"], hidden=hdr["hidden"], n_layers=hdr["n_layers"])
+        if not weights_only:
+            for i, st in enumerate(states):
+                s.set_state(st, hdr["steps"][i], net=i)
+        s.gate = dict(s.gate, **hdr.get("gate", {}))
+        s.sampler_pos = hdr.get("sampler_pos", 0)
+        s.rng_state = hdr.get("rng_state")
+        s.header = hdr
+        return s
+
+
+# ---------------------------------------------------------------- training
+def train(sur, X, Yt, steps, batch=4096, lr=1e-3, lr_min=1e-5, net=0, seed=0, log_every=1000, start=0,
+          total=None, log=None):
+    """Adam with cosine decay over device-resident (X, Yt); returns loss history.
+
+    Mini-batches are drawn by a seeded permutation stream: batch i of the run
+    uses generator(seed).permutation epochs, so that resuming at step `start`
+    replays exactly the batches of a continuous run."""
+    import torch
+    n = X.shape[0]
+    total = total or steps
+    hist = []
+    gen = torch.Generator(device=X.device)
+    per_epoch = max(1, n // batch)
+    epoch = -1
+    perm = None
+    for it in range(start, start + steps):
+        e = it // per_epoch
+        if e != epoch:
+            gen.manual_seed(seed * 1000003 + e)
+            perm = torch.randperm(n, generator=gen, device=X.device)
+            epoch = e
+        j = it % per_epoch
+        idx = perm[j * batch:(j + 1) * batch]
+        xb, yb = X.index_select(0, idx).contiguous(), Yt.index_select(0, idx).contiguous()
+        a = lr_min + 0.5 * (lr - lr_min) * (1 + math.cos(math.pi * min(it, total) / total))
+        want = (it + 1) % log_every == 0
+        loss = sur.train_step(xb, yb, a, net=net, want_loss=want)
+        if want:
+            hist.append((it + 1, loss))
+            if log:
+                log(f"net {net} step {it + 1} lr {a:.2e} loss {loss:.3e}")
+    sur.sampler_pos = start + steps
+    return hist
+
+
+def errors_vs_integrator(Tsur, Ysur, Tref, Yref):
+    dT = (Tsur - Tref).abs()
+    dY = (Ysur - Yref).abs().amax(dim=1)
+    return dT, dY
+
+
+def calibrate(sur, d, target_dT=1.0, target_dY=1e-4, margin=0.5):
+    """Gate thresholds from held-out samples judged by the integrator.
+
+    The surrogate is applied to every validation cell (``evaluate``); a grid
+    over the energy-residual and ensemble-spread thresholds (their quantiles)
+    is searched for the largest accepted fraction such that every accepted
+    validation cell is within margin * (target_dT, target_dY) of the FP64
+    integrator.  Returns (accept_fraction, gate dict, max dT, max dY)."""
+    T = d["T0"].clone(); Y = d["Y0"].clone()
+    M = sur.evaluate(T, d["p"], Y, d["dt"]).cpu().numpy()
+    eT = (T - d["T1"]).abs().cpu().numpy()
+    eY = (Y - d["Y1"]).abs().amax(dim=1).cpu().numpy()
+    base = (M[:, 5] > 0) & (M[:, 1] <= sur.gate["max_elem_resid"]) & (M[:, 2] >= sur.gate["min_Y"])
+    good = (eT <= margin * target_dT) & (eY <= margin * target_dY)
+    qs = np.concatenate([[0.0], np.quantile(M[base, 0], np.linspace(0.05, 1.0, 24))]) if base.any() else [0.0]
+    cand_e = [(1e30, 1e30)]
+    if sur.n_nets > 1 and base.any():
+        q3 = np.quantile(M[base, 3], np.linspace(0.05, 1.0, 20))
+        q4 = np.quantile(M[base, 4], np.linspace(0.05, 1.0, 20))
+        cand_e = [(a, b) for a in q3 for b in q4]
+    best = None
+    for a in qs:
+        acc_a = base & (M[:, 0] <= a)
+        for (b, c) in cand_e:
+            acc = acc_a & (M[:, 3] <= b) & (M[:, 4] <= c)
+            if not acc.any() or not good[acc].all():
+                continue
+            frac = acc.mean()
+            if best is None or frac > best[0]:
+                best = (float(frac), {"max_dT_resid": float(a), "max_ens_dT": float(b), "max_ens_dY": float(c)},
+                        float(eT[acc].max()), float(eY[acc].max()))
+    return best
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("cmd", choices=["train"])
+    ap.add_argument("--out", required=True)
+    ap.add_argument("--cells", type=int, default=524288)
+    ap.add_argument("--val", type=int, default=65536)
+    ap.add_argument("--steps", type=int, default=20000)
+    ap.add_argument("--batch", type=int, default=4096)
+    ap.add_argument("--nets", type=int, default=2)
+    ap.add_argument("--seed", type=int, default=7)
+    args = ap.parse_args()
+    import torch
+    chem = Chemistry.from_config("c2")
+    t0 = time.time()
+    d = generate(chem, args.cells, seed=5000 + args.seed)
+    v = generate(chem, args.val, seed=6000 + args.seed)
+    tgen = time.time() - t0
+    bath = chem.mech.index("N2")
+    stats = fit_stats(d, bath)
+    sur = Surrogate(chem, stats, n_nets=args.nets, seed=args.seed)
+    X = sur.features(d["T0"], d["p"], d["Y0"], d["dt"])
+    Yt = sur.targets(d["T0"], d["Y0"], d["T1"], d["Y1"])
+    hist = {}
+    t1 = time.time()
+    for net in range(args.nets):
+        hist[net] = train(sur, X, Yt, args.steps, batch=args.batch, net=net, seed=args.seed + net,
+                          log=print)
+    torch.cuda.synchronize()
+    ttrain = time.time() - t1
+    Xv = sur.features(v["T0"], v["p"], v["Y0"], v["dt"])
+    Yv = sur.targets(v["T0"], v["Y0"], v["T1"], v["Y1"])
+    val_loss = [float(((sur.predict(Xv, net=i) - Yv) ** 2).mean()) for i in range(args.nets)]
+    best = calibrate(sur, v)
+    if best is not None:
+        sur.gate.update(best[1])
+    rep = {"train_cells": int(d["T0"].shape[0]), "val_cells": int(v["T0"].shape[0]), "gen_s": tgen,
+           "train_s": ttrain, "steps": args.steps, "batch": args.batch, "val_loss": val_loss,
+           "loss_history": {str(k): h for k, h in hist.items()},
+           "gate": sur.gate, "calibration": None if best is None else
+           {"accept_frac": best[0], "max_dT": best[2], "max_dY": best[3]}}
+    sur.save(args.out, extra=rep)
+    with open(os.path.splitext(args.out)[0] + ".json", "w") as f:
+        json.dump(rep, f, indent=1)
+    print(json.dumps({k: rep[k] for k in ("train_cells", "gen_s", "train_s", "val_loss", "calibration")}))
+
+
+if __name__ == "__main__":
+    main()

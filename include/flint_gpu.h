@@ -229,6 +229,81 @@ int flint_reactor_advance_noalloc(flint_mech_t mech, int64_t n, double* T, const
                                   double* Y, const double* dt, const flint_reactor_opts* opts,
                                   int* status, int* nsteps, void* stream);
 
+/* ------------------------------------------------------------- surrogate */
+/* Learned surrogate of the reactor advance (no reference counterpart: a new
+ * path next to run_odesolver).  An MLP maps (log10 Y of all species but the
+ * bath, T, log10 p, log10 dt), normalised, to (dY, dT) normalised; BF16
+ * weights and activations as tensor-core operands, FP32 accumulation, FP32
+ * master weights trained by Adam on the device. */
+typedef struct flint_surrogate_s* flint_surrogate_t;
+
+typedef struct {
+  int n_layers;           /* GEMM layers (5 = four hidden layers)            */
+  int hidden;             /* hidden width (256)                              */
+  int n_nets;             /* 1, or 2 for a two-network ensemble               */
+  int bath;               /* species implied by sum Y = 1 (not an input)      */
+  int n_elements;         /* rows of elem                                    */
+  int reserved;
+  const float* weights;   /* [n_nets][P] initial parameters, per layer W[out][in] then b[out] */
+  const float* x_mean;    /* [ns+2] input normalisation                      */
+  const float* x_std;
+  const float* y_mean;    /* [ns+1] target normalisation (dY_k, dT)          */
+  const float* y_std;
+  const double* elem;     /* [n_elements][ns] atoms of each element per species */
+} flint_surrogate_desc;
+
+/* Gate of a surrogate step: a cell is accepted only if every test passes,
+ * else it is re-solved by the BDF integrator from its original state. */
+typedef struct {
+  double max_dT_resid;    /* |T(h conservation) - (T0 + dT_net)| limit [K]     */
+  double max_elem_resid;  /* max_e |sum_k a_ek dY_net,k / W_k| [kmol/kg]        */
+  double min_Y;           /* smallest mass fraction allowed after projection  */
+  double max_ens_dT;      /* two networks: |dT_1 - dT_2| limit [K]              */
+  double max_ens_dY;      /* two networks: max_k |dY_1,k - dY_2,k| limit        */
+  double T_lo, T_hi;      /* input domain of the training data                 */
+  double log10p_lo, log10p_hi;
+  double log10dt_lo, log10dt_hi;
+} flint_surrogate_gate;
+
+int flint_surrogate_create(flint_mech_t mech, const flint_surrogate_desc* desc, flint_surrogate_t* out);
+int flint_surrogate_destroy(flint_surrogate_t s);
+/* Number of parameters of one network. */
+int64_t flint_surrogate_nparams(flint_surrogate_t s);
+/* Normalised inputs X[n][ns+2] (float, device) of cells (T, p, Y, dt). */
+int flint_surrogate_features(flint_surrogate_t s, int64_t n, const double* T, const double* p,
+                             const double* Y, const double* dt, float* X, void* stream);
+/* Normalised targets Yt[n][ns+1] from states before (T0, Y0) and after (T1, Y1). */
+int flint_surrogate_targets(flint_surrogate_t s, int64_t n, const double* T0, const double* Y0,
+                            const double* T1, const double* Y1, float* Yt, void* stream);
+/* One Adam step of network `net` on a device batch; *loss (may be NULL) gets
+ * the batch MSE before the update (synchronises the stream when non-NULL). */
+int flint_surrogate_train_step(flint_surrogate_t s, int net, int64_t n, const float* X,
+                               const float* Yt, float lr, double* loss, void* stream);
+/* Forward pass of network `net`: normalised outputs Yn[n][ns+1] (device). */
+int flint_surrogate_predict(flint_surrogate_t s, int net, int64_t n, const float* X, float* Yn,
+                            void* stream);
+/* Training state of network `net` (host buffer of 3*P floats: weights, Adam
+ * first and second moments) and its Adam step: get = 1 reads, 0 writes. */
+int flint_surrogate_state(flint_surrogate_t s, int net, float* host, int64_t* step, int get);
+/* Surrogate + fallback advance with the arguments of flint_reactor_advance.
+ * Accepted cells: status FLINT_CELL_OK, nsteps 0; rejected cells are re-solved
+ * by the BDF integrator (status FLINT_CELL_SURROGATE_REJECTED when it
+ * succeeds, else its failure code; nsteps its step count).  counts (may be
+ * NULL) gets {accepted, rejected}. */
+int flint_surrogate_advance(flint_surrogate_t s, int64_t n, double* T, const double* p, double* Y,
+                            const double* dt, const flint_reactor_opts* opts,
+                            const flint_surrogate_gate* gate, int* status, int* nsteps,
+                            int64_t* counts, void* stream);
+
+/* Apply the surrogate to every cell (no gate, no fallback; T, Y in place) and
+ * write the gate quantities per cell, metrics[cell][6] = {energy residual [K],
+ * element residual, min Y after projection, ensemble |dT| spread, ensemble
+ * max |dY| spread, 1 if the input is inside the gate's domain else 0}: the
+ * calibration of the gate thresholds. */
+int flint_surrogate_evaluate(flint_surrogate_t s, int64_t n, double* T, const double* p, double* Y,
+                             const double* dt, const flint_surrogate_gate* gate, double* metrics,
+                             void* stream);
+
 /* Work counters of the last flint_reactor_advance on this handle (blocks until
  * it has finished): out[0] RHS evaluations, out[1] Jacobian evaluations,
  * out[2] Newton iterations (one LU solve each), out[3] accepted steps,
