@@ -279,6 +279,143 @@ def run_ours(args):
         torch.distributed.destroy_process_group()
 
 
+SURROGATE_CKPT = os.path.join(REPO, "flint_gb300", "data", "surrogate_c3.bin")
+SUR_CELLS = 1048576
+PLAIN_SAMPLE = 131072
+
+
+def run_surrogate(args):
+    """Headline: surrogate + fallback advance of 1,048,576 reactor cells vs the
+    plain FP64 integrator, errors judged by the integrator on a 131,072-cell sample."""
+    import torch
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+        torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    from flint_gb300 import mechgen
+    from flint_gb300.api import Chemistry, reactor_stats, kernel_launches
+    from flint_gb300.surrogate import Surrogate
+    chem = Chemistry(mechgen.load("c2"))
+    sur = Surrogate.load(chem, args.checkpoint, weights_only=True)
+    n = args.cells or SUR_CELLS
+    T0, p0, Y0, dt0 = mechgen.c3_states(n, chem.mech, seed=1004 + rank)
+    Td0, Yd0 = torch.from_numpy(T0).to(dev), torch.from_numpy(Y0).to(dev)
+    pd, dtd = torch.from_numpy(p0).to(dev), torch.from_numpy(dt0).to(dev)
+    Td, Yd = Td0.clone(), Yd0.clone()
+    st = torch.empty(n, dtype=torch.int32, device=dev)
+    nst = torch.empty(n, dtype=torch.int32, device=dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream()
+    counts = {}
+
+    def step():
+        Td.copy_(Td0)
+        Yd.copy_(Yd0)
+        _, _, c = sur.advance(Td, pd, Yd, dtd, status=st, nsteps=nst)
+        counts["c"] = c
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    l0 = kernel_launches()
+    times = []
+    if ws > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    for _ in range(args.steps):
+        flush.zero_()
+        e0 = torch.cuda.Event(enable_timing=True); e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream); step(); e1.record(stream); e1.synchronize()
+        times.append(e0.elapsed_time(e1) / 1e3)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    launches = kernel_launches() - l0
+    fb = reactor_stats(chem)
+    t_sur = statistics.mean(times)
+    if ws > 1:
+        tt = torch.tensor([t_sur], device=dev, dtype=torch.float64)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        t_sur = float(tt.item())
+    acc, rej = counts["c"]
+    Ts, Ys, sts, nsts = Td.clone(), Yd.clone(), st.clone(), nst.clone()
+    # ---- plain FP64 integrator on a sample of the same cells (timed) + errors
+    m = min(PLAIN_SAMPLE, n)
+    Tp, Yp = Td0[:m].clone(), Yd0[:m].clone()
+    stp = torch.empty(m, dtype=torch.int32, device=dev); nsp = torch.empty(m, dtype=torch.int32, device=dev)
+    flush.zero_()
+    e0 = torch.cuda.Event(enable_timing=True); e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    chem.reactor_advance(Tp, pd[:m], Yp, dtd[:m], status=stp, nsteps=nsp)
+    e1.record(stream); e1.synchronize()
+    t_plain = e0.elapsed_time(e1) / 1e3
+    plain_stats = reactor_stats(chem)
+    plain = m / t_plain
+    dT = (Ts[:m] - Tp).abs()
+    dY = (Ys[:m] - Yp).abs().amax(dim=1)
+    accm = (sts[:m] == 0) & (nsts[:m] == 0)
+    # ---- end to end through pinned host buffers
+    Th = torch.from_numpy(T0).pin_memory(); ph = torch.from_numpy(p0).pin_memory()
+    Yh = torch.from_numpy(Y0).pin_memory(); dth = torch.from_numpy(dt0).pin_memory()
+    To = torch.empty_like(Th).pin_memory(); Yo = torch.empty_like(Yh).pin_memory()
+    so = torch.empty(n, dtype=torch.int32).pin_memory()
+    Te, pe, Ye, dte = (torch.empty_like(x, device=dev) for x in (Th, ph, Yh, dth))
+    h2d = sum(x.numel() * x.element_size() for x in (Th, ph, Yh, dth))
+    d2h = sum(x.numel() * x.element_size() for x in (To, Yo, so))
+    e2e = []
+    for i in range(args.warmup + args.steps):
+        flush.zero_(); torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        Te.copy_(Th, non_blocking=True); pe.copy_(ph, non_blocking=True)
+        Ye.copy_(Yh, non_blocking=True); dte.copy_(dth, non_blocking=True)
+        sur.advance(Te, pe, Ye, dte, status=st, nsteps=nst)
+        To.copy_(Te, non_blocking=True); Yo.copy_(Ye, non_blocking=True); so.copy_(st, non_blocking=True)
+        torch.cuda.synchronize()
+        if i >= args.warmup:
+            e2e.append(time.perf_counter() - t0)
+    t_e2e = statistics.mean(e2e)
+    if ws > 1:
+        tt = torch.tensor([t_e2e], device=dev, dtype=torch.float64)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        t_e2e = float(tt.item())
+    ops = (fb["rhs"] * FP64_OPS["rhs"] + fb["jac"] * FP64_OPS["jac"] + fb["lu"] * FP64_OPS["lu"]
+           + fb["newton"] * FP64_OPS["solve"])
+    peak = chem_peak_fp64()
+    line = {"metric": METRIC, "value": n * ws / t_sur, "unit": "cell-steps/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t_sur * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64 (integrator, gate) + bf16/fp32 (network)",
+            "data": "synthetic (seeded states, seeded synthetic mechanism)",
+            "config": {"workload": "reactor-c4: surrogate+fallback, 31sp/160r, 1048576 cells, rtol 1e-8 atol 1e-14",
+                       "cells_per_gpu": n, "path": "surrogate + FP64 BDF fallback",
+                       "network": "MLP 33-256-256-256-256-32 GELU x2 (ensemble), bf16 mma.sync, fp32 accumulate",
+                       "l2": "flushed (256 MiB write) between timed steps"},
+            "surrogate": {"accepted": int(acc), "rejected": int(rej), "accept_frac": acc / max(acc + rej, 1),
+                          "plain_fp64_cell_steps_per_s": plain, "plain_sample_cells": m,
+                          "speedup_vs_plain": (n / t_sur) / plain,
+                          "max_abs_dT_K": float(dT.max()), "max_abs_dY": float(dY.max()),
+                          "max_abs_dT_accepted_K": float(dT[accm].max()) if accm.any() else 0.0,
+                          "max_abs_dY_accepted": float(dY[accm].max()) if accm.any() else 0.0,
+                          "target": {"dT_K": 1.0, "dY": 1e-4}, "gate": sur.gate},
+            "e2e": {"value": n * ws / t_e2e, "unit": "cell-steps/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h},
+            "gpu_launches": launches, "clocks": clk,
+            "roofline": {"bound": "fp64", "kernel": "k_reactor (fallback cells)",
+                         "achieved": ops / t_sur / 1e12 if ops else 0.0, "peak": peak, "unit": "TFLOP/s",
+                         "frac": (ops / t_sur / 1e12) / peak if (peak and ops) else None, "traffic": None,
+                         "peak_source": "DFMA probe kernel measured in this run (MEASURED_PEAKS.json has no FP64 figure)",
+                         "events_per_launch": fb,
+                         "plain_leg": {"events": plain_stats, "seconds": t_plain}}}
+    if rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(chem.mech, T0, p0, Y0, dt0)
+    if rank == 0:
+        print(json.dumps(line))
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
 def run_kernel_workload(args):
     """Source-term workloads: c1-wdot (65,536 states, 2-step CH4/air: wdot, cp, h)
     and c2-wdotjac (1,048,576 states, 31 species: wdot + 32x32 Jacobian).
@@ -350,14 +487,24 @@ def main():
     ap.add_argument("--workload", default="reactor", choices=["reactor", "c1-wdot", "c2-wdot", "c2-wdotjac"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--ref-seconds", type=float, default=10.0)
+    ap.add_argument("--path", default="auto", choices=["auto", "surrogate", "plain"],
+                    help="surrogate+fallback (headline, needs the trained checkpoint) or the plain integrator")
+    ap.add_argument("--checkpoint", default=SURROGATE_CKPT)
     args = ap.parse_args()
     if args.workload != "reactor":
         run_kernel_workload(args)
         return
-    args.cells = args.cells or CELLS
     if args.impl == "reference":
+        args.cells = args.cells or CELLS
         run_reference(args)
+        return
+    path = args.path
+    if path == "auto":
+        path = "surrogate" if os.path.exists(args.checkpoint) else "plain"
+    if path == "surrogate":
+        run_surrogate(args)
     else:
+        args.cells = args.cells or CELLS
         run_ours(args)
 
 

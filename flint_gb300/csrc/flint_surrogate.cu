@@ -3,11 +3,15 @@
 //
 // A cell (T0, p, Y0, dt) is mapped by an MLP (flint_mlp.cu) to (dY, dT) over dt.
 // The prediction is then made exactly conservative and checked:
-//   * element conservation: dY is projected onto the null space of the
-//     element matrix (mass fractions: sum_k a_ek dY_k / W_k = 0; total mass
-//     follows), P = I - B^T (B B^T)^-1 B;
+//   * element conservation with non-negative mass fractions: dY is projected
+//     onto the null space of the element matrix (mass fractions:
+//     sum_k a_ek dY_k / W_k = 0; total mass follows) by least squares over the
+//     species not clipped at zero, clipping negatives and repeating
+//     (an active-set projection, at most 4 passes);
 //   * energy conservation (adiabatic, constant p): T1 solves h(T1, Y1) = h(T0, Y0)
 //     by Newton on the NASA-7 enthalpy, started from the network's T0 + dT;
+//   (no clipping afterwards: a mass fraction below the gate's min_Y rejects
+//   the cell, so accepted results conserve elements and enthalpy exactly)
 // and the cell is accepted only if the residuals of the raw prediction are
 // small: |T1(h) - (T0 + dT_net)| (energy residual), the element residual
 // |B dY_net| (projection size), min Y1 (realizability), the input inside the
@@ -119,9 +123,7 @@ k_post(const uint8_t* __restrict__ img, ImageLayout L, int64_t n, int64_t base, 
   MechView m;
   m.bind(L, smem);
   const int ns = m.ns, nout = ns + 1;
-  double* sP = reinterpret_cast<double*>(smem + L.bytes);
-  for (int i = threadIdx.x; i < ns * ns; i += blockDim.x) sP[i] = proj[i];
-  double* sB = sP + ns * ns;
+  double* sB = reinterpret_cast<double*>(smem + L.bytes);
   for (int i = threadIdx.x; i < ne * ns; i += blockDim.x) sB[i] = Bm[i];
   __syncthreads();
   double dY[32], Y1[32];
@@ -154,14 +156,68 @@ k_post(const uint8_t* __restrict__ img, ImageLayout L, int64_t n, int64_t base, 
       for (int k = 0; k < ns; ++k) s += sB[e * ns + k] * dY[k];
       er = fmax(er, fabs(s));
     }
-    // projection and realizability
-    double ymin = 1.0;
-    for (int k = 0; k < ns; ++k) {
-      double s = 0.0;
-      for (int j = 0; j < ns; ++j) s += sP[k * ns + j] * dY[j];
-      Y1[k] = Y[cell * ns + k] + s;
-      ymin = fmin(ymin, Y1[k]);
+    // conservative, non-negative mass fractions: project dY onto element
+    // conservation over the free species, clip negatives to zero (they leave
+    // the free set), repeat (active-set least-squares, at most 4 passes)
+    unsigned int fixed = 0u;   // bit k: species k clipped at zero
+    double clipped = 0.0;
+    for (int k = 0; k < ns; ++k) Y1[k] = Y[cell * ns + k] + dY[k];
+    bool clean = false;
+    for (int pass = 0; pass < 4 && !clean; ++pass) {
+      double r[8], G[8][8], lam[8];
+      for (int e = 0; e < ne; ++e) {
+        double se = 0.0;
+        for (int k = 0; k < ns; ++k) se += sB[e * ns + k] * (Y1[k] - Y[cell * ns + k]);
+        r[e] = se;
+        for (int f = 0; f < ne; ++f) {
+          double g = 0.0;
+          for (int k = 0; k < ns; ++k)
+            if (!((fixed >> k) & 1u)) g += sB[e * ns + k] * sB[f * ns + k];
+          G[e][f] = g;
+        }
+      }
+      // solve G lam = r (Gauss-Jordan, partial pivoting; empty rows get lam = 0)
+      for (int e = 0; e < ne; ++e) lam[e] = r[e];
+      int live[8];
+      for (int c = 0; c < ne; ++c) {
+        int pr = c; double best = fabs(G[c][c]);
+        for (int q = c + 1; q < ne; ++q) if (fabs(G[q][c]) > best) { best = fabs(G[q][c]); pr = q; }
+        live[c] = best > 1e-300;
+        if (!live[c]) continue;
+        if (pr != c) {
+          for (int f = 0; f < ne; ++f) { double t = G[c][f]; G[c][f] = G[pr][f]; G[pr][f] = t; }
+          double t = lam[c]; lam[c] = lam[pr]; lam[pr] = t;
+        }
+        const double inv = 1.0 / G[c][c];
+        for (int f = 0; f < ne; ++f) G[c][f] *= inv;
+        lam[c] *= inv;
+        for (int q = 0; q < ne; ++q) {
+          if (q == c) continue;
+          const double fq = G[q][c];
+          for (int f = 0; f < ne; ++f) G[q][f] -= fq * G[c][f];
+          lam[q] -= fq * lam[c];
+        }
+      }
+      for (int e = 0; e < ne; ++e) if (!live[e]) lam[e] = 0.0;
+      clean = true;
+      for (int k = 0; k < ns; ++k) {
+        if ((fixed >> k) & 1u) continue;
+        double corr = 0.0;
+        for (int e = 0; e < ne; ++e) corr += sB[e * ns + k] * lam[e];
+        Y1[k] -= corr;
+        if (Y1[k] < 0.0 && pass < 3) {
+          clipped += -Y1[k];
+          Y1[k] = 0.0;
+          fixed |= 1u << k;
+          clean = false;
+        }
+      }
     }
+    double ymin = 1.0;
+    for (int k = 0; k < ns; ++k) ymin = fmin(ymin, Y1[k]);
+    // realizability measure reported to the gate: clipped mass (negative) or
+    // the most negative mass fraction left
+    const double yreal = fmin(-clipped, ymin);
     // energy: h(T1, Y1) = h(T0, Y0), Newton from the network's temperature
     double h0 = 0.0;
     {
@@ -189,15 +245,15 @@ k_post(const uint8_t* __restrict__ img, ImageLayout L, int64_t n, int64_t base, 
       // evaluation mode: every cell takes the surrogate result, the gate
       // quantities are reported instead of applied
       double* mt = metrics + i * 6;
-      mt[0] = dTres; mt[1] = er; mt[2] = ymin; mt[3] = ensT; mt[4] = ens; mt[5] = ok ? 1.0 : 0.0;
-      for (int k = 0; k < ns; ++k) Y[cell * ns + k] = Y1[k] > 0.0 ? Y1[k] : 0.0;
+      mt[0] = dTres; mt[1] = er; mt[2] = yreal; mt[3] = ensT; mt[4] = ens; mt[5] = ok ? 1.0 : 0.0;
+      for (int k = 0; k < ns; ++k) Y[cell * ns + k] = Y1[k];
       T[cell] = conv ? T1 : T0 + dTn;
       continue;
     }
-    ok = ok && conv && dTres <= gp.max_dT_resid && er <= gp.max_elem_resid && ymin >= gp.min_Y;
+    ok = ok && conv && dTres <= gp.max_dT_resid && er <= gp.max_elem_resid && yreal >= gp.min_Y && ymin >= 0.0;
     if (yn2) ok = ok && ensT <= gp.max_ens_dT && ens <= gp.max_ens_dY;
     if (ok) {
-      for (int k = 0; k < ns; ++k) Y[cell * ns + k] = Y1[k] > 0.0 ? Y1[k] : 0.0;
+      for (int k = 0; k < ns; ++k) Y[cell * ns + k] = Y1[k];
       T[cell] = T1;
       if (status) status[cell] = FLINT_CELL_OK;
       if (nsteps) nsteps[cell] = 0;
@@ -510,7 +566,7 @@ int surrogate_advance(Surrogate* s, int64_t n, double* T, const double* p, doubl
   gp.max_ens_dT = gate->max_ens_dT; gp.max_ens_dY = gate->max_ens_dY;
   gp.Tlo = gate->T_lo; gp.Thi = gate->T_hi; gp.lpl = gate->log10p_lo; gp.lph = gate->log10p_hi;
   gp.ldl = gate->log10dt_lo; gp.ldh = gate->log10dt_hi;
-  const size_t psm = s->L.bytes + (size_t)(s->ns * s->ns + std::max(s->ne, 1) * s->ns) * sizeof(double);
+  const size_t psm = s->L.bytes + (size_t)(std::max(s->ne, 1) * s->ns) * sizeof(double);
   cudaFuncSetAttribute(k_post, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)psm);
   for (int64_t b = 0; b < n; b += s->cap) {
     const int64_t m = std::min<int64_t>(s->cap, n - b);

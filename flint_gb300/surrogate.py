@@ -145,7 +145,9 @@ def fit_stats(d, bath):
             "y_std": ys.astype(np.float32), "bath": int(bath), "domain": dom}
 
 
-DEFAULT_GATE = {"max_dT_resid": 1.0, "max_elem_resid": 1e-5, "min_Y": -1e-6, "max_ens_dT": 1.0, "max_ens_dY": 1e-4}
+DEFAULT_GATE = {"max_dT_resid": 1.0, "max_elem_resid": 1e-4, "min_Y": -1e-4, "max_ens_dT": 1.0, "max_ens_dY": 1e-4,
+                "T_lo": 0.0, "T_hi": 1e9, "log10p_lo": -1e9, "log10p_hi": 1e9, "log10dt_lo": -1e9,
+                "log10dt_hi": 1e9}
 
 
 # ---------------------------------------------------------------- handle
@@ -258,10 +260,14 @@ class Surrogate:
         return M
 
     # ---------------------------------------------------------- checkpoints
-    def save(self, path, extra=None):
-        """Checkpoint: JSON header (dims, stats, gate, Adam steps, sampler state) + FP32 blobs."""
+    def save(self, path, extra=None, inference_only=False):
+        """Checkpoint: JSON header (dims, stats, gate, Adam steps, sampler state) + FP32 blobs
+        (weights, Adam first and second moments per network; weights only when inference_only)."""
         nets = [self.get_state(i) for i in range(self.n_nets)]
-        hdr = {"format": "flint-surrogate-1", "ns": self.ns, "dims": self.dims, "hidden": self.hidden,
+        if inference_only:
+            nets = [(b[:self.P], k) for b, k in nets]
+        hdr = {"format": "flint-surrogate-1", "inference_only": bool(inference_only),
+               "ns": self.ns, "dims": self.dims, "hidden": self.hidden,
                "n_layers": self.n_layers, "n_nets": self.n_nets, "P": self.P,
                "steps": [s for _, s in nets], "bath": int(self.stats["bath"]),
                "domain": self.stats.get("domain", {}), "gate": self.gate, "sampler_pos": self.sampler_pos,
@@ -286,10 +292,11 @@ class Surrogate:
         for k, n in (("x_mean", ns + 2), ("x_std", ns + 2), ("y_mean", ns + 1), ("y_std", ns + 1)):
             stats[k] = data[o:o + n].copy(); o += n
         P = hdr["P"]
-        states = [data[o + 3 * P * i:o + 3 * P * (i + 1)].copy() for i in range(hdr["n_nets"])]
+        per = P if hdr.get("inference_only") else 3 * P
+        states = [data[o + per * i:o + per * (i + 1)].copy() for i in range(hdr["n_nets"])]
         w0 = np.concatenate([s[:P] for s in states])
         s = cls(chem, stats, weights=w0, n_nets=hdr["n_nets"], hidden=hdr["hidden"], n_layers=hdr["n_layers"])
-        if not weights_only:
+        if not weights_only and not hdr.get("inference_only"):
             for i, st in enumerate(states):
                 s.set_state(st, hdr["steps"][i], net=i)
         s.gate = dict(s.gate, **hdr.get("gate", {}))
@@ -361,6 +368,19 @@ def calibrate(sur, d, target_dT=1.0, target_dY=1e-4, margin=0.5):
         q3 = np.quantile(M[base, 3], np.linspace(0.05, 1.0, 20))
         q4 = np.quantile(M[base, 4], np.linspace(0.05, 1.0, 20))
         cand_e = [(a, b) for a in q3 for b in q4]
+    diag = {"eT_q": [float(x) for x in np.quantile(eT, [0.5, 0.9, 0.99, 0.999, 1.0])],
+            "eY_q": [float(x) for x in np.quantile(eY, [0.5, 0.9, 0.99, 0.999, 1.0])],
+            "resid_q": [float(x) for x in np.quantile(M[:, 0], [0.5, 0.9, 0.99, 1.0])],
+            "ensT_q": [float(x) for x in np.quantile(M[:, 3], [0.5, 0.9, 0.99, 1.0])],
+            "ensY_q": [float(x) for x in np.quantile(M[:, 4], [0.5, 0.9, 0.99, 1.0])],
+            "elem_q": [float(x) for x in np.quantile(M[:, 1], [0.5, 0.9, 1.0])],
+            "minY_q": [float(x) for x in np.quantile(M[:, 2], [0.0, 0.01, 0.5])],
+            "base_frac": float(base.mean()), "good_frac": float(good.mean())}
+    calibrate.diag = diag
+    calibrate.data = {"M": M, "eT": eT, "eY": eY,
+                      "eYk": (Y - d["Y1"]).abs().cpu().numpy().astype(np.float32),
+                      "T0": d["T0"].cpu().numpy(), "p": d["p"].cpu().numpy(), "dt": d["dt"].cpu().numpy(),
+                      "Y0": d["Y0"].cpu().numpy().astype(np.float32)}
     best = None
     for a in qs:
         acc_a = base & (M[:, 0] <= a)
@@ -385,6 +405,8 @@ def main():
     ap.add_argument("--batch", type=int, default=4096)
     ap.add_argument("--nets", type=int, default=2)
     ap.add_argument("--seed", type=int, default=7)
+    ap.add_argument("--margin", type=float, default=0.8)
+    ap.add_argument("--lr", type=float, default=1e-3)
     args = ap.parse_args()
     import torch
     chem = Chemistry.from_config("c2")
@@ -401,21 +423,26 @@ def main():
     t1 = time.time()
     for net in range(args.nets):
         hist[net] = train(sur, X, Yt, args.steps, batch=args.batch, net=net, seed=args.seed + net,
-                          log=print)
+                          lr=args.lr, log=print)
     torch.cuda.synchronize()
     ttrain = time.time() - t1
     Xv = sur.features(v["T0"], v["p"], v["Y0"], v["dt"])
     Yv = sur.targets(v["T0"], v["Y0"], v["T1"], v["Y1"])
     val_loss = [float(((sur.predict(Xv, net=i) - Yv) ** 2).mean()) for i in range(args.nets)]
-    best = calibrate(sur, v)
+    best = calibrate(sur, v, margin=args.margin)
+    print("calibration diagnostics", json.dumps(getattr(calibrate, "diag", {})))
     if best is not None:
         sur.gate.update(best[1])
     rep = {"train_cells": int(d["T0"].shape[0]), "val_cells": int(v["T0"].shape[0]), "gen_s": tgen,
            "train_s": ttrain, "steps": args.steps, "batch": args.batch, "val_loss": val_loss,
            "loss_history": {str(k): h for k, h in hist.items()},
-           "gate": sur.gate, "calibration": None if best is None else
+           "gate": sur.gate, "diagnostics": getattr(calibrate, "diag", {}),
+           "calibration": None if best is None else
            {"accept_frac": best[0], "max_dT": best[2], "max_dY": best[3]}}
+    if getattr(calibrate, "data", None) is not None:
+        np.savez_compressed(os.path.splitext(args.out)[0] + "_val.npz", **calibrate.data)
     sur.save(args.out, extra=rep)
+    sur.save(os.path.splitext(args.out)[0] + "_inference.bin", extra=rep, inference_only=True)
     with open(os.path.splitext(args.out)[0] + ".json", "w") as f:
         json.dump(rep, f, indent=1)
     print(json.dumps({k: rep[k] for k in ("train_cells", "gen_s", "train_s", "val_loss", "calibration")}))

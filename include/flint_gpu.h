@@ -257,7 +257,7 @@ typedef struct {
 typedef struct {
   double max_dT_resid;    /* |T(h conservation) - (T0 + dT_net)| limit [K]     */
   double max_elem_resid;  /* max_e |sum_k a_ek dY_net,k / W_k| [kmol/kg]        */
-  double min_Y;           /* smallest mass fraction allowed after projection  */
+  double min_Y;           /* -(mass clipped to keep Y >= 0) must be >= min_Y   */
   double max_ens_dT;      /* two networks: |dT_1 - dT_2| limit [K]              */
   double max_ens_dY;      /* two networks: max_k |dY_1,k - dY_2,k| limit        */
   double T_lo, T_hi;      /* input domain of the training data                 */
@@ -297,7 +297,7 @@ int flint_surrogate_advance(flint_surrogate_t s, int64_t n, double* T, const dou
 
 /* Apply the surrogate to every cell (no gate, no fallback; T, Y in place) and
  * write the gate quantities per cell, metrics[cell][6] = {energy residual [K],
- * element residual, min Y after projection, ensemble |dT| spread, ensemble
+ * element residual, -(clipped mass), ensemble |dT| spread, ensemble
  * max |dY| spread, 1 if the input is inside the gate's domain else 0}: the
  * calibration of the gate thresholds. */
 int flint_surrogate_evaluate(flint_surrogate_t s, int64_t n, double* T, const double* p, double* Y,

@@ -50,13 +50,15 @@ def np_forward_backward(w, dims, X, T):
     return y, grads
 
 
-def small_surrogate(seed=0, n_nets=1, hidden=64, n_layers=3):
+def small_surrogate(seed=0, n_nets=1, hidden=64, n_layers=3, dy_scale=1.0):
     from flint_gb300.api import Chemistry
     from flint_gb300.surrogate import Surrogate
     chem = Chemistry.from_config("c2")
     ns = chem.ns
+    ys = np.full(ns + 1, dy_scale, np.float32)
+    ys[-1] = 1.0
     stats = {"x_mean": np.zeros(ns + 2, np.float32), "x_std": np.ones(ns + 2, np.float32),
-             "y_mean": np.zeros(ns + 1, np.float32), "y_std": np.ones(ns + 1, np.float32),
+             "y_mean": np.zeros(ns + 1, np.float32), "y_std": ys,
              "bath": chem.mech.index("N2"), "domain": {}}
     return chem, Surrogate(chem, stats, n_nets=n_nets, hidden=hidden, n_layers=n_layers, seed=seed)
 
@@ -145,7 +147,7 @@ def test_accepted_cells_conserve_elements_and_enthalpy():
     """With an open gate every in-domain cell takes the network step, made exactly
     conservative: elements by projection, enthalpy by the Newton temperature."""
     from oracle.oracle import Oracle
-    chem, sur = small_surrogate(seed=3)
+    chem, sur = small_surrogate(seed=3, dy_scale=1e-4)
     T, p, Y, dt = _cells(chem, 256, 43)
     T0, Y0 = T.cpu().numpy(), Y.cpu().numpy()
     open_gate = {"max_dT_resid": 1e30, "max_elem_resid": 1e30, "min_Y": -1e30, "T_lo": 0.0, "T_hi": 1e9,
@@ -156,15 +158,14 @@ def test_accepted_cells_conserve_elements_and_enthalpy():
     stn, nsn = st.cpu().numpy(), ns.cpu().numpy()
     ok = (stn == 0) & (nsn == 0)
     assert ok.sum() == acc and acc > 0
+    assert (Y.cpu().numpy()[ok] >= 0.0).all()
     T1, Y1 = T.cpu().numpy(), Y.cpu().numpy()
     E = chem.mech.element_matrix()
     W = np.array([s.mw for s in chem.mech.species])
     el0 = (Y0 / W) @ E.T
     el1 = (Y1 / W) @ E.T
-    # clipping of tiny negative mass fractions is the only non-conservative step
-    neg = (Y0 + 0 < 0).any()
-    assert not neg
-    np.testing.assert_allclose(el1[ok], el0[ok], rtol=1e-6, atol=1e-9)
+    np.testing.assert_allclose(el1[ok], el0[ok], rtol=0, atol=1e-12 * np.abs(el0).max())
+    assert np.abs(Y1[ok].sum(1) - Y0[ok].sum(1)).max() < 1e-12
     orc = Oracle(chem.mech)
     P = p.cpu().numpy()
     for i in np.flatnonzero(ok)[:40]:
