@@ -56,6 +56,8 @@ struct flint_mech_s {
   // saved-Jacobian scratch of the reactor, one slot per resident warp
   double* djsave = nullptr;
   int jslots = 0;
+  // Jacobian work area of the warp kernels for 32-63 species
+  double* dwscratch = nullptr;
   // staging buffers of the *_host entry points (grow only)
   void* dstage = nullptr;
   size_t stage_bytes = 0;
@@ -67,7 +69,7 @@ namespace flint {
 static int pack(const flint_mech_desc* d, ImageLayout& L, std::vector<uint8_t>& img) {
   const int ns = d->ns, nr = d->nr;
   if (ns < 1 || nr < 0) return fail(FLINT_ERR_ARG, "ns=%d nr=%d", ns, nr);
-  if (ns > 31) return fail(FLINT_ERR_MECH, "ns=%d: the kernels of this build support up to 31 species", ns);
+  if (ns > 63) return fail(FLINT_ERR_MECH, "ns=%d: the kernels of this build support up to 63 species", ns);
   if (!d->mw || !d->nasa7 || (nr > 0 && (!d->rtype || !d->reversible || !d->arrh || !d->rsp || !d->rnu ||
                                          !d->rord || !d->psp || !d->pnu)))
     return fail(FLINT_ERR_ARG, "NULL array in mechanism description");
@@ -267,6 +269,7 @@ int flint_mech_destroy(flint_mech_t h) {
   if (h->dcounter) cudaFree(h->dcounter);
   if (h->dstage) cudaFree(h->dstage);
   if (h->djsave) cudaFree(h->djsave);
+  if (h->dwscratch) cudaFree(h->dwscratch);
   delete h;
   return FLINT_OK;
 }
@@ -331,7 +334,12 @@ int flint_wdot_jac_batch(flint_mech_t h, int64_t n, int layout, const double* T,
   if (rc) return rc;
   if (n == 0) return FLINT_OK;
   if (!T || !p || !Y || !jac) return fail(FLINT_ERR_ARG, "NULL array");
-  cudaError_t e = launch_wdot_jac(h->dimg, h->L, n, layout, T, p, Y, wdot, jac, (cudaStream_t)stream);
+  const int64_t need = warp_jac_scratch_doubles(h->L);
+  if (need > 0 && !h->dwscratch) {
+    cudaError_t ea = cudaMalloc(&h->dwscratch, (size_t)need * sizeof(double));
+    if (ea != cudaSuccess) { h->dwscratch = nullptr; return fail(FLINT_ERR_NOMEM, "Jacobian work area: %s", cudaGetErrorString(ea)); }
+  }
+  cudaError_t e = launch_wdot_jac(h->dimg, h->L, n, layout, T, p, Y, wdot, jac, h->dwscratch, (cudaStream_t)stream);
   return e == cudaSuccess ? FLINT_OK : cuda_fail(e, "flint_wdot_jac_batch");
 }
 
@@ -365,7 +373,7 @@ int flint_reactor_advance(flint_mech_t h, int64_t n, double* T, const double* p,
   if (!h->djsave) {
     int slots = reactor_slots(h->L);
     if (slots < 1) return fail(FLINT_ERR_MECH, "reactor kernel does not fit this mechanism (shared memory)");
-    cudaError_t ea = cudaMalloc(&h->djsave, (size_t)slots * reactor_slot_bytes());
+    cudaError_t ea = cudaMalloc(&h->djsave, (size_t)slots * reactor_slot_bytes(h->L));
     if (ea != cudaSuccess) { h->djsave = nullptr; return fail(FLINT_ERR_NOMEM, "reactor scratch: %s", cudaGetErrorString(ea)); }
     h->jslots = slots;
   }
@@ -402,7 +410,7 @@ static int ensure_jsave(flint_mech_t h) {
   if (h->djsave) return FLINT_OK;
   int slots = reactor_slots(h->L);
   if (slots < 1) return fail(FLINT_ERR_MECH, "reactor kernel does not fit this mechanism (shared memory)");
-  cudaError_t ea = cudaMalloc(&h->djsave, (size_t)slots * reactor_slot_bytes());
+  cudaError_t ea = cudaMalloc(&h->djsave, (size_t)slots * reactor_slot_bytes(h->L));
   if (ea != cudaSuccess) { h->djsave = nullptr; return fail(FLINT_ERR_NOMEM, "reactor scratch: %s", cudaGetErrorString(ea)); }
   h->jslots = slots;
   return FLINT_OK;

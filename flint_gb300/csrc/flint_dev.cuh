@@ -184,35 +184,50 @@ struct WarpScratch {
   int ldj;
 };
 
-// Layout: c, hRT, gRT [nsp each], q [nrpad], then either the Jacobian area
-// dq [8][nrpad] + Jr [(nsp+1)^2] or (source terms only) the falloff area [8][32].
-// The falloff pre-pass of a source-term evaluation inside a Jacobian carve
-// uses the dq area (dead between Jacobian evaluations); a Jacobian evaluation
-// uses Jr (written only after the rates of progress are done).
+// Per-warp scratch in two parts.  The small part (shared memory): c, hRT, gRT
+// [nsp each], q [nrpad] and the falloff pre-pass area [8][32].  The Jacobian
+// part: dq [8][nrpad] and the rows Jr [(nsp+1)^2] -- in shared memory for up to
+// 31 species, in a per-warp slot of global memory (L2-resident) for 32-63.
+// The falloff pre-pass of a Jacobian evaluation uses Jr (written only after the
+// rates of progress are done).
+__host__ __device__ inline int scratch_small_doubles(int nsp, int nrpad) {
+  return (3 * nsp + nrpad + 8 * 32 + 1) & ~1;   // keep 16-byte alignment
+}
+__host__ __device__ inline int scratch_jac_doubles(int nsp, int nrpad) {
+  return (8 * nrpad + (nsp + 1) * (nsp + 1) + 1) & ~1;
+}
 __host__ __device__ inline int scratch_doubles(int nsp, int nrpad, bool jac) {
-  int base = 3 * nsp + nrpad + (jac ? 8 * nrpad + (nsp + 1) * (nsp + 1) : 8 * 32);
-  return (base + 1) & ~1;   // keep 16-byte alignment
+  return scratch_small_doubles(nsp, nrpad) + (jac ? scratch_jac_doubles(nsp, nrpad) : 0);
 }
 
-__device__ inline WarpScratch carve(double* p, int nsp, int nrpad, bool jac) {
+__device__ inline WarpScratch carve2(double* small, double* jacbuf, int nsp, int nrpad) {
   WarpScratch s;
-  s.c = p; s.hRT = p + nsp; s.gRT = p + 2 * nsp; s.q = p + 3 * nsp;
-  s.ldj = nsp + 1;
-  if (jac) { s.dq = s.q + nrpad; s.Jr = s.dq + 8 * nrpad; } else { s.dq = nullptr; s.Jr = nullptr; }
+  s.c = small; s.hRT = small + nsp; s.gRT = small + 2 * nsp; s.q = small + 3 * nsp;
   s.fo = s.q + nrpad;
+  s.ldj = nsp + 1;
+  s.dq = jacbuf;
+  s.Jr = jacbuf ? jacbuf + 8 * nrpad : nullptr;
   return s;
+}
+
+// Both parts contiguous in one buffer (shared memory, up to 31 species).
+__device__ inline WarpScratch carve(double* p, int nsp, int nrpad, bool jac) {
+  return carve2(p, jac ? p + scratch_small_doubles(nsp, nrpad) : nullptr, nsp, nrpad);
 }
 
 // Cell-level results held per lane: lane k (< ns) gets species k, the T-row
 // quantities are uniform across the warp.
-struct CellOut {
-  double wmol;    // lane k: molar production (kmol/m^3/s)
-  double cpR;     // lane k: cp_k / R
-  double f;       // lane k < ns: dY_k/dt; lane ns (if < 32): dT/dt
-  double fT;      // dT/dt (uniform)
-  double rho;     // uniform
+// SPL = species per lane: component k = lane + 32 j lives in slot j.
+template <int SPL>
+struct CellOutT {
+  double wmol[SPL];   // component k < ns: molar production (kmol/m^3/s)
+  double cpR[SPL];    // component k < ns: cp_k / R
+  double f[SPL];      // component k < ns: dY_k/dt; k == ns: dT/dt
+  double fT;          // dT/dt (uniform)
+  double rho;         // uniform
   double cp_mass, h_mass;   // uniform: mixture cp [J/kg/K], h [J/kg]
 };
+using CellOut = CellOutT<1>;
 
 // Troe / Lindemann effective forward coefficient with its derivatives.
 struct Falloff { double keff, dlnkeff, dkeff_dM; };
@@ -255,32 +270,41 @@ __device__ inline Falloff falloff_eval(const MechView& m, int r, int type, doubl
   return o;
 }
 
-// Warp-cooperative kinetics of one cell.  Lane k < ns supplies Y_k (others 0).
-// Computes c, thermo, rates of progress, molar production, the RHS of the
-// constant-pressure reactor and (JAC) the Jacobian rows in s.Jr:
+// Warp-cooperative kinetics of one cell.  Component k = lane + 32 j (slot j
+// of SPL) supplies Y_k (0 beyond ns).  Computes c, thermo, rates of progress,
+// molar production, the RHS of the constant-pressure reactor and (JAC) the
+// Jacobian rows in s.Jr:
 //   s.Jr[i*ldj + j] = d f_i / d x_j,  x = (Y_0..Y_{ns-1}, T), f = (dY/dt, dT/dt).
-template <bool JAC>
-__device__ void warp_kinetics(const MechView& m, const WarpScratch& s, int lane, double Yk,
-                              double T, double p, CellOut& out) {
+template <bool JAC, int SPL>
+__device__ void warp_kinetics(const MechView& m, const WarpScratch& s, int lane, const double (&Yk)[SPL],
+                              double T, double p, CellOutT<SPL>& out) {
   const int ns = m.ns, nsp = m.nsp, nrpad = m.nrpad;
   const double lnT = log(T), invT = 1.0 / T;
   const double lnC0 = m.lnpref_rth - lnT;        // ln(p_ref / (R T))
   // mixture molar mass and density
-  double sumYW = warp_sum(lane < ns ? Yk * m.invmw[lane] : 0.0);
+  double yw = 0.0;
+#pragma unroll
+  for (int j = 0; j < SPL; ++j) {
+    const int k = lane + 32 * j;
+    if (k < ns) yw += Yk[j] * m.invmw[k];
+  }
+  double sumYW = warp_sum(yw);
   double rho = p / (m.r_eos * T * sumYW);
   double wbar = 1.0 / sumYW;
-  // species-parallel: concentrations and thermo, species k on lane k
-  // (the warp kernels are used for ns <= 31, so one pass covers all species)
-  double my_cpR = 0.0, my_hRT = 0.0, my_dcpR = 0.0, my_c = 0.0;
-  {
+  // species-parallel: concentrations and thermo, species k = lane + 32 j
+  double my_cpR[SPL], my_hRT[SPL], my_dcpR[SPL], my_c[SPL];
+#pragma unroll
+  for (int j = 0; j < SPL; ++j) {
+    const int k = lane + 32 * j;
     double ck = 0.0, hr = 0.0, gr = 0.0;
-    if (lane < ns) {
-      ck = rho * Yk * m.invmw[lane];
-      SpThermo th = nasa7(m, lane, T, lnT, invT);
+    my_cpR[j] = 0.0; my_hRT[j] = 0.0; my_dcpR[j] = 0.0; my_c[j] = 0.0;
+    if (k < ns) {
+      ck = rho * Yk[j] * m.invmw[k];
+      SpThermo th = nasa7(m, k, T, lnT, invT);
       hr = th.hRT; gr = th.hRT - th.sR;
-      my_cpR = th.cpR; my_hRT = th.hRT; my_dcpR = th.dcpR; my_c = ck;
+      my_cpR[j] = th.cpR; my_hRT[j] = th.hRT; my_dcpR[j] = th.dcpR; my_c[j] = ck;
     }
-    s.c[lane] = ck; s.hRT[lane] = hr; s.gRT[lane] = gr;
+    if (k < nsp) { s.c[k] = ck; s.hRT[k] = hr; s.gRT[k] = gr; }
   }
   __syncwarp();
   const double* tab = m.exptab;
@@ -458,87 +482,116 @@ __device__ void warp_kinetics(const MechView& m, const WarpScratch& s, int lane,
     s.q[r] = q;
   }
   __syncwarp();
-  // species-parallel: production rates (lane k sums its reaction list)
-  double wm = 0.0;
-  if (lane < ns) {
-    for (int e = m.cstart[lane]; e < m.cstart[lane + 1]; ++e) wm += m.lnu[e] * s.q[m.lr[e]];
+  // species-parallel: production rates (each lane sums its species' reaction lists)
+  double wm[SPL];
+  double Ql = 0.0, Dl = 0.0, cpl = 0.0, hl = 0.0;
+#pragma unroll
+  for (int j = 0; j < SPL; ++j) {
+    const int k = lane + 32 * j;
+    wm[j] = 0.0;
+    if (k < ns) {
+      for (int e = m.cstart[k]; e < m.cstart[k + 1]; ++e) wm[j] += m.lnu[e] * s.q[m.lr[e]];
+      Ql += my_hRT[j] * wm[j];
+      Dl += my_c[j] * my_cpR[j];
+      cpl += Yk[j] * my_cpR[j] * m.invmw[k];
+      hl += Yk[j] * my_hRT[j] * m.invmw[k];
+    }
   }
-  double Q = warp_sum(lane < ns ? my_hRT * wm : 0.0);
-  double D = warp_sum(lane < ns ? my_c * my_cpR : 0.0);
-  double fT = -T * Q / D;
-  out.wmol = wm;
-  out.cpR = my_cpR;
+  const double Q = warp_sum(Ql);
+  const double D = warp_sum(Dl);
+  const double fT = -T * Q / D;
   out.rho = rho;
   out.fT = fT;
-  out.f = (lane < ns) ? m.mw[lane] * wm / rho : (lane == ns ? fT : 0.0);
+#pragma unroll
+  for (int j = 0; j < SPL; ++j) {
+    const int k = lane + 32 * j;
+    out.wmol[j] = wm[j];
+    out.cpR[j] = my_cpR[j];
+    out.f[j] = (k < ns) ? m.mw[k] * wm[j] / rho : (k == ns ? fT : 0.0);
+  }
   // mixture cp and h (mass)
-  double cpm = warp_sum(lane < ns ? Yk * my_cpR * m.invmw[lane] : 0.0);
-  double hm = warp_sum(lane < ns ? Yk * my_hRT * m.invmw[lane] : 0.0);
-  out.cp_mass = cpm * m.r_thermo;
-  out.h_mass = hm * m.r_thermo * T;
+  out.cp_mass = warp_sum(cpl) * m.r_thermo;
+  out.h_mass = warp_sum(hl) * m.r_thermo * T;
   if (!JAC) return;
 
-  // ---- Jacobian in concentration space: row k = species k (lane k) -------
+  // ---- Jacobian in concentration space: row k = species k ------------------
   const int ld = s.ldj;
-  double* Jrow = s.Jr + lane * ld;
-  double JT = 0.0;
-  if (lane < ns) {
-    for (int j = 0; j < ns; ++j) Jrow[j] = 0.0;
-    for (int e = m.cstart[lane]; e < m.cstart[lane + 1]; ++e) {
-      const int r = m.lr[e];
-      const double nu = m.lnu[e];
+  double JT[SPL];
 #pragma unroll
-      for (int sl = 0; sl < MAXSIDE; ++sl) {
-        int sp = m.rsp[sl * nrpad + r];
-        if (sp >= 0) Jrow[sp] += nu * s.dq[sl * nrpad + r];
-        int sq = m.psp[sl * nrpad + r];
-        if (sq >= 0) Jrow[sq] += nu * s.dq[(3 + sl) * nrpad + r];
+  for (int j = 0; j < SPL; ++j) {
+    const int k = lane + 32 * j;
+    JT[j] = 0.0;
+    if (k < ns) {
+      double* Jrow = s.Jr + k * ld;
+      for (int jj = 0; jj < ns; ++jj) Jrow[jj] = 0.0;
+      for (int e = m.cstart[k]; e < m.cstart[k + 1]; ++e) {
+        const int r = m.lr[e];
+        const double nu = m.lnu[e];
+#pragma unroll
+        for (int sl = 0; sl < MAXSIDE; ++sl) {
+          int sp = m.rsp[sl * nrpad + r];
+          if (sp >= 0) Jrow[sp] += nu * s.dq[sl * nrpad + r];
+          int sq = m.psp[sl * nrpad + r];
+          if (sq >= 0) Jrow[sq] += nu * s.dq[(3 + sl) * nrpad + r];
+        }
+        const uint32_t w = m.code[r];
+        if (rx_type(w) != 0) {
+          const double t = nu * s.dq[6 * nrpad + r];
+          const double* effrow = m.eff + rx_tbrow(w) * nsp;
+          for (int jj = 0; jj < ns; ++jj) Jrow[jj] += t * effrow[jj];
+        }
+        JT[j] += nu * s.dq[7 * nrpad + r];
       }
-      const uint32_t w = m.code[r];
-      if (rx_type(w) != 0) {
-        const double t = nu * s.dq[6 * nrpad + r];
-        const double* effrow = m.eff + rx_tbrow(w) * nsp;
-        for (int j = 0; j < ns; ++j) Jrow[j] += t * effrow[j];
-      }
-      JT += nu * s.dq[7 * nrpad + r];
     }
   }
   __syncwarp();
   // S_k = sum_j c_j Jc[k][j] (row k); HJ_m = sum_k hRT_k Jc[k][m] (column m)
-  double Sk = 0.0, HJ = 0.0;
-  if (lane < ns) {
-    for (int j = 0; j < ns; ++j) Sk += s.c[j] * Jrow[j];
-    for (int k = 0; k < ns; ++k) HJ += s.hRT[k] * s.Jr[k * ld + lane];
+  double Sk[SPL], HJ[SPL];
+  double HSl = 0.0, dQTl = 0.0, dDTl = 0.0;
+#pragma unroll
+  for (int j = 0; j < SPL; ++j) {
+    const int k = lane + 32 * j;
+    Sk[j] = 0.0; HJ[j] = 0.0;
+    if (k < ns) {
+      const double* Jrow = s.Jr + k * ld;
+      for (int jj = 0; jj < ns; ++jj) Sk[j] += s.c[jj] * Jrow[jj];
+      for (int kk = 0; kk < ns; ++kk) HJ[j] += s.hRT[kk] * s.Jr[kk * ld + k];
+      HSl += my_hRT[j] * Sk[j];
+      dQTl += (my_cpR[j] - my_hRT[j]) * invT * wm[j] + my_hRT[j] * (JT[j] - Sk[j] * invT);
+      dDTl += my_c[j] * (my_dcpR[j] - my_cpR[j] * invT);
+    }
   }
-  double HS = warp_sum(lane < ns ? my_hRT * Sk : 0.0);
+  const double HS = warp_sum(HSl);
   __syncwarp();
   const double wr = wbar / rho;
-  // T row pieces (lane m computes column m of the T row)
-  double dQT_l = 0.0, dDT_l = 0.0;
-  if (lane < ns) {
-    dQT_l = (my_cpR - my_hRT) * invT * wm + my_hRT * (JT - Sk * invT);
-    dDT_l = my_c * (my_dcpR - my_cpR * invT);
-  }
-  double dQT = warp_sum(dQT_l), dDT = warp_sum(dDT_l);
-  double JTT = -Q / D - (T / D) * (dQT - (Q / D) * dDT);
-  double JTm = 0.0;
-  if (lane < ns) {
-    double rw = rho * m.invmw[lane], ww = wbar * m.invmw[lane];
-    double dQ = rw * HJ - ww * HS;
-    double dD = rw * my_cpR - ww * D;
-    JTm = -(T / D) * (dQ - (Q / D) * dD);
-  }
-  // species rows in (Y, T) variables
-  if (lane < ns) {
-    const double tk = Sk - wm;
-    const double Wk = m.mw[lane];
-    for (int j = 0; j < ns; ++j) Jrow[j] = Wk * m.invmw[j] * (Jrow[j] - wr * tk);
-    Jrow[ns] = (Wk / rho) * (JT - tk * invT);
+  const double dQT = warp_sum(dQTl), dDT = warp_sum(dDTl);
+  const double JTT = -Q / D - (T / D) * (dQT - (Q / D) * dDT);
+  double JTm[SPL];
+#pragma unroll
+  for (int j = 0; j < SPL; ++j) {
+    const int k = lane + 32 * j;
+    JTm[j] = 0.0;
+    if (k < ns) {
+      const double rw = rho * m.invmw[k], ww = wbar * m.invmw[k];
+      const double dQ = rw * HJ[j] - ww * HS;
+      const double dD = rw * my_cpR[j] - ww * D;
+      JTm[j] = -(T / D) * (dQ - (Q / D) * dD);
+      // species row k in (Y, T) variables
+      const double tk = Sk[j] - wm[j];
+      const double Wk = m.mw[k];
+      double* Jrow = s.Jr + k * ld;
+      for (int jj = 0; jj < ns; ++jj) Jrow[jj] = Wk * m.invmw[jj] * (Jrow[jj] - wr * tk);
+      Jrow[ns] = (Wk / rho) * (JT[j] - tk * invT);
+    }
   }
   __syncwarp();
   // T row (row ns)
   double* JrowT = s.Jr + ns * ld;
-  if (lane < ns) JrowT[lane] = JTm;
+#pragma unroll
+  for (int j = 0; j < SPL; ++j) {
+    const int k = lane + 32 * j;
+    if (k < ns) JrowT[k] = JTm[j];
+  }
   if (lane == 0) JrowT[ns] = JTT;
   __syncwarp();
 }

@@ -21,11 +21,13 @@ cudaError_t launch_thermo(const uint8_t* img, const ImageLayout& L, int64_t n, i
 cudaError_t launch_chemistry_source(const uint8_t* img, const ImageLayout& L, int64_t n, double* roi,
                                     const double* T, double* omegadot, cudaStream_t st);
 cudaError_t launch_wdot_jac(const uint8_t* img, const ImageLayout& L, int64_t n, int layout, const double* T,
-                            const double* p, const double* Y, double* wdot, double* jac, cudaStream_t st);
+                            const double* p, const double* Y, double* wdot, double* jac, double* gscratch,
+                            cudaStream_t st);
+int64_t warp_jac_scratch_doubles(const ImageLayout& L);
 cudaError_t launch_rhs(const uint8_t* img, const ImageLayout& L, int64_t n, const double* T, const double* p,
                        const double* Y, double* f, cudaStream_t st);
 int reactor_slots(const ImageLayout& L);
-size_t reactor_slot_bytes();
+size_t reactor_slot_bytes(const ImageLayout& L);
 cudaError_t launch_reactor(const uint8_t* img, const ImageLayout& L, int64_t n, double* T, const double* p,
                            double* Y, const double* dt, const flint_reactor_opts& o, int* status, int* nsteps,
                            unsigned int* work_counter, double* jsave, int slots, cudaStream_t st);

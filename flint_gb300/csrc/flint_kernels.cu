@@ -5,7 +5,7 @@
 //                 every thread reads the same reaction word at the same time
 //                 (broadcast), per-thread species arrays live in shared memory
 //                 as [species][thread] (conflict-free).
-//  k_wdot_warp    one warp per cell (ns <= 31): reaction-parallel rates of
+//  k_wdot_warp    one warp per cell (ns <= 63, species k on lane k % 32): reaction-parallel rates of
 //                 progress, species-parallel sums; optional analytic Jacobian
 //                 written coalesced (lane = row, one column per store).
 //  k_rhs_warp     constant-pressure reactor right-hand side.
@@ -138,42 +138,65 @@ k_wdot_small(const uint8_t* __restrict__ img, ImageLayout L, int64_t n, int layo
 }
 
 // ---------------------------------------------------------------- warp
-template <bool JAC>
+template <bool JAC, int SPL>
 __global__ void __launch_bounds__(WARP_THREADS)
 k_wdot_warp(const uint8_t* __restrict__ img, ImageLayout L, int64_t n, int layout,
             const double* __restrict__ Tg, const double* __restrict__ pg,
             const double* __restrict__ Yg, double* __restrict__ wdot, double* __restrict__ cpo,
-            double* __restrict__ ho, double* __restrict__ jac, double* __restrict__ rhs_out) {
+            double* __restrict__ ho, double* __restrict__ jac, double* __restrict__ rhs_out,
+            double* __restrict__ gscratch) {
   extern __shared__ __align__(16) uint8_t smem[];
   stage_image(smem, img, L.bytes);
   MechView m;
   m.bind(L, smem);
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  const int sd = scratch_doubles(m.nsp, m.nrpad, JAC);
-  WarpScratch s = carve(reinterpret_cast<double*>(smem + L.bytes) + wid * sd, m.nsp, m.nrpad, JAC);
+  WarpScratch s;
+  if (SPL == 1) {
+    const int sd = scratch_doubles(m.nsp, m.nrpad, JAC);
+    s = carve(reinterpret_cast<double*>(smem + L.bytes) + wid * sd, m.nsp, m.nrpad, JAC);
+  } else {
+    // 32-63 species: the Jacobian work area is a per-warp slot of global memory
+    const int sd = scratch_small_doubles(m.nsp, m.nrpad);
+    const int64_t gw = (int64_t)blockIdx.x * (blockDim.x >> 5) + wid;
+    s = carve2(reinterpret_cast<double*>(smem + L.bytes) + wid * sd,
+               JAC ? gscratch + gw * scratch_jac_doubles(m.nsp, m.nrpad) : nullptr, m.nsp, m.nrpad);
+  }
   const int ns = m.ns, nv = ns + 1;
   const int64_t nwarps = (int64_t)gridDim.x * (blockDim.x >> 5);
   for (int64_t cell = (int64_t)blockIdx.x * (blockDim.x >> 5) + wid; cell < n; cell += nwarps) {
     const double T = Tg[cell], p = pg[cell];
-    double Yk = 0.0;
-    if (lane < ns) Yk = (layout == 1) ? Yg[(int64_t)lane * n + cell] : Yg[cell * ns + lane];
-    CellOut o;
-    warp_kinetics<JAC>(m, s, lane, Yk, T, p, o);
-    if (wdot && lane < ns) {
-      double v = m.mw[lane] * o.wmol;
-      if (layout == 1) wdot[(int64_t)lane * n + cell] = v;
-      else wdot[cell * ns + lane] = v;
+    double Yk[SPL];
+#pragma unroll
+    for (int j = 0; j < SPL; ++j) {
+      const int k = lane + 32 * j;
+      Yk[j] = 0.0;
+      if (k < ns) Yk[j] = (layout == 1) ? Yg[(int64_t)k * n + cell] : Yg[cell * ns + k];
     }
-    if (rhs_out && lane < nv) rhs_out[cell * nv + lane] = o.f;
+    CellOutT<SPL> o;
+    warp_kinetics<JAC, SPL>(m, s, lane, Yk, T, p, o);
+#pragma unroll
+    for (int j = 0; j < SPL; ++j) {
+      const int k = lane + 32 * j;
+      if (wdot && k < ns) {
+        const double v = m.mw[k] * o.wmol[j];
+        if (layout == 1) wdot[(int64_t)k * n + cell] = v;
+        else wdot[cell * ns + k] = v;
+      }
+      if (rhs_out && k < nv) rhs_out[cell * nv + k] = o.f[j];
+    }
     if (lane == 0) {
       if (cpo) cpo[cell] = o.cp_mass;
       if (ho) ho[cell] = o.h_mass;
     }
     if (JAC && jac) {
-      // Fortran (nv, nv, N): column j of this cell is contiguous; lane = row.
+      // Fortran (nv, nv, N): column c of this cell is contiguous; lanes = rows.
       double* dst = jac + cell * (int64_t)nv * nv;
-      if (lane < nv)
-        for (int j = 0; j < nv; ++j) dst[(int64_t)j * nv + lane] = s.Jr[lane * s.ldj + j];
+#pragma unroll
+      for (int j = 0; j < SPL; ++j) {
+        const int r = lane + 32 * j;
+        if (r < nv)
+          for (int c = 0; c < nv; ++c) dst[(int64_t)c * nv + r] = s.Jr[r * s.ldj + c];
+      }
     }
     __syncwarp();
   }
@@ -290,7 +313,45 @@ static int64_t grid_for(const void* fn, int threads, size_t smem, int64_t work_i
 
 size_t small_smem(const ImageLayout& L) { return L.bytes + 3 * SMALL_NSMAX * SMALL_THREADS * sizeof(double); }
 size_t warp_smem(const ImageLayout& L, bool jac) {
+  if (L.nsp > 32) return L.bytes + (WARP_THREADS / 32) * scratch_small_doubles(L.nsp, L.nrpad) * sizeof(double);
   return L.bytes + (WARP_THREADS / 32) * scratch_doubles(L.nsp, L.nrpad, jac) * sizeof(double);
+}
+
+template <bool JAC>
+static const void* warp_fn(const ImageLayout& L) {
+  return L.nsp > 32 ? (const void*)k_wdot_warp<JAC, 2> : (const void*)k_wdot_warp<JAC, 1>;
+}
+
+// Global Jacobian work area needed by the warp kernels for 32-63 species
+// (doubles), for a grid of full waves.
+int64_t warp_jac_scratch_doubles(const ImageLayout& L) {
+  if (L.nsp <= 32) return 0;
+  size_t sm = warp_smem(L, true);
+  const void* fn = warp_fn<true>(L);
+  cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  int per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, WARP_THREADS, sm);
+  if (per_sm < 1) per_sm = 1;
+  return (int64_t)per_sm * device_sms() * (WARP_THREADS / 32) * scratch_jac_doubles(L.nsp, L.nrpad);
+}
+
+template <bool JAC>
+static cudaError_t launch_warp(const uint8_t* img, const ImageLayout& L, int64_t n, int layout, const double* T,
+                               const double* p, const double* Y, double* wdot, double* cp, double* h, double* jac,
+                               double* rhs, double* gscratch, cudaStream_t st) {
+  size_t sm = warp_smem(L, JAC);
+  const void* fn = warp_fn<JAC>(L);
+  cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  if (e != cudaSuccess) return e;
+  int64_t g = grid_for(fn, WARP_THREADS, sm, n * 32);
+  if (L.nsp > 32)
+    k_wdot_warp<JAC, 2><<<(unsigned)g, WARP_THREADS, sm, st>>>(img, L, n, layout, T, p, Y, wdot, cp, h, jac, rhs,
+                                                                gscratch);
+  else
+    k_wdot_warp<JAC, 1><<<(unsigned)g, WARP_THREADS, sm, st>>>(img, L, n, layout, T, p, Y, wdot, cp, h, jac, rhs,
+                                                                nullptr);
+  count_launch();
+  return cudaGetLastError();
 }
 
 bool use_small_kernel(const ImageLayout& L) { return L.ns <= SMALL_NSMAX && L.ns <= 8; }
@@ -304,15 +365,10 @@ cudaError_t launch_wdot(const uint8_t* img, const ImageLayout& L, int64_t n, int
     cudaFuncSetAttribute(k_wdot_small, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     int64_t g = grid_for((const void*)k_wdot_small, SMALL_THREADS, sm, n);
     k_wdot_small<<<(unsigned)g, SMALL_THREADS, sm, st>>>(img, L, n, layout, T, p, Y, wdot, cp, h, 0, nullptr);
-  } else {
-    size_t sm = warp_smem(L, false);
-    cudaFuncSetAttribute(k_wdot_warp<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    int64_t g = grid_for((const void*)k_wdot_warp<false>, WARP_THREADS, sm, n * 32);
-    k_wdot_warp<false><<<(unsigned)g, WARP_THREADS, sm, st>>>(img, L, n, layout, T, p, Y, wdot, cp, h,
-                                                               nullptr, nullptr);
+    count_launch();
+    return cudaGetLastError();
   }
-  count_launch();
-  return cudaGetLastError();
+  return launch_warp<false>(img, L, n, layout, T, p, Y, wdot, cp, h, nullptr, nullptr, nullptr, st);
 }
 
 cudaError_t launch_thermo(const uint8_t* img, const ImageLayout& L, int64_t n, int layout, const double* T,
@@ -339,27 +395,16 @@ cudaError_t launch_chemistry_source(const uint8_t* img, const ImageLayout& L, in
 }
 
 cudaError_t launch_wdot_jac(const uint8_t* img, const ImageLayout& L, int64_t n, int layout, const double* T,
-                            const double* p, const double* Y, double* wdot, double* jac, cudaStream_t st) {
+                            const double* p, const double* Y, double* wdot, double* jac, double* gscratch,
+                            cudaStream_t st) {
   if (n <= 0) return cudaSuccess;
-  size_t sm = warp_smem(L, true);
-  cudaFuncSetAttribute(k_wdot_warp<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-  int64_t g = grid_for((const void*)k_wdot_warp<true>, WARP_THREADS, sm, n * 32);
-  k_wdot_warp<true><<<(unsigned)g, WARP_THREADS, sm, st>>>(img, L, n, layout, T, p, Y, wdot, nullptr, nullptr,
-                                                            jac, nullptr);
-  count_launch();
-  return cudaGetLastError();
+  return launch_warp<true>(img, L, n, layout, T, p, Y, wdot, nullptr, nullptr, jac, nullptr, gscratch, st);
 }
 
 cudaError_t launch_rhs(const uint8_t* img, const ImageLayout& L, int64_t n, const double* T, const double* p,
                        const double* Y, double* f, cudaStream_t st) {
   if (n <= 0) return cudaSuccess;
-  size_t sm = warp_smem(L, false);
-  cudaFuncSetAttribute(k_wdot_warp<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-  int64_t g = grid_for((const void*)k_wdot_warp<false>, WARP_THREADS, sm, n * 32);
-  k_wdot_warp<false><<<(unsigned)g, WARP_THREADS, sm, st>>>(img, L, n, 0, T, p, Y, nullptr, nullptr, nullptr,
-                                                             nullptr, f);
-  count_launch();
-  return cudaGetLastError();
+  return launch_warp<false>(img, L, n, 0, T, p, Y, nullptr, nullptr, nullptr, nullptr, f, nullptr, st);
 }
 
 }  // namespace flint

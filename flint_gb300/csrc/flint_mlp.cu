@@ -17,6 +17,13 @@
 //
 // Tiles: 64 x 64 per block, 4 warps of 32 x 32, K staged 32 at a time with rows
 // padded to 40 BF16 (80 bytes) so the fragment loads are bank-conflict free.
+//
+// Split mode (the forward pass): every operand x is staged as the BF16 pair
+// hi = bf16(x), lo = bf16(x - hi), and each fragment product is accumulated as
+// lo*hi + hi*lo + hi*hi in FP32.  A single BF16 operand carries 8 significant
+// bits; the pair carries about 16, which moves the network's rounding floor
+// from ~1e-3 to ~1e-5 of its output scale at three times the MMA work (the
+// lo*lo term is below the FP32 accumulation error and is skipped).
 #include <cstdint>
 #include <algorithm>
 #include <cuda_bf16.h>
@@ -42,9 +49,19 @@ __device__ __forceinline__ float ld_any(const void* p, int bf16, int64_t idx) {
   return bf16 ? __bfloat162float(static_cast<const __nv_bfloat16*>(p)[idx]) : static_cast<const float*>(p)[idx];
 }
 
+__device__ __forceinline__ void mma_bf16(float (&c)[4], const uint32_t (&a)[4], const uint32_t (&b)[2]) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 "
+      "{%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};\n"
+      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+template <bool SPLIT>
 __global__ void __launch_bounds__(GTHREADS) k_gemm_bf16(GemmArgs g) {
-  __shared__ __align__(16) __nv_bfloat16 sA[GBM][GKP];
-  __shared__ __align__(16) __nv_bfloat16 sB[GBN][GKP];
+  constexpr int NP = SPLIT ? 2 : 1;   // hi (and lo) planes
+  __shared__ __align__(16) __nv_bfloat16 sA[NP][GBM][GKP];
+  __shared__ __align__(16) __nv_bfloat16 sB[NP][GBN][GKP];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int wm = (warp >> 1) * 32, wn = (warp & 1) * 32;
   const int m0 = blockIdx.y * GBM, n0 = blockIdx.x * GBN;
@@ -64,42 +81,50 @@ __global__ void __launch_bounds__(GTHREADS) k_gemm_bf16(GemmArgs g) {
       const int m = m0 + r, k = k0 + c;
       float v = 0.f;
       if (m < g.M && k < g.K) v = ld_any(g.A, g.a_bf16, (int64_t)m * g.sa_m + (int64_t)k * g.sa_k);
-      sA[r][c] = __float2bfloat16_rn(v);
+      const __nv_bfloat16 hi = __float2bfloat16_rn(v);
+      sA[0][r][c] = hi;
+      if (SPLIT) sA[NP - 1][r][c] = __float2bfloat16_rn(v - __bfloat162float(hi));
     }
     for (int e = tid; e < GBN * GBK; e += GTHREADS) {
       const int r = e / GBK, c = e % GBK;
       const int n = n0 + r, k = k0 + c;
       float v = 0.f;
       if (n < g.N && k < g.K) v = ld_any(g.B, g.b_bf16, (int64_t)k * g.sb_k + (int64_t)n * g.sb_n);
-      sB[r][c] = __float2bfloat16_rn(v);
+      const __nv_bfloat16 hi = __float2bfloat16_rn(v);
+      sB[0][r][c] = hi;
+      if (SPLIT) sB[NP - 1][r][c] = __float2bfloat16_rn(v - __bfloat162float(hi));
     }
     __syncthreads();
 #pragma unroll
     for (int kk = 0; kk < GBK; kk += 16) {
-      uint32_t af[2][4], bfr[4][2];
+      uint32_t af[NP][2][4], bfr[NP][4][2];
 #pragma unroll
-      for (int i = 0; i < 2; ++i) {
-        const int r = wm + i * 16 + grp;
-        af[i][0] = *reinterpret_cast<const uint32_t*>(&sA[r][kk + tig * 2]);
-        af[i][1] = *reinterpret_cast<const uint32_t*>(&sA[r + 8][kk + tig * 2]);
-        af[i][2] = *reinterpret_cast<const uint32_t*>(&sA[r][kk + tig * 2 + 8]);
-        af[i][3] = *reinterpret_cast<const uint32_t*>(&sA[r + 8][kk + tig * 2 + 8]);
-      }
+      for (int pl = 0; pl < NP; ++pl) {
 #pragma unroll
-      for (int j = 0; j < 4; ++j) {
-        const int n = wn + j * 8 + grp;
-        bfr[j][0] = *reinterpret_cast<const uint32_t*>(&sB[n][kk + tig * 2]);
-        bfr[j][1] = *reinterpret_cast<const uint32_t*>(&sB[n][kk + tig * 2 + 8]);
+        for (int i = 0; i < 2; ++i) {
+          const int r = wm + i * 16 + grp;
+          af[pl][i][0] = *reinterpret_cast<const uint32_t*>(&sA[pl][r][kk + tig * 2]);
+          af[pl][i][1] = *reinterpret_cast<const uint32_t*>(&sA[pl][r + 8][kk + tig * 2]);
+          af[pl][i][2] = *reinterpret_cast<const uint32_t*>(&sA[pl][r][kk + tig * 2 + 8]);
+          af[pl][i][3] = *reinterpret_cast<const uint32_t*>(&sA[pl][r + 8][kk + tig * 2 + 8]);
+        }
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          const int n = wn + j * 8 + grp;
+          bfr[pl][j][0] = *reinterpret_cast<const uint32_t*>(&sB[pl][n][kk + tig * 2]);
+          bfr[pl][j][1] = *reinterpret_cast<const uint32_t*>(&sB[pl][n][kk + tig * 2 + 8]);
+        }
       }
 #pragma unroll
       for (int i = 0; i < 2; ++i)
 #pragma unroll
-        for (int j = 0; j < 4; ++j)
-          asm volatile(
-              "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 "
-              "{%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};\n"
-              : "+f"(acc[i][j][0]), "+f"(acc[i][j][1]), "+f"(acc[i][j][2]), "+f"(acc[i][j][3])
-              : "r"(af[i][0]), "r"(af[i][1]), "r"(af[i][2]), "r"(af[i][3]), "r"(bfr[j][0]), "r"(bfr[j][1]));
+        for (int j = 0; j < 4; ++j) {
+          if (SPLIT) {
+            mma_bf16(acc[i][j], af[NP - 1][i], bfr[0][j]);
+            mma_bf16(acc[i][j], af[0][i], bfr[NP - 1][j]);
+          }
+          mma_bf16(acc[i][j], af[0][i], bfr[0][j]);
+        }
     }
     __syncthreads();
   }
@@ -120,7 +145,11 @@ __global__ void __launch_bounds__(GTHREADS) k_gemm_bf16(GemmArgs g) {
           float* cp = g.C + (int64_t)m * g.ldc + n;
           *cp = g.accumulate ? *cp + v : v;
         }
-        if (g.Cb) g.Cb[(int64_t)m * g.ldcb + n] = __float2bfloat16_rn(g.epi == EPI_BIAS_GELU ? gelu_f(v) : v);
+        if (g.Cb || g.Cf) {
+          const float a = g.epi == EPI_BIAS_GELU ? gelu_f(v) : v;
+          if (g.Cb) g.Cb[(int64_t)m * g.ldcb + n] = __float2bfloat16_rn(a);
+          if (g.Cf) g.Cf[(int64_t)m * g.ldcf + n] = a;
+        }
       }
 }
 
@@ -171,7 +200,8 @@ __global__ void k_f32_to_bf16(const float* __restrict__ x, __nv_bfloat16* __rest
 cudaError_t launch_gemm(const GemmArgs& g, cudaStream_t st) {
   if (g.M <= 0 || g.N <= 0) return cudaSuccess;
   dim3 grid((g.N + GBN - 1) / GBN, (g.M + GBM - 1) / GBM);
-  k_gemm_bf16<<<grid, GTHREADS, 0, st>>>(g);
+  if (g.split) k_gemm_bf16<true><<<grid, GTHREADS, 0, st>>>(g);
+  else k_gemm_bf16<false><<<grid, GTHREADS, 0, st>>>(g);
   count_launch();
   return cudaGetLastError();
 }

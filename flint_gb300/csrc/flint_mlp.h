@@ -16,9 +16,11 @@ struct GemmArgs {
   const float* bias;                 // [N]
   float* C; int64_t ldc;             // FP32 output (pre-activation or result)
   __nv_bfloat16* Cb; int64_t ldcb;   // optional BF16 activation output
+  float* Cf; int64_t ldcf;           // optional FP32 activation output (GELU applied for EPI_BIAS_GELU)
   const float* Zprev; int64_t ldz;   // GELU_BWD: pre-activation of the previous layer
   int epi;
   int accumulate;                    // C += result
+  int split;                         // operands as BF16 hi + lo pairs, three MMAs per fragment
 };
 
 cudaError_t launch_gemm(const GemmArgs& g, cudaStream_t st);

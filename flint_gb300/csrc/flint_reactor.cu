@@ -18,7 +18,9 @@
 // Nordsieck BDF of order 1-5, modified Newton with a Jacobian/LU refresh when
 // gamma moves by more than 30 %, every 20 steps or after a convergence
 // failure with a stale matrix; step and order chosen every q+1 steps from the
-// order q-1, q, q+1 error estimates.  The Newton matrix I - gamma*J is factored
+// order q-1, q, q+1 error estimates; Newton converged in the weighted max norm;
+// after an error-test failure with a stale Jacobian, a fresh one.  A cell whose
+// integration fails is integrated again at order <= 2, then 1.  The Newton matrix I - gamma*J is factored
 // in shared memory by a row-per-lane LU with partial pivoting that records the
 // pivot order instead of swapping rows.  Step-size factors eta = (c*dsm)^(-1/(q+1))
 // are heuristics and are evaluated in FP32 (the oracle does the same); every
@@ -62,60 +64,117 @@ constexpr int NCOUNTERS = 7;
 constexpr double DGMAX = 0.3;
 constexpr int MSBP = 20;
 constexpr int MSBJ = 50;
-constexpr int JSLOT = 32 * 32;   // doubles per saved-Jacobian slot
+constexpr int JSLOT = 32 * 32;   // doubles per saved-Jacobian slot of up to 31 species
 
-__device__ inline double wrms(double v, double w, bool act, int nv) {
-  double t = act ? v * w : 0.0;
-  return sqrt(warp_sum(t * t) / nv);
+// Component k = lane + 32 j of the state lives in slot j (SPL slots per lane).
+template <int SPL>
+__device__ inline double wrms(const double (&v)[SPL], const double (&w)[SPL], int lane, int nv) {
+  double t = 0.0;
+#pragma unroll
+  for (int j = 0; j < SPL; ++j) {
+    const double a = (lane + 32 * j < nv) ? v[j] * w[j] : 0.0;
+    t += a * a;
+  }
+  return sqrt(warp_sum(t) / nv);
 }
 
-// LU of the rows held in smem (row i on lane i), pivot order in piv[step] = row.
-__device__ inline void warp_lu(double* A, int ld, int nv, int lane, int* piv, int& mystep) {
-  const bool act = lane < nv;
-  mystep = act ? -1 : 1 << 20;
+// Weighted max norm (the Newton convergence test); fmax is exact, so the
+// butterfly leaves the same value on every lane.
+template <int SPL>
+__device__ inline double wmax(const double (&v)[SPL], const double (&w)[SPL], int lane, int nv) {
+  double t = 0.0;
+#pragma unroll
+  for (int j = 0; j < SPL; ++j)
+    if (lane + 32 * j < nv) t = fmax(t, fabs(v[j] * w[j]));
+  return warp_max(t);
+}
+
+// LU of the rows (row r = lane + 32 j) held at A[r*ld ...], partial pivoting by
+// the largest |a| (lowest row on ties); the pivot order goes to piv[step] and
+// each row remembers its step in mystep (rows are not swapped).
+template <int SPL>
+__device__ inline void warp_lu(double* A, int ld, int nv, int lane, int* piv, int (&mystep)[SPL]) {
+#pragma unroll
+  for (int j = 0; j < SPL; ++j) mystep[j] = (lane + 32 * j < nv) ? -1 : 1 << 20;
   for (int k = 0; k < nv; ++k) {
-    double cand = (act && mystep < 0) ? fabs(A[lane * ld + k]) : -1.0;
+    double cand = -1.0;
     int who = lane;
+#pragma unroll
+    for (int j = 0; j < SPL; ++j) {
+      const int r = lane + 32 * j;
+      if (r < nv && mystep[j] < 0) {
+        const double v = fabs(A[r * ld + k]);
+        if (v > cand) { cand = v; who = r; }
+      }
+    }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
       double oc = __shfl_xor_sync(FULL, cand, o);
       int ow = __shfl_xor_sync(FULL, who, o);
       if (oc > cand || (oc == cand && ow < who)) { cand = oc; who = ow; }
     }
-    if (lane == who) mystep = k;
+#pragma unroll
+    for (int j = 0; j < SPL; ++j)
+      if (lane + 32 * j == who) mystep[j] = k;
     if (lane == 0) piv[k] = who;
     const double* prow = A + who * ld;
     const double inv = 1.0 / prow[k];
-    if (act && mystep < 0) {
-      double* row = A + lane * ld;
-      const double l = row[k] * inv;
-      row[k] = l;
-      for (int j = k + 1; j < nv; ++j) row[j] -= l * prow[j];
+#pragma unroll
+    for (int j = 0; j < SPL; ++j) {
+      const int r = lane + 32 * j;
+      if (r < nv && mystep[j] < 0) {
+        double* row = A + r * ld;
+        const double l = row[k] * inv;
+        row[k] = l;
+        for (int c = k + 1; c < nv; ++c) row[c] -= l * prow[c];
+      }
     }
     __syncwarp();
   }
 }
 
-// Solve (LU) x = b; b on lane i in, x on lane i out.
-__device__ inline double warp_lu_solve(const double* A, int ld, int nv, int lane, const int* piv, int mystep,
-                                       double b) {
+// Solve (LU) x = b; component r = lane + 32 j of b in slot j in, x out.
+template <int SPL>
+__device__ inline void warp_lu_solve(const double* A, int ld, int nv, int lane, const int* piv,
+                                     const int (&mystep)[SPL], double (&b)[SPL]) {
   // forward: y_k = b_{piv[k]}; rows pivoted later subtract L * y_k
   for (int k = 0; k < nv; ++k) {
     const int pk = piv[k];
-    const double yk = __shfl_sync(FULL, b, pk);
-    if (lane < nv && mystep > k) b -= A[lane * ld + k] * yk;
+    const double src = (SPL == 1 || (pk >> 5) == 0) ? b[0] : b[SPL - 1];
+    const double yk = __shfl_sync(FULL, src, pk & 31);
+#pragma unroll
+    for (int j = 0; j < SPL; ++j) {
+      const int r = lane + 32 * j;
+      if (r < nv && mystep[j] > k) b[j] -= A[r * ld + k] * yk;
+    }
   }
-  // backward by columns: x_j = b_{piv[j]} / U_{piv[j], j}
-  double x = 0.0;
-  for (int j = nv - 1; j >= 0; --j) {
-    const int pj = piv[j];
-    double xj = __shfl_sync(FULL, b, pj) / A[pj * ld + j];
-    if (lane < nv && mystep < j) b -= A[lane * ld + j] * xj;
-    if (lane == j) x = xj;
+  // backward by columns: x_c = b_{piv[c]} / U_{piv[c], c}
+  double x[SPL];
+#pragma unroll
+  for (int j = 0; j < SPL; ++j) x[j] = 0.0;
+  for (int c = nv - 1; c >= 0; --c) {
+    const int pc = piv[c];
+    const double src = (SPL == 1 || (pc >> 5) == 0) ? b[0] : b[SPL - 1];
+    const double xc = __shfl_sync(FULL, src, pc & 31) / A[pc * ld + c];
+#pragma unroll
+    for (int j = 0; j < SPL; ++j) {
+      const int r = lane + 32 * j;
+      if (r < nv && mystep[j] < c) b[j] -= A[r * ld + c] * xc;
+      if (r == c) x[j] = xc;
+    }
   }
-  return x;
+#pragma unroll
+  for (int j = 0; j < SPL; ++j) b[j] = x[j];
 }
 
+// Doubles per resident-warp slot of the reactor's global scratch: the saved
+// Jacobian (32*SPL)^2, and for SPL = 2 the Jacobian work area too.
+__host__ __device__ inline int64_t reactor_slot_doubles_of(const ImageLayout& L) {
+  const int spl = L.nsp / 32;
+  return (int64_t)(32 * spl) * (32 * spl) + (spl > 1 ? scratch_jac_doubles(L.nsp, L.nrpad) : 0);
+}
+
+template <int SPL>
 __global__ void __launch_bounds__(REACTOR_THREADS)
 k_reactor(const uint8_t* __restrict__ img, ImageLayout L, int64_t n, double* __restrict__ Tg,
           const double* __restrict__ pg, double* __restrict__ Yg, const double* __restrict__ dtg,
@@ -126,17 +185,26 @@ k_reactor(const uint8_t* __restrict__ img, ImageLayout L, int64_t n, double* __r
   MechView m;
   m.bind(L, smem);
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  const int sd = scratch_doubles(m.nsp, m.nrpad, true);
-  double* wbase = reinterpret_cast<double*>(smem + L.bytes) + wid * sd;
-  WarpScratch s = carve(wbase, m.nsp, m.nrpad, true);
-  int* pivs = reinterpret_cast<int*>(reinterpret_cast<double*>(smem + L.bytes) + (blockDim.x >> 5) * sd) + wid * 32;
+  const int64_t slot = (int64_t)blockIdx.x * (blockDim.x >> 5) + wid;
+  double* Jg = jsave + slot * reactor_slot_doubles_of(L);
+  constexpr int JW = 32 * SPL;   // row stride of the saved Jacobian
+  WarpScratch s;
+  int* pivs;
+  if (SPL == 1) {
+    const int sd = scratch_doubles(m.nsp, m.nrpad, true);
+    double* wbase = reinterpret_cast<double*>(smem + L.bytes) + wid * sd;
+    s = carve(wbase, m.nsp, m.nrpad, true);
+    pivs = reinterpret_cast<int*>(reinterpret_cast<double*>(smem + L.bytes) + (blockDim.x >> 5) * sd) + wid * 32;
+  } else {
+    const int sd = scratch_small_doubles(m.nsp, m.nrpad);
+    double* wbase = reinterpret_cast<double*>(smem + L.bytes) + wid * sd;
+    s = carve2(wbase, Jg + JW * JW, m.nsp, m.nrpad);
+    pivs = reinterpret_cast<int*>(reinterpret_cast<double*>(smem + L.bytes) + (blockDim.x >> 5) * sd) + wid * 64;
+  }
   const int ns = m.ns, nv = ns + 1;
-  const bool act = lane < nv;
   const int ld = s.ldj;
   const BdfL& B = c_bdf;
-  const int qmax = o.max_order;
   unsigned long long n_rhs = 0, n_jac = 0, n_newt = 0, n_rej = 0, n_lu = 0;
-  double* Jg = jsave + (size_t)(blockIdx.x * (blockDim.x >> 5) + wid) * JSLOT;
 
   while (true) {
     unsigned long long c0 = 0;
@@ -145,40 +213,70 @@ k_reactor(const uint8_t* __restrict__ img, ImageLayout L, int64_t n, double* __r
     if (cell >= n) break;
 
     const double p = pg[cell], tout = dtg[cell];
-    double y = 0.0;
-    if (lane < ns) y = Yg[cell * ns + lane];
-    else if (lane == ns) y = Tg[cell];
+    double y[SPL];
+    int bad = 0;
+#pragma unroll
+    for (int j = 0; j < SPL; ++j) {
+      const int k = lane + 32 * j;
+      y[j] = 0.0;
+      if (k < ns) y[j] = Yg[cell * ns + k];
+      else if (k == ns) y[j] = Tg[cell];
+      if (k < nv && !isfinite(y[j])) bad = 1;
+    }
     const double T0 = Tg[cell];
-    int bad = !(isfinite(T0) && isfinite(p) && p > 0.0 && isfinite(tout) && tout >= 0.0);
-    bad |= (act && !isfinite(y)) ? 1 : 0;
+    bad |= !(isfinite(T0) && isfinite(p) && p > 0.0 && isfinite(tout) && tout >= 0.0);
     bad = __any_sync(FULL, bad);
     int status = FLINT_CELL_OK, nst = 0;
     if (bad) status = FLINT_CELL_NAN_INPUT;
     else if (T0 < o.tmin || T0 > o.tmax) status = FLINT_CELL_T_OUT_OF_RANGE;
 
     if (status == FLINT_CELL_OK && tout > 0.0) {
-      double z[6], zs[6], e = 0.0, eprev = 0.0, ewt, f;
+      double z[6][SPL], zs[6][SPL], e[SPL], eprev[SPL], ewt[SPL], f[SPL];
+      int nst_total = 0;
+      // attempt 0 with the caller's options; a cell that fails the error test
+      // or Newton is integrated again from its initial state at order <= 2
+      // with atol / 100 (BDF1-2 are A-stable, orders 3-5 are not), then at
+      // order 1.  nsteps counts the steps of every attempt.
+      for (int att = 0; att < 3; ++att) {
+      const int qmax = att == 0 ? o.max_order : (att == 1 ? min(o.max_order, 2) : 1);
+      const double atol = att == 1 ? o.atol * 1e-2 : o.atol;
+      status = FLINT_CELL_OK;
+      nst = 0;
 #pragma unroll
-      for (int j = 0; j < 6; ++j) { z[j] = 0.0; zs[j] = 0.0; }
-      CellOut co;
-      auto rhs = [&](double yv) -> double {
+      for (int jj = 0; jj < 6; ++jj)
+#pragma unroll
+        for (int j = 0; j < SPL; ++j) { z[jj][j] = 0.0; zs[jj][j] = 0.0; }
+#pragma unroll
+      for (int j = 0; j < SPL; ++j) { e[j] = 0.0; eprev[j] = 0.0; }
+      CellOutT<SPL> co;
+      const int Tslot = ns >> 5, Tlane = ns & 31;
+      auto rhs = [&](const double (&yv)[SPL], double (&fo)[SPL]) {
         ++n_rhs;
-        const double Tv = __shfl_sync(FULL, yv, ns);
-        warp_kinetics<false>(m, s, lane, lane < ns ? yv : 0.0, Tv, p, co);
+        const double Tv = __shfl_sync(FULL, (SPL == 1 || Tslot == 0) ? yv[0] : yv[SPL - 1], Tlane);
+        double yk[SPL];
+#pragma unroll
+        for (int j = 0; j < SPL; ++j) yk[j] = (lane + 32 * j < ns) ? yv[j] : 0.0;
+        warp_kinetics<false, SPL>(m, s, lane, yk, Tv, p, co);
         __syncwarp();
-        return co.f;
+#pragma unroll
+        for (int j = 0; j < SPL; ++j) fo[j] = co.f[j];
       };
-      z[0] = y;
-      f = rhs(y);
-      ewt = act ? 1.0 / (o.rtol * fabs(y) + o.atol) : 0.0;
-      const double fn = wrms(f, ewt, act, nv);
+#pragma unroll
+      for (int j = 0; j < SPL; ++j) z[0][j] = y[j];
+      rhs(y, f);
+#pragma unroll
+      for (int j = 0; j < SPL; ++j) ewt[j] = (lane + 32 * j < nv) ? 1.0 / (o.rtol * fabs(y[j]) + atol) : 0.0;
+      const double fn = wrms<SPL>(f, ewt, lane, nv);
       double h = (fn * tout > 1.0) ? 1.0 / fn : tout;
-      z[1] = h * f;
+#pragma unroll
+      for (int j = 0; j < SPL; ++j) z[1][j] = h * f[j];
       int q = 1;
       double t = 0.0;
       int ialth = 2, have_J = 0, jfresh = 0, nstJ = 0, nstP = 0, have_eprev = 0, last = 0;
       double gammaJ = 0.0, crate = 1.0, etamax = 1.0e4;
-      int mystep = 0;
+      int mystep[SPL];
+#pragma unroll
+      for (int j = 0; j < SPL; ++j) mystep[j] = 0;
 
       while (t < tout) {
         if (nst >= o.max_steps) { status = FLINT_CELL_MAX_STEPS; break; }
@@ -187,60 +285,98 @@ k_reactor(const uint8_t* __restrict__ img, ImageLayout L, int64_t n, double* __r
           const double eta = (tout - t) / h;
           double r = 1.0;
 #pragma unroll
-          for (int j = 1; j <= 5; ++j) if (j <= q) { r *= eta; z[j] *= r; }
+          for (int jj = 1; jj <= 5; ++jj) if (jj <= q) { r *= eta; for (int j = 0; j < SPL; ++j) z[jj][j] *= r; }
           h = tout - t;
           ialth = q + 1; have_eprev = 0; last = 1;
         }
-        ewt = act ? 1.0 / (o.rtol * fabs(z[0]) + o.atol) : 0.0;
+#pragma unroll
+        for (int j = 0; j < SPL; ++j) ewt[j] = (lane + 32 * j < nv) ? 1.0 / (o.rtol * fabs(z[0][j]) + atol) : 0.0;
         int ncf = 0, nef = 0, need_J = 0, accepted = 0;
         double dsm = 0.0;
+        // the first Newton iterate of a step is judged with a rate of at least
+        // 0.3: a small rate carried over from the last step would accept it unchecked
+        if (crate < 0.3) crate = 0.3;
         while (!accepted) {
           if (h < 1e-300 || t + h == t) { status = FLINT_CELL_ERRTEST_FAIL; break; }
 #pragma unroll
-          for (int j = 0; j < 6; ++j) zs[j] = z[j];
+          for (int jj = 0; jj < 6; ++jj)
+#pragma unroll
+            for (int j = 0; j < SPL; ++j) zs[jj][j] = z[jj][j];
           // predict: z <- z * Pascal
 #pragma unroll
           for (int k = 0; k < 5; ++k)
 #pragma unroll
-            for (int j = 4; j >= 0; --j)
-              if (k < q && j >= k && j <= q - 1) z[j] += z[j + 1];
+            for (int jj = 4; jj >= 0; --jj)
+              if (k < q && jj >= k && jj <= q - 1)
+#pragma unroll
+                for (int j = 0; j < SPL; ++j) z[jj][j] += z[jj + 1][j];
           const double l1 = B.l[q][1];
           const double gamma = h / l1;
-          const double ypred = z[0];
+          double ypred[SPL];
+#pragma unroll
+          for (int j = 0; j < SPL; ++j) ypred[j] = z[0][j];
           if (!have_J || need_J || fabs(gamma / gammaJ - 1.0) > DGMAX || nst >= nstP + MSBP) {
-            double* row = s.Jr + lane * ld;
             if (!have_J || need_J || nst >= nstJ + MSBJ) {
-              const double Tv = __shfl_sync(FULL, ypred, ns);
+              const double Tv = __shfl_sync(FULL, (SPL == 1 || Tslot == 0) ? ypred[0] : ypred[SPL - 1], Tlane);
               ++n_jac;
-              warp_kinetics<true>(m, s, lane, lane < ns ? ypred : 0.0, Tv, p, co);
-              if (act)
-                for (int j = 0; j < nv; ++j) Jg[j * 32 + lane] = row[j];
+              double yk[SPL];
+#pragma unroll
+              for (int j = 0; j < SPL; ++j) yk[j] = (lane + 32 * j < ns) ? ypred[j] : 0.0;
+              warp_kinetics<true, SPL>(m, s, lane, yk, Tv, p, co);
+#pragma unroll
+              for (int j = 0; j < SPL; ++j) {
+                const int r = lane + 32 * j;
+                if (r < nv) {
+                  const double* row = s.Jr + r * ld;
+                  for (int c = 0; c < nv; ++c) Jg[c * JW + r] = row[c];
+                }
+              }
               have_J = 1; jfresh = 1; nstJ = nst; need_J = 0;
-            } else if (act) {
-              for (int j = 0; j < nv; ++j) row[j] = Jg[j * 32 + lane];
+            } else {
+#pragma unroll
+              for (int j = 0; j < SPL; ++j) {
+                const int r = lane + 32 * j;
+                if (r < nv) {
+                  double* row = s.Jr + r * ld;
+                  for (int c = 0; c < nv; ++c) row[c] = Jg[c * JW + r];
+                }
+              }
             }
-            if (act)
-              for (int j = 0; j < nv; ++j) row[j] = (j == lane ? 1.0 : 0.0) - gamma * row[j];
+#pragma unroll
+            for (int j = 0; j < SPL; ++j) {
+              const int r = lane + 32 * j;
+              if (r < nv) {
+                double* row = s.Jr + r * ld;
+                for (int c = 0; c < nv; ++c) row[c] = (c == r ? 1.0 : 0.0) - gamma * row[c];
+              }
+            }
             __syncwarp();
             ++n_lu;
-            warp_lu(s.Jr, ld, nv, lane, pivs, mystep);
+            warp_lu<SPL>(s.Jr, ld, nv, lane, pivs, mystep);
             gammaJ = gamma; nstP = nst; crate = 1.0;
           }
           const double gamrat = gamma / gammaJ;
-          e = 0.0;
-          double yv = ypred;
+          double yv[SPL];
+#pragma unroll
+          for (int j = 0; j < SPL; ++j) { e[j] = 0.0; yv[j] = ypred[j]; }
           int conv = 0;
           double delp = 0.0;
           const double Eq = 1.0 / ((double)(q + 1) * l1 + 1.0);
           for (int mi = 0; mi < 3; ++mi) {
             ++n_newt;
-            f = rhs(yv);
-            double bv = act ? gamma * f - z[1] / l1 - e : 0.0;
-            bv = warp_lu_solve(s.Jr, ld, nv, lane, pivs, mystep, bv);
-            if (gamrat != 1.0) bv *= 2.0 / (1.0 + gamrat);
-            const double del = wrms(bv, ewt, act, nv);
-            e += bv;
-            yv = ypred + e;
+            rhs(yv, f);
+            double bv[SPL];
+#pragma unroll
+            for (int j = 0; j < SPL; ++j) bv[j] = (lane + 32 * j < nv) ? gamma * f[j] - z[1][j] / l1 - e[j] : 0.0;
+            warp_lu_solve<SPL>(s.Jr, ld, nv, lane, pivs, mystep, bv);
+            if (gamrat != 1.0) {
+              const double sc = 2.0 / (1.0 + gamrat);
+#pragma unroll
+              for (int j = 0; j < SPL; ++j) bv[j] *= sc;
+            }
+            const double del = wmax<SPL>(bv, ewt, lane, nv);
+#pragma unroll
+            for (int j = 0; j < SPL; ++j) { e[j] += bv[j]; yv[j] = ypred[j] + e[j]; }
             if (mi > 0) { const double r = del / delp; crate = (0.3 * crate > r) ? 0.3 * crate : r; }
             const double dcon = del * (crate < 1.0 ? crate : 1.0) * Eq / 0.1;
             if (dcon <= 1.0) { conv = 1; break; }
@@ -249,7 +385,9 @@ k_reactor(const uint8_t* __restrict__ img, ImageLayout L, int64_t n, double* __r
           }
           if (!conv) {
 #pragma unroll
-            for (int j = 0; j < 6; ++j) z[j] = zs[j];
+            for (int jj = 0; jj < 6; ++jj)
+#pragma unroll
+              for (int j = 0; j < SPL; ++j) z[jj][j] = zs[jj][j];
             ++ncf;
             ++n_rej;
             if (ncf >= 10) { status = FLINT_CELL_NEWTON_FAIL; break; }
@@ -257,14 +395,16 @@ k_reactor(const uint8_t* __restrict__ img, ImageLayout L, int64_t n, double* __r
             const double eta = 0.25;
             double r = 1.0;
 #pragma unroll
-            for (int j = 1; j <= 5; ++j) if (j <= q) { r *= eta; z[j] *= r; }
+            for (int jj = 1; jj <= 5; ++jj) if (jj <= q) { r *= eta; for (int j = 0; j < SPL; ++j) z[jj][j] *= r; }
             h *= eta; ialth = q + 1; have_eprev = 0; need_J = 1; last = 0;
             continue;
           }
-          dsm = Eq * wrms(e, ewt, act, nv);
+          dsm = Eq * wrms<SPL>(e, ewt, lane, nv);
           if (!(dsm <= 1.0)) {
 #pragma unroll
-            for (int j = 0; j < 6; ++j) z[j] = zs[j];
+            for (int jj = 0; jj < 6; ++jj)
+#pragma unroll
+              for (int j = 0; j < SPL; ++j) z[jj][j] = zs[jj][j];
             ++nef;
             ++n_rej;
             if (nef >= 7) { status = FLINT_CELL_ERRTEST_FAIL; break; }
@@ -279,8 +419,9 @@ k_reactor(const uint8_t* __restrict__ img, ImageLayout L, int64_t n, double* __r
             }
             double r = 1.0;
 #pragma unroll
-            for (int j = 1; j <= 5; ++j) if (j <= q) { r *= eta; z[j] *= r; }
+            for (int jj = 1; jj <= 5; ++jj) if (jj <= q) { r *= eta; for (int j = 0; j < SPL; ++j) z[jj][j] *= r; }
             h *= eta; ialth = q + 1; have_eprev = 0; last = 0;
+            if (!jfresh) need_J = 1;   // retry with a Jacobian of this state
             continue;
           }
           accepted = 1;
@@ -290,7 +431,7 @@ k_reactor(const uint8_t* __restrict__ img, ImageLayout L, int64_t n, double* __r
         ++nst;
         jfresh = 0;
 #pragma unroll
-        for (int j = 0; j <= 5; ++j) if (j <= q) z[j] += B.l[q][j] * e;
+        for (int jj = 0; jj <= 5; ++jj) if (jj <= q) for (int j = 0; j < SPL; ++j) z[jj][j] += B.l[q][jj] * e[j];
         if (last || t >= tout) { t = tout; break; }
         --ialth;
         double eta = 1.0;
@@ -301,15 +442,22 @@ k_reactor(const uint8_t* __restrict__ img, ImageLayout L, int64_t n, double* __r
           if (q > 1) {
             double fact = 1.0;
             for (int i = 2; i <= q; ++i) fact *= i;
-            double zq = 0.0;
+            double zq[SPL];
 #pragma unroll
-            for (int j = 2; j <= 5; ++j) if (j == q) zq = z[j];
-            const double ddn = wrms(zq, ewt, act, nv) * fact / ((double)q * B.l[q - 1][1]);
+            for (int j = 0; j < SPL; ++j) {
+              zq[j] = 0.0;
+#pragma unroll
+              for (int jj = 2; jj <= 5; ++jj) if (jj == q) zq[j] = z[jj][j];
+            }
+            const double ddn = wrms<SPL>(zq, ewt, lane, nv) * fact / ((double)q * B.l[q - 1][1]);
             etadn = 1.0 / ((double)powf((float)(1.3 * ddn), 1.0f / (float)q) + 1.3e-6);
           }
           if (q < qmax && have_eprev) {
             const double Kq = 1.0 + 1.0 / ((double)(q + 1) * l1);
-            const double dup = wrms(e - eprev, ewt, act, nv) / (Kq * (double)(q + 2) * B.l[q + 1][1]);
+            double de[SPL];
+#pragma unroll
+            for (int j = 0; j < SPL; ++j) de[j] = e[j] - eprev[j];
+            const double dup = wrms<SPL>(de, ewt, lane, nv) / (Kq * (double)(q + 2) * B.l[q + 1][1]);
             etaup = 1.0 / ((double)powf((float)(1.4 * dup), 1.0f / (float)(q + 2)) + 1.4e-6);
           }
           int newq = q;
@@ -319,7 +467,7 @@ k_reactor(const uint8_t* __restrict__ img, ImageLayout L, int64_t n, double* __r
           if (newq == q + 1) {
             const double fct = B.l[q][q] / (double)(q + 1);
 #pragma unroll
-            for (int j = 2; j <= 5; ++j) if (j == q + 1) z[j] = e * fct;
+            for (int jj = 2; jj <= 5; ++jj) if (jj == q + 1) for (int j = 0; j < SPL; ++j) z[jj][j] = e[j] * fct;
           }
           if (eta < 1.1 && newq == q) {
             eta = 1.0;
@@ -332,20 +480,28 @@ k_reactor(const uint8_t* __restrict__ img, ImageLayout L, int64_t n, double* __r
           have_eprev = 0;
           etamax = 10.0;
         } else if (ialth == 1 && q < qmax) {
-          eprev = e;
+#pragma unroll
+          for (int j = 0; j < SPL; ++j) eprev[j] = e[j];
           have_eprev = 1;
         }
         if (eta != 1.0) {
           double r = 1.0;
 #pragma unroll
-          for (int j = 1; j <= 5; ++j) if (j <= q) { r *= eta; z[j] *= r; }
+          for (int jj = 1; jj <= 5; ++jj) if (jj <= q) { r *= eta; for (int j = 0; j < SPL; ++j) z[jj][j] *= r; }
           h *= eta;
         }
       }
+      nst_total += nst;
+      if (status != FLINT_CELL_ERRTEST_FAIL && status != FLINT_CELL_NEWTON_FAIL) break;
+      }  // attempts
+      nst = nst_total;
       if (lane == 0) atomicAdd(counter + 4, (unsigned long long)nst);
-      y = z[0];
-      if (lane < ns) Yg[cell * ns + lane] = y;
-      else if (lane == ns) Tg[cell] = y;
+#pragma unroll
+      for (int j = 0; j < SPL; ++j) {
+        const int k = lane + 32 * j;
+        if (k < ns) Yg[cell * ns + k] = z[0][j];
+        else if (k == ns) Tg[cell] = z[0][j];
+      }
     }
     if (lane == 0) {
       if (status_g) status_g[cell] = status;
@@ -362,29 +518,41 @@ k_reactor(const uint8_t* __restrict__ img, ImageLayout L, int64_t n, double* __r
   }
 }
 
+static int spl_of(const ImageLayout& L) { return L.nsp / 32; }
+
 size_t reactor_smem(const ImageLayout& L) {
-  return L.bytes + (REACTOR_THREADS / 32) * (scratch_doubles(L.nsp, L.nrpad, true) * sizeof(double) + 32 * sizeof(int));
+  if (spl_of(L) == 1)
+    return L.bytes + (REACTOR_THREADS / 32) * (scratch_doubles(L.nsp, L.nrpad, true) * sizeof(double) + 32 * sizeof(int));
+  return L.bytes + (REACTOR_THREADS / 32) * (scratch_small_doubles(L.nsp, L.nrpad) * sizeof(double) + 64 * sizeof(int));
+}
+
+static const void* reactor_fn(const ImageLayout& L) {
+  return spl_of(L) == 1 ? (const void*)k_reactor<1> : (const void*)k_reactor<2>;
 }
 
 int reactor_slots(const ImageLayout& L) {
+  if (spl_of(L) < 1 || spl_of(L) > 2) return 0;
   size_t sm = reactor_smem(L);
-  if (cudaFuncSetAttribute(k_reactor, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) != cudaSuccess) return 0;
+  const void* fn = reactor_fn(L);
+  if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) != cudaSuccess) return 0;
   int per_sm = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_reactor, REACTOR_THREADS, sm);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, REACTOR_THREADS, sm);
   return per_sm * device_sms() * (REACTOR_THREADS / 32);
 }
 
-size_t reactor_slot_bytes() { return JSLOT * sizeof(double); }
+size_t reactor_slot_bytes(const ImageLayout& L) { return (size_t)reactor_slot_doubles_of(L) * sizeof(double); }
 
 cudaError_t launch_reactor(const uint8_t* img, const ImageLayout& L, int64_t n, double* T, const double* p,
                            double* Y, const double* dt, const flint_reactor_opts& o, int* status, int* nsteps,
                            unsigned int* work_counter, double* jsave, int slots, cudaStream_t st) {
   if (n <= 0) return cudaSuccess;
+  if (spl_of(L) < 1 || spl_of(L) > 2) return cudaErrorInvalidValue;
   size_t sm = reactor_smem(L);
-  cudaError_t e = cudaFuncSetAttribute(k_reactor, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  const void* fn = reactor_fn(L);
+  cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   if (e != cudaSuccess) return e;
   int per_sm = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_reactor, REACTOR_THREADS, sm);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, REACTOR_THREADS, sm);
   if (per_sm < 1) return cudaErrorInvalidConfiguration;
   int64_t warps_needed = n;
   int64_t blocks = (warps_needed + REACTOR_THREADS / 32 - 1) / (REACTOR_THREADS / 32);
@@ -411,8 +579,12 @@ cudaError_t launch_reactor(const uint8_t* img, const ImageLayout& L, int64_t n, 
   }
   e = cudaMemsetAsync(work_counter, 0, NCOUNTERS * sizeof(unsigned long long), st);
   if (e != cudaSuccess) return e;
-  k_reactor<<<(unsigned)blocks, REACTOR_THREADS, sm, st>>>(img, L, n, T, p, Y, dt, o, status, nsteps,
-                                                            reinterpret_cast<unsigned long long*>(work_counter), jsave);
+  if (spl_of(L) == 1)
+    k_reactor<1><<<(unsigned)blocks, REACTOR_THREADS, sm, st>>>(img, L, n, T, p, Y, dt, o, status, nsteps,
+                                                                 reinterpret_cast<unsigned long long*>(work_counter), jsave);
+  else
+    k_reactor<2><<<(unsigned)blocks, REACTOR_THREADS, sm, st>>>(img, L, n, T, p, Y, dt, o, status, nsteps,
+                                                                 reinterpret_cast<unsigned long long*>(work_counter), jsave);
   count_launch();
   return cudaGetLastError();
 }

@@ -63,7 +63,7 @@ struct Surrogate {
   // workspaces
   int64_t cap = 0;          // rows of the training / inference workspaces
   float* Z[MAXL] = {nullptr};
-  __nv_bfloat16* A[MAXL] = {nullptr};
+  float* A[MAXL] = {nullptr};   // FP32 activations (the forward GEMMs split them into BF16 hi + lo)
   float *dz0 = nullptr, *dz1 = nullptr, *yhat = nullptr, *xf = nullptr, *yout2 = nullptr;
   double* loss = nullptr;
   // fallback compaction
@@ -300,14 +300,15 @@ static cudaError_t net_forward(Surrogate* s, Net& nt, int64_t n, const float* X,
   for (int l = 0; l < nt.nl && !e; ++l) {
     GemmArgs g{};
     g.M = (int)n; g.N = nt.dims[l + 1]; g.K = nt.dims[l];
-    if (l == 0) { g.A = X; g.a_bf16 = 0; } else { g.A = s->A[l - 1]; g.a_bf16 = 1; }
+    if (l == 0) { g.A = X; g.a_bf16 = 0; } else { g.A = s->A[l - 1]; g.a_bf16 = 0; }
     g.sa_m = g.K; g.sa_k = 1;
-    g.B = nt.wb + nt.off_w[l]; g.b_bf16 = 1; g.sb_k = 1; g.sb_n = g.K;
+    g.B = nt.w + nt.off_w[l]; g.b_bf16 = 0; g.sb_k = 1; g.sb_n = g.K;
+    g.split = 1;
     g.bias = nt.w + nt.off_b[l];
     if (l < nt.nl - 1) {
       g.epi = EPI_BIAS_GELU;
       g.C = keep ? s->Z[l] : nullptr; g.ldc = g.N;
-      g.Cb = s->A[l]; g.ldcb = g.N;
+      g.Cf = s->A[l]; g.ldcf = g.N;
     } else {
       g.epi = EPI_BIAS;
       g.C = out; g.ldc = g.N;
@@ -327,7 +328,7 @@ static int alloc_ws(Surrogate* s, int64_t cap) {
   cudaError_t e = cudaSuccess;
   for (int l = 0; l < s->net[0].nl - 1 && !e; ++l) {
     e = cudaMalloc(&s->Z[l], cap * s->H * sizeof(float));
-    if (!e) e = cudaMalloc(&s->A[l], cap * s->H * sizeof(__nv_bfloat16));
+    if (!e) e = cudaMalloc(&s->A[l], cap * s->H * sizeof(float));
   }
   if (!e) e = cudaMalloc(&s->dz0, cap * W * sizeof(float));
   if (!e) e = cudaMalloc(&s->dz1, cap * W * sizeof(float));
@@ -505,7 +506,7 @@ int surrogate_train_step(Surrogate* s, int net, int64_t n, const float* X, const
     GemmArgs g{};
     g.M = N; g.N = K; g.K = (int)n;
     g.A = dz; g.a_bf16 = 0; g.sa_m = 1; g.sa_k = N;
-    if (l == 0) { g.B = X; g.b_bf16 = 0; } else { g.B = s->A[l - 1]; g.b_bf16 = 1; }
+    if (l == 0) { g.B = X; g.b_bf16 = 0; } else { g.B = s->A[l - 1]; g.b_bf16 = 0; }
     g.sb_k = K; g.sb_n = 1;
     g.C = nt.g + nt.off_w[l]; g.ldc = K; g.epi = EPI_STORE;
     if (launch_gemm(g, st)) return FLINT_ERR_CUDA;

@@ -468,6 +468,14 @@ static double wrms(int n, const double* v, const double* w) {
   return sqrt(s / n);
 }
 
+/* Weighted max norm: the Newton convergence test, so that no single
+ * component (a trace radical at atol) can stay unconverged behind the RMS. */
+static double wmax(int n, const double* v, const double* w) {
+  double m = 0.0;
+  for (int i = 0; i < n; ++i) { double t = fabs(v[i] * w[i]); if (t > m) m = t; }
+  return m;
+}
+
 /* LU with partial pivoting (first maximal |a| on ties), in place, column-major. */
 static int lu_factor(int n, double* a, int* piv) {
   for (int k = 0; k < n; ++k) {
@@ -557,6 +565,9 @@ static int bdf_cell(const rhs_ctx* cx, int n, double* y, double tout, const flin
     for (int i = 0; i < n; ++i) ewt[i] = 1.0 / (rtol * fabs(z[0][i]) + atol);
     int ncf = 0, nef = 0, need_J = 0;
     double dsm = 0.0;
+    /* the first Newton iterate of a step is judged with a rate of at least 0.3:
+     * a small rate carried over from the last step would accept it unchecked */
+    if (crate < 0.3) crate = 0.3;
     int accepted = 0;
     while (!accepted) {
       if (h < 1e-300 || t + h == t) { status = FLINT_CELL_ERRTEST_FAIL; break; }
@@ -591,7 +602,7 @@ static int bdf_cell(const rhs_ctx* cx, int n, double* y, double tout, const flin
         for (int i = 0; i < n; ++i) b[i] = gamma * f[i] - z[1][i] / l1 - e[i];
         lu_solve(n, Mlu, piv, b);
         if (gamrat != 1.0) { double s = 2.0 / (1.0 + gamrat); for (int i = 0; i < n; ++i) b[i] *= s; }
-        double del = wrms(n, b, ewt);
+        double del = wmax(n, b, ewt);
         for (int i = 0; i < n; ++i) { e[i] += b[i]; y[i] = ypred[i] + e[i]; }
         if (mi > 0) { double r = del / delp; crate = (0.3 * crate > r) ? 0.3 * crate : r; }
         double dcon = del * (crate < 1.0 ? crate : 1.0) * Eq / 0.1;
@@ -626,6 +637,7 @@ static int bdf_cell(const rhs_ctx* cx, int n, double* y, double tout, const flin
         double r = 1.0;
         for (int j = 1; j <= q; ++j) { r *= eta; for (int i = 0; i < n; ++i) z[j][i] *= r; }
         h *= eta; ialth = q + 1; have_eprev = 0; last = 0;
+        if (!jfresh) need_J = 1;   /* retry with a Jacobian of this state */
         continue;
       }
       accepted = 1;
@@ -690,6 +702,29 @@ static int bdf_cell(const rhs_ctx* cx, int n, double* y, double tout, const flin
   return status;
 }
 
+/* A cell whose integration fails (error test or Newton) is integrated again
+ * from its initial state, first at order <= 2 with atol / 100 (BDF1-2 are
+ * A-stable; orders 3-5 are not, and a mechanism's oscillatory modes can defeat
+ * them), then at order 1.  nsteps counts the steps of every attempt. */
+static int reactor_cell(const rhs_ctx* cx, int n, double* y, double tout, const flint_reactor_opts* o,
+                        int* nsteps_out) {
+  double y0[MAXNS + 1];
+  for (int i = 0; i < n; ++i) y0[i] = y[i];
+  int total = 0, st = FLINT_CELL_OK;
+  for (int att = 0; att < 3; ++att) {
+    flint_reactor_opts oa = *o;
+    if (att == 1) { if (oa.max_order > 2) oa.max_order = 2; oa.atol *= 1e-2; }
+    if (att == 2) oa.max_order = 1;
+    if (att > 0) for (int i = 0; i < n; ++i) y[i] = y0[i];
+    int nst = 0;
+    st = bdf_cell(cx, n, y, tout, &oa, &nst);
+    total += nst;
+    if (st != FLINT_CELL_ERRTEST_FAIL && st != FLINT_CELL_NEWTON_FAIL) break;
+  }
+  *nsteps_out = total;
+  return st;
+}
+
 void orc_reactor_advance(const flint_mech_desc* m, int64_t n, double* T, const double* p,
                          double* Y, const double* dt, const flint_reactor_opts* o,
                          int* status, int* nsteps, int nthreads) {
@@ -708,7 +743,7 @@ void orc_reactor_advance(const flint_mech_desc* m, int64_t n, double* T, const d
     else if (dt[i] == 0.0) st = FLINT_CELL_OK;
     else {
       rhs_ctx cx = {m, p[i], o->constant_volume};
-      st = bdf_cell(&cx, ns + 1, y, dt[i], o, &nst);
+      st = reactor_cell(&cx, ns + 1, y, dt[i], o, &nst);
       for (int k = 0; k < ns; ++k) Y[i * ns + k] = y[k];
       T[i] = y[ns];
     }

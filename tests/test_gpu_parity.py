@@ -108,12 +108,15 @@ def test_c1_chemistry_source_clamps(c1):
     assert wdot_err(w.cpu().numpy().ravel(), w_o, ws_o) < 1e-11
 
 
-@pytest.mark.parametrize("cfg", ["c2", "pelucchi"])
+@pytest.mark.parametrize("cfg", ["c2", "pelucchi", "c5"])
 def test_wdot_and_jacobian(cfg):
     if cfg == "pelucchi":
         import os
         mech = Mechanism.load(os.path.join(os.path.dirname(__file__), "golden", "mech_pelucchi.json"))
         T, p, Y = mechgen.c2_states(1500, mech, seed=11)
+    elif cfg == "c5":
+        mech = mechgen.load("c5")            # 54 species: two species per lane
+        T, p, Y = mechgen.c2_states(1200, mech, seed=12)
     else:
         mech = mechgen.load("c2")
         T, p, Y = mechgen.c2_states(3000, mech)
@@ -254,4 +257,24 @@ def test_reactor_real_mechanism_pelucchi():
     # non-igniting synthetic cases
     for Tv, Yv in ((Tg, Yg), (T_o, Y_o)):
         assert np.max(np.abs(Tv - T_x) / T_x) < 5e-5 and np.abs(Yv - Y_x).max() < 2e-5
+    assert abs(nst.cpu().numpy().sum() / ns_o.sum() - 1.0) < 0.05
+
+
+def test_reactor_c5_54_species():
+    """The 54-species / 320-reaction scale-up mechanism (55 unknowns: two per lane,
+    the Newton matrix in a global per-warp slot)."""
+    mech = mechgen.load("c5")
+    T, p, Y, dt = mechgen.c5_states(160, mech, seed=51)
+    orc = Oracle(mech)
+    T_o, Y_o, st_o, ns_o = orc.reactor_advance(T, p, Y, dt, reactor_opts())
+    T_x, Y_x, st_x, _ = orc.reactor_advance(T, p, Y, dt, reactor_opts(rtol=1e-12, atol=1e-18, max_steps=400000))
+    chem = Chemistry(mech)
+    Tt, pt, Yt, dtt = cuda(T, p, Y, dt)
+    st, nst = chem.reactor_advance(Tt, pt, Yt, dtt)
+    torch.cuda.synchronize()
+    st = st.cpu().numpy()
+    assert (st == 0).all() and (st_o == 0).all() and (st_x == 0).all()
+    Tg, Yg = Tt.cpu().numpy(), Yt.cpu().numpy()
+    for Tv, Yv in ((Tg, Yg), (T_o, Y_o)):
+        assert np.max(np.abs(Tv - T_x) / T_x) < 1e-5 and np.abs(Yv - Y_x).max() < 1e-6
     assert abs(nst.cpu().numpy().sum() / ns_o.sum() - 1.0) < 0.05

@@ -1,5 +1,5 @@
 """The learned surrogate: MLP forward and gradients against a NumPy oracle of
-the same BF16/FP32 arithmetic, training, checkpoint resume, and the gated
+the same split-BF16 / BF16 / FP32 arithmetic, training, checkpoint resume, and the gated
 surrogate + fallback advance (conservation, status codes, fallback = integrator)."""
 import numpy as np
 import pytest
@@ -25,8 +25,14 @@ def gelu_grad(x):
     return 0.5 * (1 + t) + 0.5 * x * (1 - t * t) * 0.7978845608028654 * (1 + 3 * 0.044715 * x * x)
 
 
-def np_forward_backward(w, dims, X, T):
-    """NumPy oracle: BF16 operands, FP64 accumulation, FP32 storage."""
+def np_forward_backward(w, dims, X, T, rnd=None):
+    """NumPy oracle of the device arithmetic, FP64 accumulation, FP32 storage.
+
+    Forward: FP32 operands (the device splits each into a BF16 hi + lo pair,
+    about 16 significant bits); ``rnd=bf16`` gives plain single-BF16 operands
+    instead, for comparison.  Backward: BF16 operands (weights, activations
+    and back-propagated errors rounded once)."""
+    rnd = rnd or (lambda x: np.asarray(x, np.float32))
     Ws, bs, o = [], [], 0
     for i in range(len(dims) - 1):
         Ws.append(w[o:o + dims[i + 1] * dims[i]].reshape(dims[i + 1], dims[i])); o += dims[i + 1] * dims[i]
@@ -34,9 +40,9 @@ def np_forward_backward(w, dims, X, T):
     a, ins, zs = X.astype(np.float32), [], []
     for l in range(len(Ws)):
         ins.append(bf16(a))
-        z = (ins[-1].astype(np.float64) @ bf16(Ws[l]).T.astype(np.float64) + bs[l]).astype(np.float32)
+        z = (rnd(a).astype(np.float64) @ rnd(Ws[l]).T.astype(np.float64) + bs[l]).astype(np.float32)
         zs.append(z)
-        a = bf16(gelu(z)) if l < len(Ws) - 1 else z
+        a = gelu(z).astype(np.float32) if l < len(Ws) - 1 else z
     y = a
     g = (2.0 * (y - T) / y.size).astype(np.float32)
     grads = [None] * len(Ws)
@@ -74,7 +80,11 @@ def test_mlp_forward_and_gradient_vs_numpy():
     y_np, grads = np_forward_backward(w0, sur.dims, X, Tt)
     Xd, Td = torch.from_numpy(X).cuda(), torch.from_numpy(Tt).cuda()
     y = sur.predict(Xd).cpu().numpy()
-    assert np.abs(y - y_np).max() / np.abs(y_np).max() < 1e-3
+    err = np.abs(y - y_np).max() / np.abs(y_np).max()
+    assert err < 1e-4, err
+    # the split operands beat single-BF16 operands by more than an order of magnitude
+    y_b, _ = np_forward_backward(w0, sur.dims, X, Tt, rnd=bf16)
+    assert err < 0.1 * np.abs(y_b - y_np).max() / np.abs(y_np).max()
     loss = sur.train_step(Xd, Td, 1e-7, want_loss=True)
     assert abs(loss - float(((y_np - Tt) ** 2).mean())) < 1e-3 * loss
     st, step = sur.get_state()
