@@ -160,9 +160,13 @@ def run_ours(args):
     from flint_gb300 import mechgen
     from flint_gb300.api import Chemistry, reactor_stats, kernel_launches
     from flint_gb300 import native
-    mech = mechgen.load("c2")
+    c5 = args.workload == "reactor-c5"
+    mech = mechgen.load("c5" if c5 else "c2")
     n = args.cells
-    T0, p0, Y0, dt0 = mechgen.c3_states(n, mech, seed=1003 + rank)
+    if c5:
+        T0, p0, Y0, dt0 = mechgen.c5_states(n, mech, seed=1005 + rank)
+    else:
+        T0, p0, Y0, dt0 = mechgen.c3_states(n, mech, seed=1003 + rank)
     chem = Chemistry(mech)
     Td0 = torch.from_numpy(T0).to(dev)
     Yd0 = torch.from_numpy(Y0).to(dev)
@@ -262,9 +266,13 @@ def run_ours(args):
     line = {"metric": METRIC, "value": value, "unit": "cell-steps/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded states, seeded synthetic mechanism)",
-            "config": {"workload": "reactor-c3: 31sp/160r constant-p BDF/Newton, 262144 cells, rtol 1e-8 atol 1e-14",
-                       "cells_per_gpu": n, "mechanism": "synthetic-31sp-160r (12 third-body, 6 Troe)",
-                       "path": "plain FP64 integrator", "l2": "flushed (256 MiB write) between timed steps"},
+            "config": ({"workload": f"reactor-c5: 54sp/320r constant-p BDF/Newton, {n} cells (sample of the "
+                                    "4,194,304-cell scale-up), T0 900-2000 K, p 1-40 atm, phi 0.4-3, dt 1e-7..1e-4 s, "
+                                    "rtol 1e-8 atol 1e-14",
+                        "cells_per_gpu": n, "mechanism": "synthetic-54sp-320r (20 third-body, 12 Troe)"} if c5 else
+                       {"workload": "reactor-c3: 31sp/160r constant-p BDF/Newton, 262144 cells, rtol 1e-8 atol 1e-14",
+                        "cells_per_gpu": n, "mechanism": "synthetic-31sp-160r (12 third-body, 6 Troe)"})
+                      | {"path": "plain FP64 integrator", "l2": "flushed (256 MiB write) between timed steps"},
             "e2e": {"value": n * ws / e2e_t, "unit": "cell-steps/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
             "gpu_launches": launches, "clocks": clk, "roofline": roof,
@@ -439,9 +447,17 @@ def run_kernel_workload(args):
         if args.workload == "c2-wdotjac" else None
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
     stream = torch.cuda.current_stream()
+    gen = None
+    if args.generated:
+        if jac is not None:
+            raise SystemExit("--generated covers wdot/cp/h only")
+        from flint_gb300.ytf_cuda import GeneratedMechanism
+        gen = GeneratedMechanism(chem.mech)
 
     def step():
-        if jac is None:
+        if gen is not None:
+            gen.wdot(Td, pd, Yd, wdot=w, cp=cp, h=h)
+        elif jac is None:
             chem.wdot(Td, pd, Yd, wdot=w, cp=cp, h=h)
         else:
             chem.wdot_jac(Td, pd, Yd, wdot=w, jac=jac)
@@ -459,7 +475,8 @@ def run_kernel_workload(args):
     t = statistics.mean(times)
     nv = chem.ns + 1
     bytes_per_state = 8 * (2 + 2 * chem.ns) + (8 * nv * nv if jac is not None else 16)
-    print(json.dumps({"workload": args.workload, "metric": "states/s", "value": n / t, "unit": "states/s",
+    print(json.dumps({"workload": args.workload, "kernel": "generated (ytf_cuda)" if gen else "data-driven",
+                      "metric": "states/s", "value": n / t, "unit": "states/s",
                       "ms_per_step": t * 1e3, "states": n, "steps": args.steps, "warmup": args.warmup,
                       "gpu_launches": kernel_launches() - l0,
                       "hbm_gbs_algorithmic": n * bytes_per_state / t / 1e9,
@@ -484,13 +501,20 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cells", type=int, default=None)
-    ap.add_argument("--workload", default="reactor", choices=["reactor", "c1-wdot", "c2-wdot", "c2-wdotjac"])
+    ap.add_argument("--workload", default="reactor",
+                    choices=["reactor", "reactor-c5", "c1-wdot", "c2-wdot", "c2-wdotjac"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--generated", action="store_true",
+                    help="source-term workloads: run the per-mechanism generated kernel (ytf_cuda)")
     ap.add_argument("--ref-seconds", type=float, default=10.0)
     ap.add_argument("--path", default="auto", choices=["auto", "surrogate", "plain"],
                     help="surrogate+fallback (headline, needs the trained checkpoint) or the plain integrator")
     ap.add_argument("--checkpoint", default=SURROGATE_CKPT)
     args = ap.parse_args()
+    if args.workload == "reactor-c5":
+        args.cells = args.cells or CELLS
+        run_ours(args)
+        return
     if args.workload != "reactor":
         run_kernel_workload(args)
         return

@@ -485,7 +485,7 @@ int flint_surrogate_advance(flint_surrogate_t s, int64_t n, double* T, const dou
   rc = ensure_jsave(s->mech);
   if (rc) return rc;
   rc = surrogate_advance(s->s, n, T, p, Y, dt, o, gate, status, nsteps, s->mech->djsave, s->mech->jslots,
-                         nullptr, (cudaStream_t)stream);
+                         nullptr, counts != nullptr, (cudaStream_t)stream);
   if (rc) return fail(rc, "flint_surrogate_advance failed: %s", cudaGetErrorString(cudaGetLastError()));
   if (counts) surrogate_counts(s->s, &counts[0], &counts[1]);
   return FLINT_OK;
@@ -500,7 +500,8 @@ int flint_surrogate_evaluate(flint_surrogate_t s, int64_t n, double* T, const do
   if (!T || !p || !Y || !dt) return fail(FLINT_ERR_ARG, "NULL array");
   flint_reactor_opts o;
   flint_reactor_default_opts(&o);
-  rc = surrogate_advance(s->s, n, T, p, Y, dt, o, gate, nullptr, nullptr, nullptr, 0, metrics, (cudaStream_t)stream);
+  rc = surrogate_advance(s->s, n, T, p, Y, dt, o, gate, nullptr, nullptr, nullptr, 0, metrics, false,
+                         (cudaStream_t)stream);
   return rc ? fail(rc, "flint_surrogate_evaluate failed") : FLINT_OK;
 }
 

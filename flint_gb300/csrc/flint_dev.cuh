@@ -196,8 +196,12 @@ __host__ __device__ inline int scratch_small_doubles(int nsp, int nrpad) {
 __host__ __device__ inline int scratch_jac_doubles(int nsp, int nrpad) {
   return (8 * nrpad + (nsp + 1) * (nsp + 1) + 1) & ~1;
 }
+// One block of scratch per warp.  With the Jacobian, the derivative rows dq
+// start where the falloff scratch fo starts: fo is used only by the kernel
+// calls without the Jacobian (in the Jacobian call it lives in Jr), and dq only
+// inside a Jacobian call, so the two may share (8 nrpad >= 256 doubles).
 __host__ __device__ inline int scratch_doubles(int nsp, int nrpad, bool jac) {
-  return scratch_small_doubles(nsp, nrpad) + (jac ? scratch_jac_doubles(nsp, nrpad) : 0);
+  return jac ? ((3 * nsp + nrpad + 8 * nrpad + (nsp + 1) * (nsp + 1) + 1) & ~1) : scratch_small_doubles(nsp, nrpad);
 }
 
 __device__ inline WarpScratch carve2(double* small, double* jacbuf, int nsp, int nrpad) {
@@ -212,7 +216,7 @@ __device__ inline WarpScratch carve2(double* small, double* jacbuf, int nsp, int
 
 // Both parts contiguous in one buffer (shared memory, up to 31 species).
 __device__ inline WarpScratch carve(double* p, int nsp, int nrpad, bool jac) {
-  return carve2(p, jac ? p + scratch_small_doubles(nsp, nrpad) : nullptr, nsp, nrpad);
+  return carve2(p, jac ? p + 3 * nsp + nrpad : nullptr, nsp, nrpad);
 }
 
 // Cell-level results held per lane: lane k (< ns) gets species k, the T-row

@@ -30,7 +30,8 @@ int reactor_slots(const ImageLayout& L);
 size_t reactor_slot_bytes(const ImageLayout& L);
 cudaError_t launch_reactor(const uint8_t* img, const ImageLayout& L, int64_t n, double* T, const double* p,
                            double* Y, const double* dt, const flint_reactor_opts& o, int* status, int* nsteps,
-                           unsigned int* work_counter, double* jsave, int slots, cudaStream_t st);
+                           unsigned int* work_counter, double* jsave, int slots, cudaStream_t st,
+                           const unsigned long long* n_dev = nullptr);   // optional device-side cell count <= n
 
 size_t reactor_noalloc_bytes();
 int reactor_noalloc_slots();
@@ -54,7 +55,7 @@ int surrogate_train_step(Surrogate* s, int net, int64_t n, const float* X, const
 int surrogate_state(Surrogate* s, int net, float* host, int64_t* step, int get);
 int surrogate_advance(Surrogate* s, int64_t n, double* T, const double* p, double* Y, const double* dt,
                       const flint_reactor_opts& o, const flint_surrogate_gate* gate, int* status, int* nsteps,
-                      double* jsave, int jslots, double* metrics, cudaStream_t st);
+                      double* jsave, int jslots, double* metrics, bool want_counts, cudaStream_t st);
 void surrogate_counts(Surrogate* s, int64_t* acc, int64_t* rej);
 
 // tabulated (reference general-loop) path, flint_table.cu

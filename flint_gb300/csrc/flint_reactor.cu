@@ -179,8 +179,10 @@ __global__ void __launch_bounds__(REACTOR_THREADS)
 k_reactor(const uint8_t* __restrict__ img, ImageLayout L, int64_t n, double* __restrict__ Tg,
           const double* __restrict__ pg, double* __restrict__ Yg, const double* __restrict__ dtg,
           flint_reactor_opts o, int* __restrict__ status_g, int* __restrict__ nsteps_g,
-          unsigned long long* __restrict__ counter, double* __restrict__ jsave) {
+          unsigned long long* __restrict__ counter, double* __restrict__ jsave,
+          const unsigned long long* __restrict__ n_dev) {
   extern __shared__ __align__(16) uint8_t smem[];
+  if (n_dev) n = min(n, (int64_t)*n_dev);   // cell count produced on the device
   stage_image(smem, img, L.bytes);
   MechView m;
   m.bind(L, smem);
@@ -544,7 +546,8 @@ size_t reactor_slot_bytes(const ImageLayout& L) { return (size_t)reactor_slot_do
 
 cudaError_t launch_reactor(const uint8_t* img, const ImageLayout& L, int64_t n, double* T, const double* p,
                            double* Y, const double* dt, const flint_reactor_opts& o, int* status, int* nsteps,
-                           unsigned int* work_counter, double* jsave, int slots, cudaStream_t st) {
+                           unsigned int* work_counter, double* jsave, int slots, cudaStream_t st,
+                           const unsigned long long* n_dev) {
   if (n <= 0) return cudaSuccess;
   if (spl_of(L) < 1 || spl_of(L) > 2) return cudaErrorInvalidValue;
   size_t sm = reactor_smem(L);
@@ -581,10 +584,12 @@ cudaError_t launch_reactor(const uint8_t* img, const ImageLayout& L, int64_t n, 
   if (e != cudaSuccess) return e;
   if (spl_of(L) == 1)
     k_reactor<1><<<(unsigned)blocks, REACTOR_THREADS, sm, st>>>(img, L, n, T, p, Y, dt, o, status, nsteps,
-                                                                 reinterpret_cast<unsigned long long*>(work_counter), jsave);
+                                                                 reinterpret_cast<unsigned long long*>(work_counter), jsave,
+                                                                 n_dev);
   else
     k_reactor<2><<<(unsigned)blocks, REACTOR_THREADS, sm, st>>>(img, L, n, T, p, Y, dt, o, status, nsteps,
-                                                                 reinterpret_cast<unsigned long long*>(work_counter), jsave);
+                                                                 reinterpret_cast<unsigned long long*>(work_counter), jsave,
+                                                                 n_dev);
   count_launch();
   return cudaGetLastError();
 }

@@ -36,6 +36,7 @@
 namespace flint {
 
 constexpr int MAXL = 8;
+constexpr int MAXS = 64;   // species of a surrogate mechanism (the reactor's limit, 63)
 constexpr int SURR_THREADS = 128;
 
 struct Net {
@@ -61,7 +62,9 @@ struct Surrogate {
   double* Bm;               // [ne][ns] element rows divided by W (device)
   int ne;
   // workspaces
-  int64_t cap = 0;          // rows of the training / inference workspaces
+  int64_t cap = 0;          // rows of the inference workspaces (A, yhat, yout2, xf)
+  int64_t cap_tr = 0;       // rows of the training-only workspaces (Z, dz0, dz1)
+  int64_t cap_fb = 0;       // cells of the fallback compaction buffers
   float* Z[MAXL] = {nullptr};
   float* A[MAXL] = {nullptr};   // FP32 activations (the forward GEMMs split them into BF16 hi + lo)
   float *dz0 = nullptr, *dz1 = nullptr, *yhat = nullptr, *xf = nullptr, *yout2 = nullptr;
@@ -126,7 +129,7 @@ k_post(const uint8_t* __restrict__ img, ImageLayout L, int64_t n, int64_t base, 
   double* sB = reinterpret_cast<double*>(smem + L.bytes);
   for (int i = threadIdx.x; i < ne * ns; i += blockDim.x) sB[i] = Bm[i];
   __syncthreads();
-  double dY[32], Y1[32];
+  double dY[MAXS], Y1[MAXS];
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     const int64_t cell = base + i;
     const double T0 = T[cell], dti = dt[cell], pc = p[cell];
@@ -159,7 +162,7 @@ k_post(const uint8_t* __restrict__ img, ImageLayout L, int64_t n, int64_t base, 
     // conservative, non-negative mass fractions: project dY onto element
     // conservation over the free species, clip negatives to zero (they leave
     // the free set), repeat (active-set least-squares, at most 4 passes)
-    unsigned int fixed = 0u;   // bit k: species k clipped at zero
+    unsigned long long fixed = 0ull;   // bit k: species k clipped at zero
     double clipped = 0.0;
     for (int k = 0; k < ns; ++k) Y1[k] = Y[cell * ns + k] + dY[k];
     bool clean = false;
@@ -172,7 +175,7 @@ k_post(const uint8_t* __restrict__ img, ImageLayout L, int64_t n, int64_t base, 
         for (int f = 0; f < ne; ++f) {
           double g = 0.0;
           for (int k = 0; k < ns; ++k)
-            if (!((fixed >> k) & 1u)) g += sB[e * ns + k] * sB[f * ns + k];
+            if (!((fixed >> k) & 1ull)) g += sB[e * ns + k] * sB[f * ns + k];
           G[e][f] = g;
         }
       }
@@ -201,14 +204,14 @@ k_post(const uint8_t* __restrict__ img, ImageLayout L, int64_t n, int64_t base, 
       for (int e = 0; e < ne; ++e) if (!live[e]) lam[e] = 0.0;
       clean = true;
       for (int k = 0; k < ns; ++k) {
-        if ((fixed >> k) & 1u) continue;
+        if ((fixed >> k) & 1ull) continue;
         double corr = 0.0;
         for (int e = 0; e < ne; ++e) corr += sB[e * ns + k] * lam[e];
         Y1[k] -= corr;
         if (Y1[k] < 0.0 && pass < 3) {
           clipped += -Y1[k];
           Y1[k] = 0.0;
-          fixed |= 1u << k;
+          fixed |= 1ull << k;
           clean = false;
         }
       }
@@ -264,9 +267,10 @@ k_post(const uint8_t* __restrict__ img, ImageLayout L, int64_t n, int64_t base, 
   }
 }
 
-__global__ void k_gather(int64_t m, const int64_t* __restrict__ idx, int ns, const double* __restrict__ T,
+__global__ void k_gather(const unsigned long long* __restrict__ count, const int64_t* __restrict__ idx, int ns, const double* __restrict__ T,
                          const double* __restrict__ p, const double* __restrict__ Y, const double* __restrict__ dt,
                          double* __restrict__ cT, double* __restrict__ cp, double* __restrict__ cY, double* __restrict__ cdt) {
+  const int64_t m = (int64_t)*count;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x) {
     const int64_t c = idx[i];
     cT[i] = T[c]; cp[i] = p[c]; cdt[i] = dt[c];
@@ -274,10 +278,11 @@ __global__ void k_gather(int64_t m, const int64_t* __restrict__ idx, int ns, con
   }
 }
 
-__global__ void k_scatter(int64_t m, const int64_t* __restrict__ idx, int ns, double* __restrict__ T,
+__global__ void k_scatter(const unsigned long long* __restrict__ count, const int64_t* __restrict__ idx, int ns, double* __restrict__ T,
                           double* __restrict__ Y, const double* __restrict__ cT, const double* __restrict__ cY,
                           const int* __restrict__ cst, const int* __restrict__ cns, int* __restrict__ status,
                           int* __restrict__ nsteps) {
+  const int64_t m = (int64_t)*count;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x) {
     const int64_t c = idx[i];
     T[c] = cT[i];
@@ -318,32 +323,53 @@ static cudaError_t net_forward(Surrogate* s, Net& nt, int64_t n, const float* X,
   return e;
 }
 
-static int alloc_ws(Surrogate* s, int64_t cap) {
-  if (cap <= s->cap) return 0;
+static int alloc_ws(Surrogate* s, int64_t cap, bool train) {
   auto fr = [](void* p) { if (p) cudaFree(p); };
-  for (int l = 0; l < MAXL; ++l) { fr(s->Z[l]); fr(s->A[l]); s->Z[l] = nullptr; s->A[l] = nullptr; }
-  fr(s->dz0); fr(s->dz1); fr(s->yhat); fr(s->xf); fr(s->yout2); fr(s->rej_idx);
-  fr(s->cT); fr(s->cp); fr(s->cY); fr(s->cdt); fr(s->cst); fr(s->cns);
-  const int W = std::max(s->H, std::max(s->n_in, s->n_out));
   cudaError_t e = cudaSuccess;
-  for (int l = 0; l < s->net[0].nl - 1 && !e; ++l) {
-    e = cudaMalloc(&s->Z[l], cap * s->H * sizeof(float));
-    if (!e) e = cudaMalloc(&s->A[l], cap * s->H * sizeof(float));
+  const int nh = s->net[0].nl - 1;
+  if (cap > s->cap) {
+    for (int l = 0; l < MAXL; ++l) { fr(s->A[l]); s->A[l] = nullptr; }
+    fr(s->yhat); fr(s->xf); fr(s->yout2);
+    s->yhat = s->xf = s->yout2 = nullptr;
+    s->cap = 0;
+    for (int l = 0; l < nh && !e; ++l) e = cudaMalloc(&s->A[l], cap * s->H * sizeof(float));
+    if (!e) e = cudaMalloc(&s->yhat, cap * s->n_out * sizeof(float));
+    if (!e) e = cudaMalloc(&s->yout2, cap * s->n_out * sizeof(float));
+    if (!e) e = cudaMalloc(&s->xf, cap * s->n_in * sizeof(float));
+    if (e) return FLINT_ERR_NOMEM;
+    s->cap = cap;
   }
-  if (!e) e = cudaMalloc(&s->dz0, cap * W * sizeof(float));
-  if (!e) e = cudaMalloc(&s->dz1, cap * W * sizeof(float));
-  if (!e) e = cudaMalloc(&s->yhat, cap * s->n_out * sizeof(float));
-  if (!e) e = cudaMalloc(&s->yout2, cap * s->n_out * sizeof(float));
-  if (!e) e = cudaMalloc(&s->xf, cap * s->n_in * sizeof(float));
-  if (!e) e = cudaMalloc(&s->rej_idx, cap * sizeof(int64_t));
-  if (!e) e = cudaMalloc(&s->cT, cap * sizeof(double));
-  if (!e) e = cudaMalloc(&s->cp, cap * sizeof(double));
-  if (!e) e = cudaMalloc(&s->cdt, cap * sizeof(double));
-  if (!e) e = cudaMalloc(&s->cY, cap * s->ns * sizeof(double));
-  if (!e) e = cudaMalloc(&s->cst, cap * sizeof(int));
-  if (!e) e = cudaMalloc(&s->cns, cap * sizeof(int));
+  if (train && cap > s->cap_tr) {
+    for (int l = 0; l < MAXL; ++l) { fr(s->Z[l]); s->Z[l] = nullptr; }
+    fr(s->dz0); fr(s->dz1);
+    s->dz0 = s->dz1 = nullptr;
+    s->cap_tr = 0;
+    const int W = std::max(s->H, std::max(s->n_in, s->n_out));
+    for (int l = 0; l < nh && !e; ++l) e = cudaMalloc(&s->Z[l], cap * s->H * sizeof(float));
+    if (!e) e = cudaMalloc(&s->dz0, cap * W * sizeof(float));
+    if (!e) e = cudaMalloc(&s->dz1, cap * W * sizeof(float));
+    if (e) return FLINT_ERR_NOMEM;
+    s->cap_tr = cap;
+  }
+  return 0;
+}
+
+// Compaction buffers of the fallback: room for every cell of a call.
+static int alloc_fb(Surrogate* s, int64_t n) {
+  if (n <= s->cap_fb) return 0;
+  auto fr = [](void* p) { if (p) cudaFree(p); };
+  fr(s->rej_idx); fr(s->cT); fr(s->cp); fr(s->cY); fr(s->cdt); fr(s->cst); fr(s->cns);
+  s->rej_idx = nullptr; s->cT = s->cp = s->cY = s->cdt = nullptr; s->cst = s->cns = nullptr;
+  s->cap_fb = 0;
+  cudaError_t e = cudaMalloc(&s->rej_idx, n * sizeof(int64_t));
+  if (!e) e = cudaMalloc(&s->cT, n * sizeof(double));
+  if (!e) e = cudaMalloc(&s->cp, n * sizeof(double));
+  if (!e) e = cudaMalloc(&s->cdt, n * sizeof(double));
+  if (!e) e = cudaMalloc(&s->cY, n * s->ns * sizeof(double));
+  if (!e) e = cudaMalloc(&s->cst, n * sizeof(int));
+  if (!e) e = cudaMalloc(&s->cns, n * sizeof(int));
   if (e) return FLINT_ERR_NOMEM;
-  s->cap = cap;
+  s->cap_fb = n;
   return 0;
 }
 
@@ -389,7 +415,7 @@ static int net_init(Net& nt, int nl, const int* dims, const float* w0) {
 int surrogate_create(const uint8_t* mimg, const ImageLayout& L, unsigned int* counter, const flint_surrogate_desc* d,
                      Surrogate** out, std::string& err) {
   if (d->n_layers < 2 || d->n_layers > MAXL) { err = "n_layers out of range"; return FLINT_ERR_ARG; }
-  if (L.ns > 31 || L.ns < 2) { err = "surrogate supports 2..31 species"; return FLINT_ERR_MECH; }
+  if (L.ns > MAXS - 1 || L.ns < 2) { err = "surrogate supports 2..63 species"; return FLINT_ERR_MECH; }
   if (d->bath < 0 || d->bath >= L.ns) { err = "bath species index"; return FLINT_ERR_ARG; }
   if (d->n_nets < 1 || d->n_nets > 2) { err = "n_nets must be 1 or 2"; return FLINT_ERR_ARG; }
   if (!d->weights || !d->x_mean || !d->x_std || !d->y_mean || !d->y_std || !d->elem) { err = "NULL array"; return FLINT_ERR_ARG; }
@@ -482,7 +508,7 @@ int surrogate_targets(Surrogate* s, int64_t n, const double* T0, const double* Y
 int surrogate_predict(Surrogate* s, int net, int64_t n, const float* X, float* Yn, cudaStream_t st) {
   if (net < 0 || net >= s->nnets) return FLINT_ERR_ARG;
   if (n <= 0) return 0;
-  if (alloc_ws(s, std::min<int64_t>(n, 262144))) return FLINT_ERR_NOMEM;
+  if (alloc_ws(s, std::min<int64_t>(n, 262144), false)) return FLINT_ERR_NOMEM;
   for (int64_t b = 0; b < n; b += s->cap) {
     const int64_t m = std::min<int64_t>(s->cap, n - b);
     if (net_forward(s, s->net[net], m, X + b * s->n_in, Yn + b * s->n_out, false, st)) return FLINT_ERR_CUDA;
@@ -493,7 +519,7 @@ int surrogate_predict(Surrogate* s, int net, int64_t n, const float* X, float* Y
 int surrogate_train_step(Surrogate* s, int net, int64_t n, const float* X, const float* Yt, float lr, double* loss_out,
                          cudaStream_t st) {
   if (net < 0 || net >= s->nnets || n <= 0) return FLINT_ERR_ARG;
-  if (alloc_ws(s, n)) return FLINT_ERR_NOMEM;
+  if (alloc_ws(s, n, true)) return FLINT_ERR_NOMEM;
   Net& nt = s->net[net];
   if (net_forward(s, nt, n, X, s->yhat, true, st)) return FLINT_ERR_CUDA;
   if (cudaMemsetAsync(s->loss, 0, 8, st)) return FLINT_ERR_CUDA;
@@ -557,47 +583,52 @@ int64_t surrogate_nparams(Surrogate* s) { return s->net[0].P; }
 
 int surrogate_advance(Surrogate* s, int64_t n, double* T, const double* p, double* Y, const double* dt,
                       const flint_reactor_opts& o, const flint_surrogate_gate* gate, int* status, int* nsteps,
-                      double* jsave, int jslots, double* metrics, cudaStream_t st) {
+                      double* jsave, int jslots, double* metrics, bool want_counts, cudaStream_t st) {
   s->last_accepted = s->last_rejected = 0;
   if (n <= 0) return 0;
-  const int64_t CH = 262144;
-  if (alloc_ws(s, std::min<int64_t>(n, CH))) return FLINT_ERR_NOMEM;
+  // inference in chunks of up to 1,048,576 cells; the rejected cells of all
+  // chunks are listed on the device and re-solved by one reactor launch whose
+  // cell count is read on the device (no host round trip before it)
+  const int64_t CH = 1048576;
+  if (alloc_ws(s, std::min<int64_t>(n, CH), false)) return FLINT_ERR_NOMEM;
+  if (!metrics && alloc_fb(s, n)) return FLINT_ERR_NOMEM;
   GateParams gp;
   gp.max_dT_resid = gate->max_dT_resid; gp.max_elem_resid = gate->max_elem_resid; gp.min_Y = gate->min_Y;
   gp.max_ens_dT = gate->max_ens_dT; gp.max_ens_dY = gate->max_ens_dY;
   gp.Tlo = gate->T_lo; gp.Thi = gate->T_hi; gp.lpl = gate->log10p_lo; gp.lph = gate->log10p_hi;
   gp.ldl = gate->log10dt_lo; gp.ldh = gate->log10dt_hi;
   const size_t psm = s->L.bytes + (size_t)(std::max(s->ne, 1) * s->ns) * sizeof(double);
-  cudaFuncSetAttribute(k_post, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)psm);
+  if (cudaFuncSetAttribute(k_post, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)psm)) return FLINT_ERR_CUDA;
+  if (cudaMemsetAsync(s->rej_count, 0, 8, st)) return FLINT_ERR_CUDA;
   for (int64_t b = 0; b < n; b += s->cap) {
     const int64_t m = std::min<int64_t>(s->cap, n - b);
     if (surrogate_features(s, m, T + b, p + b, Y + b * s->ns, dt + b, s->xf, st)) return FLINT_ERR_CUDA;
     if (net_forward(s, s->net[0], m, s->xf, s->yhat, false, st)) return FLINT_ERR_CUDA;
     if (s->nnets > 1 && net_forward(s, s->net[1], m, s->xf, s->yout2, false, st)) return FLINT_ERR_CUDA;
-    if (cudaMemsetAsync(s->rej_count, 0, 8, st)) return FLINT_ERR_CUDA;
     k_post<<<blocks_for(m, SURR_THREADS), SURR_THREADS, psm, st>>>(
         s->mimg, s->L, m, b, T, p, Y, dt, s->yhat, s->nnets > 1 ? s->yout2 : nullptr, s->ymean, s->ystd, s->proj,
         s->Bm, s->ne, gp, status, nsteps, s->rej_idx, s->rej_count, metrics ? metrics + b * 6 : nullptr);
     count_launch();
     if (cudaGetLastError()) return FLINT_ERR_CUDA;
-    if (metrics) continue;
-    unsigned long long nrej = 0;
-    if (cudaMemcpyAsync(&nrej, s->rej_count, 8, cudaMemcpyDeviceToHost, st) || cudaStreamSynchronize(st))
-      return FLINT_ERR_CUDA;
-    s->last_rejected += (int64_t)nrej;
-    s->last_accepted += m - (int64_t)nrej;
-    if (nrej == 0) continue;
-    k_gather<<<blocks_for((int64_t)nrej, 256), 256, 0, st>>>((int64_t)nrej, s->rej_idx, s->ns, T, p, Y, dt, s->cT,
-                                                             s->cp, s->cY, s->cdt);
-    count_launch();
-    cudaError_t e = launch_reactor(s->mimg, s->L, (int64_t)nrej, s->cT, s->cp, s->cY, s->cdt, o, s->cst, s->cns,
-                                   s->counter, jsave, jslots, st);
-    if (e) return FLINT_ERR_CUDA;
-    k_scatter<<<blocks_for((int64_t)nrej, 256), 256, 0, st>>>((int64_t)nrej, s->rej_idx, s->ns, T, Y, s->cT, s->cY,
-                                                              s->cst, s->cns, status, nsteps);
-    count_launch();
-    if (cudaGetLastError()) return FLINT_ERR_CUDA;
   }
+  if (metrics) return 0;
+  k_gather<<<blocks_for(n, 256), 256, 0, st>>>(s->rej_count, s->rej_idx, s->ns, T, p, Y, dt, s->cT, s->cp, s->cY,
+                                                s->cdt);
+  count_launch();
+  cudaError_t e = launch_reactor(s->mimg, s->L, n, s->cT, s->cp, s->cY, s->cdt, o, s->cst, s->cns, s->counter, jsave,
+                                 jslots, st, s->rej_count);
+  if (e) return FLINT_ERR_CUDA;
+  k_scatter<<<blocks_for(n, 256), 256, 0, st>>>(s->rej_count, s->rej_idx, s->ns, T, Y, s->cT, s->cY, s->cst, s->cns,
+                                                 status, nsteps);
+  count_launch();
+  if (cudaGetLastError()) return FLINT_ERR_CUDA;
+  s->last_accepted = s->last_rejected = -1;
+  if (!want_counts) return 0;   // stays asynchronous on st (and capturable in a CUDA graph)
+  unsigned long long nrej = 0;
+  if (cudaMemcpyAsync(&nrej, s->rej_count, 8, cudaMemcpyDeviceToHost, st) || cudaStreamSynchronize(st))
+    return FLINT_ERR_CUDA;
+  s->last_rejected = (int64_t)nrej;
+  s->last_accepted = n - (int64_t)nrej;
   return 0;
 }
 

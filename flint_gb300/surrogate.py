@@ -234,7 +234,11 @@ class Surrogate:
         native.check(self.L.flint_surrogate_state(self.h, net, buf.ctypes.data_as(_fp), C.byref(s), 0),
                      "flint_surrogate_state")
 
-    def advance(self, T, p, Y, dt, status=None, nsteps=None, gate=None, rtol=1e-8, atol=1e-14, max_steps=20000):
+    def advance(self, T, p, Y, dt, status=None, nsteps=None, gate=None, rtol=1e-8, atol=1e-14, max_steps=20000,
+                wait=True):
+        """Gated surrogate + fallback advance in place.  Returns (status, nsteps,
+        (accepted, rejected)); with wait=False the call does not wait for the
+        stream and the counts are None (the form a CUDA graph captures)."""
         import torch
         g = dict(self.gate, **(gate or {}))
         gs = SurrogateGate(*[float(g[k]) for k in GATE_KEYS])
@@ -244,11 +248,11 @@ class Surrogate:
             status = torch.empty(n, dtype=torch.int32, device=T.device)
         if nsteps is None:
             nsteps = torch.empty(n, dtype=torch.int32, device=T.device)
-        counts = (C.c_int64 * 2)()
+        counts = (C.c_int64 * 2)() if wait else None
         native.check(self.L.flint_surrogate_advance(self.h, n, _ptr(T), _ptr(p), _ptr(Y), _ptr(dt), C.byref(opts),
                                                     C.byref(gs), _ptr(status), _ptr(nsteps), counts, _stream()),
                      "flint_surrogate_advance")
-        return status, nsteps, (counts[0], counts[1])
+        return status, nsteps, ((counts[0], counts[1]) if wait else None)
 
     def evaluate(self, T, p, Y, dt):
         """Surrogate result for every cell (T, Y in place) and the gate metrics (n, 6)."""
@@ -407,12 +411,17 @@ def main():
     ap.add_argument("--seed", type=int, default=7)
     ap.add_argument("--margin", type=float, default=0.8)
     ap.add_argument("--lr", type=float, default=1e-3)
+    ap.add_argument("--config", default="c2", choices=["c2", "c5"],
+                    help="c2: 31 species, c3 reactor states; c5: 54 species, scale-up states")
     args = ap.parse_args()
     import torch
-    chem = Chemistry.from_config("c2")
+    chem = Chemistry.from_config(args.config)
+    states = mechgen.fuel_air_states
+    if args.config == "c5":
+        states = lambda n, mech, seed: mechgen.c5_states(n, mech, seed)   # noqa: E731
     t0 = time.time()
-    d = generate(chem, args.cells, seed=5000 + args.seed)
-    v = generate(chem, args.val, seed=6000 + args.seed)
+    d = generate(chem, args.cells, seed=5000 + args.seed, states=states)
+    v = generate(chem, args.val, seed=6000 + args.seed, states=states)
     tgen = time.time() - t0
     bath = chem.mech.index("N2")
     stats = fit_stats(d, bath)

@@ -289,7 +289,9 @@ int flint_surrogate_state(flint_surrogate_t s, int net, float* host, int64_t* st
  * Accepted cells: status FLINT_CELL_OK, nsteps 0; rejected cells are re-solved
  * by the BDF integrator (status FLINT_CELL_SURROGATE_REJECTED when it
  * succeeds, else its failure code; nsteps its step count).  counts (may be
- * NULL) gets {accepted, rejected}. */
+ * NULL) gets {accepted, rejected} and the call waits for `stream`; with
+ * counts NULL it returns without waiting (every operation stays on `stream`,
+ * so a call made after a first, sizing call can be captured in a CUDA graph). */
 int flint_surrogate_advance(flint_surrogate_t s, int64_t n, double* T, const double* p, double* Y,
                             const double* dt, const flint_reactor_opts* opts,
                             const flint_surrogate_gate* gate, int* status, int* nsteps,

@@ -182,3 +182,35 @@ def test_accepted_cells_conserve_elements_and_enthalpy():
         _, _, _, h0 = orc.wdot_batch(T0[i:i + 1], P[i:i + 1], Y0[i:i + 1])
         _, _, _, h1 = orc.wdot_batch(T1[i:i + 1], P[i:i + 1], Y1[i:i + 1])
         assert abs(h1[0] - h0[0]) <= 1e-8 * max(abs(h0[0]), 1e5)
+
+
+def test_advance_captured_in_cuda_graph():
+    """Without counts the advance never waits on the host: after a first (sizing)
+    call it is captured in a CUDA graph, and a replay reproduces the synchronous
+    call cell by cell (accepted and re-solved cells alike)."""
+    chem, sur = small_surrogate(seed=5, dy_scale=1e-4)
+    sur.gate.update({"max_dT_resid": 1e30, "max_elem_resid": 1e30, "min_Y": -1e-6, "T_lo": 0.0, "T_hi": 1e9,
+                     "log10p_lo": -1e9, "log10p_hi": 1e9, "log10dt_lo": -1e9, "log10dt_hi": 1e9})
+    T, p, Y, dt = _cells(chem, 1000, 47)
+    T0, Y0 = T.clone(), Y.clone()
+    st_ref, ns_ref, (acc, rej) = sur.advance(T, p, Y, dt)
+    torch.cuda.synchronize()
+    assert acc > 0 and rej > 0
+    Tg, Yg = T0.clone(), Y0.clone()
+    st = torch.empty_like(st_ref); ns = torch.empty_like(ns_ref)
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(s):                      # warm call on the capture stream
+        sur.advance(Tg, p, Yg, dt, status=st, nsteps=ns, wait=False)
+    torch.cuda.current_stream().wait_stream(s)
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, capture_error_mode="relaxed"):
+        sur.advance(Tg, p, Yg, dt, status=st, nsteps=ns, wait=False)
+    Tg.copy_(T0); Yg.copy_(Y0)
+    g.replay()
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(Tg.cpu().numpy(), T.cpu().numpy())
+    np.testing.assert_array_equal(Yg.cpu().numpy(), Y.cpu().numpy())
+    np.testing.assert_array_equal(st.cpu().numpy(), st_ref.cpu().numpy())
+    np.testing.assert_array_equal(ns.cpu().numpy(), ns_ref.cpu().numpy())
