@@ -262,6 +262,19 @@ int flint_rhs_native_batch(flint_mech_t h, int64_t n, const double* Z, double* F
   return e == cudaSuccess ? FLINT_OK : cuda_fail(e, "flint_rhs_native_batch");
 }
 
+int flint_cons2prim_batch(flint_mech_t h, int64_t n, int ndim, const double* cons, const double* T, double* prim,
+                          double* T_out, void* stream) {
+  if (!h) return fail(FLINT_ERR_ARG, "NULL handle");
+  if (n < 0) return fail(FLINT_ERR_ARG, "negative cell count");
+  if (ndim < 0 || ndim > 3) return fail(FLINT_ERR_ARG, "ndim must be 0..3");
+  if (!h->table) return fail(FLINT_ERR_MECH, "flint_cons2prim_batch needs a tabulated mechanism");
+  if (n == 0) return FLINT_OK;
+  if (!cons || !T || !prim) return fail(FLINT_ERR_ARG, "NULL array");
+  const int np = table_ns(h->table) + ndim + 1;
+  cudaError_t e = table_cons2prim(h->table, n, np, cons, T, prim, T_out, (cudaStream_t)stream);
+  return e == cudaSuccess ? FLINT_OK : cuda_fail(e, "flint_cons2prim_batch");
+}
+
 int flint_mech_destroy(flint_mech_t h) {
   if (!h) return FLINT_OK;
   if (h->table) table_destroy(h->table);

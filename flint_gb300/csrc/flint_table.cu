@@ -314,6 +314,90 @@ cudaError_t launch_general(const uint8_t* img, const TableLayout& L, const doubl
   return cudaGetLastError();
 }
 
+// ------------------------------------------------------------- cons2prim
+// cons2prim (Lib_ThermoTransport.f90:129-165) over a batch: prim = (rho_s, u_d,
+// p) from cons = (rho_s, rho u_d, rho E0) by the reference's Newton iteration on
+// the static energy, with its helpers f_Rtot (:217-230), f_cp (:251-271), H
+// (:40-54) and f_tab (:500-512) in their own operation order, uncontracted, so
+// that the oracle's -ffp-contract=off restatement is matched bit for bit.  One
+// thread per cell: every sum runs over the species in order, as the Fortran
+// loops do.  norm2 is the scaled sum of squares gfortran evaluates.
+struct C2PView {
+  const double* cpt;   // [row][nsp]
+  const double* ht;
+  const double* ri;
+  int ns, nsp, tmin, nrow;
+  __device__ double lerp_row(const double* tab, double T, int s) const {
+    const int Ti = (int)T;
+    int row = Ti - tmin;
+    row = row < 0 ? 0 : (row > nrow - 2 ? nrow - 2 : row);
+    const double* a = tab + (size_t)row * nsp + s;
+    return lerp_rn(a[0], a[nsp], __dsub_rn(T, (double)Ti));
+  }
+};
+
+__device__ inline double sum_rn(const double* x, int n) {
+  double s = 0.0;
+  for (int i = 0; i < n; ++i) s = __dadd_rn(s, x[i]);
+  return s;
+}
+
+__device__ inline double rtot_rn(const C2PView& v, const double* r) {
+  const double rho = sum_rn(r, v.ns);
+  double res = 0.0;
+  for (int s = 0; s < v.ns; ++s) res = __dadd_rn(res, __ddiv_rn(__dmul_rn(v.ri[s], r[s]), rho));
+  return res;
+}
+
+__global__ void k_cons2prim(C2PView v, int64_t n, int np, const double* __restrict__ cons,
+                            const double* __restrict__ Tg, double* __restrict__ prim, double* __restrict__ Tout) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double* c = cons + i * np;
+    double* pr = prim + i * np;
+    const int ns = v.ns, nui = ns, nuf = np - 2;
+    const double Rgas = rtot_rn(v, c);
+    const double rho = sum_rn(c, ns);
+    for (int s = 0; s < ns; ++s) pr[s] = c[s];
+    for (int d = nui; d <= nuf; ++d) pr[d] = __ddiv_rn(c[d], rho);
+    double scale = 1.0, ssq = 0.0;
+    for (int d = nui; d <= nuf; ++d) {
+      const double x = pr[d];
+      if (x != 0.0) {
+        const double a = fabs(x);
+        if (scale < a) {
+          const double q = __ddiv_rn(scale, a);
+          ssq = __dadd_rn(1.0, __dmul_rn(__dmul_rn(ssq, q), q));
+          scale = a;
+        } else {
+          const double q = __ddiv_rn(a, scale);
+          ssq = __dadd_rn(ssq, __dmul_rn(q, q));
+        }
+      }
+    }
+    const double vel = __dmul_rn(scale, __dsqrt_rn(ssq));
+    const double energy = __dsub_rn(__ddiv_rn(c[np - 1], rho), __dmul_rn(__dmul_rn(0.5, vel), vel));
+    double diff_en = 1.0e3, T = Tg[i];
+    int it = 1;
+    while (fabs(__ddiv_rn(diff_en, energy)) >= 1e-6 && it <= 20) {
+      const double p_it = __dmul_rn(__dmul_rn(rho, Rgas), T);
+      double cp = 0.0;
+      for (int s = 0; s < ns; ++s) cp = __dadd_rn(cp, __dmul_rn(__ddiv_rn(c[s], rho), v.lerp_row(v.cpt, T, s)));
+      const double cv = __dsub_rn(cp, Rgas);
+      // E(p, rhoi) = H(p, rhoi) - p / sum(rhoi); H re-derives T = p / (Rtot rho)
+      const double rho_h = sum_rn(c, ns), R_h = rtot_rn(v, c);
+      const double Th = __ddiv_rn(p_it, __dmul_rn(R_h, rho_h));
+      double h = 0.0;
+      for (int s = 0; s < ns; ++s) h = __dadd_rn(h, __ddiv_rn(__dmul_rn(v.lerp_row(v.ht, Th, s), c[s]), rho_h));
+      const double e_it = __dsub_rn(h, __ddiv_rn(p_it, sum_rn(c, ns)));
+      diff_en = fabs(__dsub_rn(e_it, energy));
+      T = __dadd_rn(T, __ddiv_rn(__dsub_rn(energy, e_it), cv));
+      ++it;
+    }
+    pr[np - 1] = __dmul_rn(__dmul_rn(rho, Rgas), T);
+    if (Tout) Tout[i] = T;
+  }
+}
+
 // ------------------------------------------------------------ handle glue
 struct TableHandle {
   TableLayout L;
@@ -353,6 +437,23 @@ void table_destroy(void* p) {
 
 int table_ns(void* p) { return static_cast<TableHandle*>(p)->L.ns; }
 int table_nr(void* p) { return static_cast<TableHandle*>(p)->L.nr; }
+
+cudaError_t table_cons2prim(void* p, int64_t n, int np, const double* cons, const double* T, double* prim,
+                            double* Tout, cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  auto* th = static_cast<TableHandle*>(p);
+  const TableLayout& L = th->L;
+  C2PView v;
+  v.cpt = th->dtabs + L.g_cp; v.ht = th->dtabs + L.g_h;
+  v.ri = reinterpret_cast<const double*>(th->dimg + L.o_ri);
+  v.ns = L.ns; v.nsp = L.nsp; v.tmin = L.tmin; v.nrow = L.nrow_t;
+  int64_t blocks = (n + 127) / 128;
+  const int64_t cap = (int64_t)device_sms() * 16;
+  if (blocks > cap) blocks = cap;
+  k_cons2prim<<<(unsigned)blocks, 128, 0, st>>>(v, n, np, cons, T, prim, Tout);
+  count_launch();
+  return cudaGetLastError();
+}
 
 cudaError_t table_run(void* p, int64_t n, int rhs, const double* roi, const double* T, double* out, cudaStream_t st) {
   auto* th = static_cast<TableHandle*>(p);

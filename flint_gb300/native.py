@@ -113,6 +113,7 @@ def lib():
     L.flint_selftest_exp.argtypes = [vp, i64, vp, vp, vp]
     L.flint_mech_create_tables.argtypes = [C.POINTER(TableDesc), C.POINTER(vp)]
     L.flint_rhs_native_batch.argtypes = [vp, i64, vp, vp, vp]
+    L.flint_cons2prim_batch.argtypes = [vp, i64, C.c_int, vp, vp, vp, vp, vp]
     L.flint_wdot_batch_host.argtypes = [vp, i64, C.c_int, vp, vp, vp, vp, vp, vp]
     L.flint_wdot_jac_batch_host.argtypes = [vp, i64, C.c_int, vp, vp, vp, vp, vp]
     L.flint_reactor_advance_host.argtypes = [vp, i64, vp, vp, vp, vp, C.POINTER(ReactorOpts), vp, vp]

@@ -327,3 +327,18 @@ class Tables:
         native.check(self.L.flint_rhs_native_batch(self.h, Z.shape[0], C.c_void_p(Z.data_ptr()),
                                                    C.c_void_p(F.data_ptr()), s), "flint_rhs_native_batch")
         return F
+
+    def cons2prim(self, cons, T, prim=None, T_out=None):
+        """cons2prim over N cells: cons (N, ns+ndim+1) = (rho_i, rho u, rho E0) and
+        the Newton start T (N,) -> prim (N, ns+ndim+1) = (rho_i, u, p), last T."""
+        import torch
+        ndim = cons.shape[1] - self.ns - 1
+        if prim is None:
+            prim = torch.empty_like(cons)
+        if T_out is None:
+            T_out = torch.empty_like(T)
+        s = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+        native.check(self.L.flint_cons2prim_batch(self.h, cons.shape[0], ndim, C.c_void_p(cons.data_ptr()),
+                                                  C.c_void_p(T.data_ptr()), C.c_void_p(prim.data_ptr()),
+                                                  C.c_void_p(T_out.data_ptr()), s), "flint_cons2prim_batch")
+        return prim, T_out

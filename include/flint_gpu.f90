@@ -53,6 +53,15 @@ module FLINT_GPU
       integer(c_int64_t), value :: n
     end function
 
+    ! cons2prim over ncells on device arrays (cons, prim: (ns+ndim+1, ncells))
+    integer(c_int) function flint_cons2prim_batch(mech, n, ndim, cons, temp, prim, temp_out, stream) &
+        bind(C, name='flint_cons2prim_batch')
+      import :: c_int, c_int64_t, c_ptr
+      type(c_ptr), value :: mech, cons, temp, prim, temp_out, stream
+      integer(c_int64_t), value :: n
+      integer(c_int), value :: ndim
+    end function
+
     integer(c_int) function flint_wdot_batch_host(mech, n, layout, temp, p, Y, wdot, cp, h) &
         bind(C, name='flint_wdot_batch_host')
       import :: c_int, c_int64_t, c_double, c_ptr

@@ -190,6 +190,16 @@ int flint_chemistry_source_batch(flint_mech_t mech, int64_t n, double* roi,
  * outside the thermo table or NaN, as the reference returns.  Tabulated handles. */
 int flint_rhs_native_batch(flint_mech_t mech, int64_t n, const double* Z, double* F, void* stream);
 
+/* cons2prim(cons, T) over N cells (Lib_ThermoTransport.f90:129-165):
+ * cons, prim cell-major, np = ns + ndim + 1 per cell; cons = (rho_1..rho_ns,
+ * rho u_1..rho u_ndim, rho E0), prim = (rho_1..rho_ns, u_1..u_ndim, p).  T is
+ * the Newton start per cell (the caller's previous temperature, as in the
+ * reference); T_out (may be NULL) gets the last iterate.  The reference's
+ * iteration: at most 20 Newton steps on the static energy from the tabulated
+ * h and cp, stopping at a relative energy change below 1e-6.  Tabulated handles. */
+int flint_cons2prim_batch(flint_mech_t mech, int64_t n, int ndim, const double* cons, const double* T,
+                          double* prim, double* T_out, void* stream);
+
 /* wdot and the analytic Jacobian of the constant-pressure reactor right-hand
  * side, J = d(dY/dt, dT/dt)/d(Y, T), (ns+1)^2 per cell stored column-major
  * per cell: jac[cell*(ns+1)^2 + col*(ns+1) + row] (Fortran (ns+1, ns+1, N)). */

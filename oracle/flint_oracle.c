@@ -885,3 +885,91 @@ void orc_rhs_native_batch(const orc_table_mech* m, int64_t n, const double* Z, d
 #pragma omp parallel for schedule(static)
   for (int64_t i = 0; i < n; ++i) orc_rhs_native(m, nz, Z + i * nz, F + i * nz);
 }
+
+/* ------------------------------------------------------------- cons2prim */
+/* norm2 as gfortran evaluates it: a scaled sum of squares (overflow-safe). */
+static double norm2_f(int n, const double* x) {
+  double scale = 1.0, ssq = 0.0;
+  for (int i = 0; i < n; ++i) {
+    if (x[i] != 0.0) {
+      double a = fabs(x[i]);
+      if (scale < a) {
+        double v = scale / a;
+        ssq = 1.0 + ssq * v * v;
+        scale = a;
+      } else {
+        double v = a / scale;
+        ssq = ssq + v * v;
+      }
+    }
+  }
+  return scale * sqrt(ssq);
+}
+
+static double sum_f(int n, const double* x) {
+  double s = 0.0;
+  for (int i = 0; i < n; ++i) s = s + x[i];
+  return s;
+}
+
+/* f_Rtot (Lib_ThermoTransport.f90:217-230): sum_s Ri_s rhoi_s / rho. */
+static double rtot_f(const orc_table_mech* m, const double* r) {
+  double rho = sum_f(m->ns, r), res = 0.0;
+  for (int s = 0; s < m->ns; ++s) res = res + (m->runiv / m->wm[s]) * r[s] / rho;
+  return res;
+}
+
+/* f_cp (Lib_ThermoTransport.f90:251-271): sum_s rhoi_s / rho * cp_s(T). */
+static double cp_f(const orc_table_mech* m, const double* r, double T, double rho) {
+  int nrows = m->tmax - m->tmin + 1, Ti = (int)T;
+  double Tdiff = T - Ti, res = 0.0;
+  for (int s = 0; s < m->ns; ++s) res = res + r[s] / rho * lerp_tab(m->cp_tab, m->tmin, nrows, s, Ti, Tdiff);
+  return res;
+}
+
+/* H (Lib_ThermoTransport.f90:40-54) with f_tab's T = p / (Rtot rho) (:500-512). */
+static double h_f(const orc_table_mech* m, double p, const double* r) {
+  int nrows = m->tmax - m->tmin + 1;
+  double rho = sum_f(m->ns, r), Rgas = rtot_f(m, r), res = 0.0;
+  double T = p / (Rgas * rho);
+  int Ti = (int)T;
+  double Tdiff = T - Ti;
+  for (int s = 0; s < m->ns; ++s) res = res + lerp_tab(m->h_tab, m->tmin, nrows, s, Ti, Tdiff) * r[s] / rho;
+  return res;
+}
+
+/* cons2prim (Lib_ThermoTransport.f90:129-165): cons = (rho_s, rho u_d, rho E0),
+ * prim = (rho_s, u_d, p); T is the Newton start and *Tout the last iterate. */
+void orc_cons2prim(const orc_table_mech* m, int np, const double* cons, double T, double* prim,
+                   double* Tout, int* iters) {
+  int ns = m->ns, nui = ns, nuf = np - 2;   /* 0-based: velocity slots nui..nuf */
+  double rhoi[MAXNS];
+  for (int s = 0; s < ns; ++s) rhoi[s] = cons[s];
+  double Rgas = rtot_f(m, rhoi);
+  double rho = sum_f(ns, rhoi);
+  for (int s = 0; s < ns; ++s) prim[s] = rhoi[s];
+  for (int d = nui; d <= nuf; ++d) prim[d] = cons[d] / rho;
+  double vel = norm2_f(nuf - nui + 1, prim + nui);
+  double energy = cons[np - 1] / rho - 0.5 * vel * vel;
+  double diff_en = 1.0e3, T_iter = T;
+  int it = 1;
+  while (fabs(diff_en / energy) >= 1e-6 && it <= 20) {
+    double p_iter = rho * Rgas * T_iter;
+    double cv_iter = cp_f(m, rhoi, T_iter, rho) - Rgas;
+    double energy_iter = h_f(m, p_iter, rhoi) - p_iter / sum_f(ns, rhoi);
+    diff_en = fabs(energy_iter - energy);
+    T_iter = T_iter + (energy - energy_iter) / cv_iter;
+    it = it + 1;
+  }
+  prim[np - 1] = rho * Rgas * T_iter;
+  if (Tout) *Tout = T_iter;
+  if (iters) *iters = it - 1;
+}
+
+void orc_cons2prim_batch(const orc_table_mech* m, int64_t n, int np, const double* cons,
+                         const double* T, double* prim, double* Tout, int nthreads) {
+  set_threads(nthreads);
+#pragma omp parallel for schedule(static)
+  for (int64_t i = 0; i < n; ++i)
+    orc_cons2prim(m, np, cons + i * np, T[i], prim + i * np, Tout ? Tout + i : NULL, NULL);
+}

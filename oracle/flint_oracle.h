@@ -73,6 +73,13 @@ void orc_general_batch(const orc_table_mech* m, int64_t n, const double* roi, co
 void orc_rhs_native_batch(const orc_table_mech* m, int64_t n, const double* Z, double* F,
                           int nthreads);
 
+/* cons2prim(cons, T), Lib_ThermoTransport.f90:129-165: prim = (rho_s, u_d, p)
+ * from cons = (rho_s, rho u_d, rho E0); np = ns + ndim + 1 per cell. */
+void orc_cons2prim(const orc_table_mech* m, int np, const double* cons, double T, double* prim,
+                   double* Tout, int* iters);
+void orc_cons2prim_batch(const orc_table_mech* m, int64_t n, int np, const double* cons,
+                         const double* T, double* prim, double* Tout, int nthreads);
+
 int orc_max_threads(void);
 
 #ifdef __cplusplus

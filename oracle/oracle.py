@@ -43,6 +43,7 @@ def lib():
         td = C.POINTER(TableDesc)
         L.orc_general_batch.argtypes = [td, i64, vp, vp, vp, C.c_int]
         L.orc_rhs_native_batch.argtypes = [td, i64, vp, vp, C.c_int]
+        L.orc_cons2prim_batch.argtypes = [td, i64, C.c_int, vp, vp, vp, vp, C.c_int]
         _lib = L
     return _lib
 
@@ -139,3 +140,13 @@ class TableOracle:
         F = np.zeros_like(Z)
         self.L.orc_rhs_native_batch(C.byref(self.desc), Z.shape[0], _vp(Z), _vp(F), nthreads)
         return F
+
+    def cons2prim(self, cons, T, nthreads=0):
+        """cons (n, ns + ndim + 1) -> (prim (same shape), last Newton T (n,))."""
+        cons = np.ascontiguousarray(cons, dtype=np.float64)
+        T = np.ascontiguousarray(T, dtype=np.float64)
+        prim = np.zeros_like(cons)
+        Tout = np.zeros_like(T)
+        self.L.orc_cons2prim_batch(C.byref(self.desc), cons.shape[0], cons.shape[1], _vp(cons), _vp(T), _vp(prim),
+                                   _vp(Tout), nthreads)
+        return prim, Tout
