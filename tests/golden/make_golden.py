@@ -13,6 +13,8 @@ except unit conversion of YAML rate parameters into the IR):
 * tests/golden/pelucchi_thermo.json sampled rows of test/Pelucchi/INPUT/thermo.dat
 * tests/golden/mech_pelucchi.json  the Pelucchi YAML as a mechanism IR
 * tests/golden/wd_info.json        WD chemistry-info.txt stoichiometry + phase.txt
+* tests/golden/mech_<name>.json    the other in-tree NASA-7 mechanisms (Ecker, Smooke,
+                                   TSR-CDF-13, TSR-GP-24, TSR-Rich-31, Troyes, ZK) as IR
 * flint_gb300/data/mech_c1.json    the 2-step CH4/air mechanism: WD reactions 1-2
                                    (test/WD/INPUT/WD.yaml) with NASA-7 data of CH4, O2,
                                    CO, CO2, H2O (TSR-Rich-31.yaml) and N2 (troyes.yaml),
@@ -61,6 +63,13 @@ def sample_rows(rows, temps):
         assert rows[i, 0] == T, (T, rows[i, 0])
         out.append(rows[i].tolist())
     return out
+
+
+# the reference's in-tree mechanisms whose YAML uses NASA-7 thermo (WD and Cross
+# use NASA-9, CORIA a rate form outside the IR)
+INTREE = [("Ecker", "ecker.yaml"), ("Smooke", "smooke.yaml"), ("TSR-CDF-13", "TSR-CDF-13.yaml"),
+          ("TSR-GP-24", "TSR-GP-24.yaml"), ("TSR-Rich-31", "TSR-Rich-31.yaml"), ("Troyes", "troyes.yaml"),
+          ("ZK", "ZK.yaml")]
 
 
 def main(ref):
@@ -149,6 +158,13 @@ def main(ref):
     json.dump({"source": "C/H/O/N species of test/*/INPUT/*.yaml (TSR-Rich-31 order first)",
                "species": [{"name": n, "composition": pool[n]} for n in order]},
               open(os.path.join(data, "chon_species.json"), "w"), indent=1)
+    # ---- in-tree mechanisms with NASA-7 thermo, as IR -------------------------
+    for sub, yname in INTREE:
+        d = os.path.join(test, sub, "INPUT")
+        mi = M.from_yaml(os.path.join(d, yname), phase_mw=M.read_phase_txt(os.path.join(d, "phase.txt")))
+        with open(os.path.join(gold, "mech_" + os.path.splitext(yname)[0].lower().replace("-", "_") + ".json"),
+                  "w") as f:
+            f.write(mi.to_json())
     print("wrote fixtures")
 
 

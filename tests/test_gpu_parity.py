@@ -278,3 +278,71 @@ def test_reactor_c5_54_species():
     for Tv, Yv in ((Tg, Yg), (T_o, Y_o)):
         assert np.max(np.abs(Tv - T_x) / T_x) < 1e-5 and np.abs(Yv - Y_x).max() < 1e-6
     assert abs(nst.cpu().numpy().sum() / ns_o.sum() - 1.0) < 0.05
+
+
+INTREE = ["ecker", "smooke", "troyes", "tsr_cdf_13", "tsr_gp_24", "tsr_rich_31", "zk"]
+
+
+@pytest.mark.parametrize("name", INTREE)
+def test_intree_mechanisms_wdot_jacobian_generated(name):
+    """The reference's own NASA-7 mechanisms (test/*/INPUT/*.yaml, as IR):
+    data-driven wdot and Jacobian, and the generated per-mechanism kernel."""
+    import os
+    from flint_gb300.ytf_cuda import GeneratedMechanism
+    mech = Mechanism.load(os.path.join(os.path.dirname(__file__), "golden", f"mech_{name}.json"))
+    T, p, Y = mechgen.c2_states(1000, mech, seed=31)
+    T = np.clip(T, 300.0, 3400.0)
+    orc = Oracle(mech)
+    w_o, ws_o, cp_o, h_o = orc.wdot_batch(T, p, Y)
+    _, J_o, Js_o = orc.wdot_jac_batch(T, p, Y)
+    chem = Chemistry(mech)
+    Tt, pt, Yt = cuda(T, p, Y)
+    w, _, _ = chem.wdot(Tt, pt, Yt)
+    _, J = chem.wdot_jac(Tt, pt, Yt)
+    wg, cpg, hg = GeneratedMechanism(mech).wdot(Tt, pt, Yt)
+    torch.cuda.synchronize()
+    assert wdot_err(w.cpu().numpy().ravel(), w_o, ws_o) < RTOL_WDOT
+    assert wdot_err(wg.cpu().numpy().ravel(), w_o, ws_o) < RTOL_WDOT
+    np.testing.assert_allclose(cpg.cpu().numpy(), cp_o, rtol=1e-13)
+    err = np.abs(J.cpu().numpy().ravel() - J_o) / (Js_o + 1e-300)
+    assert err.max() < RTOL_WDOT, err.max()
+
+
+def test_reactor_tsr_rich_31():
+    """A real 31-species / 197-reaction mechanism (TSR-Rich-31, 12 Troe) in the reactor."""
+    import os
+    mech = Mechanism.load(os.path.join(os.path.dirname(__file__), "golden", "mech_tsr_rich_31.json"))
+    T, p, Y, dt = tsr_rich_states(mech, 96, 71)
+    orc = Oracle(mech)
+    T_o, Y_o, st_o, ns_o = orc.reactor_advance(T, p, Y, dt, reactor_opts())
+    T_x, Y_x, st_x, _ = orc.reactor_advance(T, p, Y, dt, reactor_opts(rtol=1e-12, atol=1e-18, max_steps=400000))
+    chem = Chemistry(mech)
+    Tt, pt, Yt, dtt = cuda(T, p, Y, dt)
+    st, nst = chem.reactor_advance(Tt, pt, Yt, dtt)
+    torch.cuda.synchronize()
+    st = st.cpu().numpy()
+    assert (st == 0).all() and (st_o == 0).all() and (st_x == 0).all()
+    Tg, Yg = Tt.cpu().numpy(), Yt.cpu().numpy()
+    for Tv, Yv in ((Tg, Yg), (T_o, Y_o)):
+        assert np.max(np.abs(Tv - T_x) / T_x) < 5e-5 and np.abs(Yv - Y_x).max() < 2e-5
+    assert abs(nst.cpu().numpy().sum() / ns_o.sum() - 1.0) < 0.05
+
+
+def tsr_rich_states(mech, n, seed):
+    """CH4/O2 at phi 0.5-2 diluted by 30-50 % CO2 and H2O (the mechanism has no N2)."""
+    rng = np.random.default_rng(seed)
+    names = [sp.name for sp in mech.species]
+    X = np.zeros((n, mech.ns))
+    phi = rng.uniform(0.5, 2.0, n)
+    dil = rng.uniform(0.3, 0.5, n)
+    X[:, names.index("CH4")] = phi / (phi + 2.0) * (1 - dil)
+    X[:, names.index("O2")] = 2.0 / (phi + 2.0) * (1 - dil)
+    X[:, names.index("CO2")] = 0.5 * dil
+    X[:, names.index("H2O")] = 0.5 * dil
+    W = np.array([sp.mw for sp in mech.species])
+    Y = X * W
+    Y /= Y.sum(1, keepdims=True)
+    T = rng.uniform(1300.0, 1900.0, n)
+    p = rng.uniform(1.0, 20.0, n) * 101325.0
+    dt = 10.0 ** rng.uniform(-5.0, -3.0, n)
+    return T, p, Y, dt
