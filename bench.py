@@ -44,7 +44,22 @@ METRIC = "cell-steps/s on 1 GB300: surrogate+fallback vs plain FP64 at stated T/
 # kernel on the 31-species mechanism, from ncu counts of the standalone
 # source-term / Jacobian kernels (profiles/fp64_ops_per_event.md) plus the
 # dense LU counts of a 32x32 system.
-FP64_OPS = {"rhs": 18500.0, "jac": 36000.0, "lu": 22900.0, "solve": 2100.0}
+# FP64 FLOPs per kinetics evaluation (2 x DFMA + DADD + DMUL thread instructions,
+# predicated on) of the warp kernels, per state: k_wdot_warp<0> for one RHS and
+# k_wdot_warp<1> for one Jacobian, from ncu on the c2-wdot / c2-wdotjac and
+# c5-wdot / c5-wdotjac workloads (profiles/fp64_ops_per_state.md).
+KINETICS_FLOPS = {"synthetic-31sp-160r": {"rhs": 18500.0, "jac": 36000.0},
+                  "synthetic-54sp-320r": {"rhs": 37000.0, "jac": 72000.0}}
+
+
+def fp64_ops(ev, ns, mech_name="synthetic-31sp-160r"):
+    """FP64 FLOPs of a reactor launch from its event counters: kinetics per RHS
+    and Jacobian evaluation (measured per state), (2/3) n^3 per LU factorization
+    and 2 n^2 per LU solve (n = ns + 1)."""
+    k = KINETICS_FLOPS[mech_name]
+    n = ns + 1
+    return (ev["rhs"] * k["rhs"] + ev["jac"] * k["jac"] + ev["lu"] * (2.0 / 3.0) * n ** 3
+            + ev["newton"] * 2.0 * n * n)
 
 
 def dist_env():
@@ -255,8 +270,7 @@ def run_ours(args):
 
     # ---- roofline: FP64 pipe ------------------------------------------------
     s = stats[-1]
-    ops = (s["rhs"] * FP64_OPS["rhs"] + s["jac"] * FP64_OPS["jac"] + s["lu"] * FP64_OPS["lu"]
-           + s["newton"] * FP64_OPS["solve"])
+    ops = fp64_ops(s, chem.ns, chem.mech.name)
     peak = chem_peak_fp64()
     achieved = ops / t_step / 1e12
     roof = {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
@@ -318,11 +332,39 @@ def run_surrogate(args):
     stream = torch.cuda.current_stream()
     counts = {}
 
-    def step():
+    def direct():
         Td.copy_(Td0)
         Yd.copy_(Yd0)
         _, _, c = sur.advance(Td, pd, Yd, dtd, status=st, nsteps=nst)
         counts["c"] = c
+
+    def async_step():
+        Td.copy_(Td0)
+        Yd.copy_(Yd0)
+        sur.advance(Td, pd, Yd, dtd, status=st, nsteps=nst, wait=False)
+
+    step = direct
+    graph_note = "not used"
+    if not args.no_graph:
+        # one step (input copy + surrogate + fallback) captured as a CUDA graph
+        try:
+            side = torch.cuda.Stream()
+            side.wait_stream(torch.cuda.current_stream())
+            with torch.cuda.stream(side):
+                async_step()
+            torch.cuda.current_stream().wait_stream(side)
+            torch.cuda.synchronize()
+            graph = torch.cuda.CUDAGraph()
+            lc = kernel_launches()
+            with torch.cuda.graph(graph, capture_error_mode="relaxed"):
+                async_step()
+            torch.cuda.synchronize()
+            per_replay = kernel_launches() - lc
+            step = graph.replay
+            graph_note = "each step one CUDA graph replay"
+        except Exception as ex:   # report it; the timed path is then the direct calls
+            graph_note = f"capture failed ({type(ex).__name__}: {ex}); direct calls"
+            step = direct
 
     for _ in range(args.warmup):
         step()
@@ -342,6 +384,9 @@ def run_surrogate(args):
     torch.cuda.synchronize()
     clk = clocks.stop()
     launches = kernel_launches() - l0
+    if step is not direct:
+        counts["c"] = sur.counts()
+        launches = per_replay * args.steps   # the library kernels captured in one replay
     fb = reactor_stats(chem)
     t_sur = statistics.mean(times)
     if ws > 1:
@@ -389,8 +434,20 @@ def run_surrogate(args):
         tt = torch.tensor([t_e2e], device=dev, dtype=torch.float64)
         torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
         t_e2e = float(tt.item())
-    ops = (fb["rhs"] * FP64_OPS["rhs"] + fb["jac"] * FP64_OPS["jac"] + fb["lu"] * FP64_OPS["lu"]
-           + fb["newton"] * FP64_OPS["solve"])
+    # ---- the dominant kernel alone: the fallback reactor on the rejected cells
+    ridx = torch.nonzero((sts != 0) | (nsts != 0)).squeeze(1)
+    Tf, Yf = Td0[ridx].contiguous(), Yd0[ridx].contiguous()
+    pf, dtf = pd[ridx].contiguous(), dtd[ridx].contiguous()
+    stf = torch.empty(ridx.numel(), dtype=torch.int32, device=dev)
+    nsf = torch.empty(ridx.numel(), dtype=torch.int32, device=dev)
+    flush.zero_()
+    e0 = torch.cuda.Event(enable_timing=True); e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    chem.reactor_advance(Tf, pf, Yf, dtf, status=stf, nsteps=nsf)
+    e1.record(stream); e1.synchronize()
+    t_fb = e0.elapsed_time(e1) / 1e3
+    fbk = reactor_stats(chem)
+    ops = fp64_ops(fbk, chem.ns, chem.mech.name)
     peak = chem_peak_fp64()
     line = {"metric": METRIC, "value": n * ws / t_sur, "unit": "cell-steps/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_sur * 1e3, "higher_is_better": True, "scaling": "weak",
@@ -399,7 +456,7 @@ def run_surrogate(args):
             "config": {"workload": "reactor-c4: surrogate+fallback, 31sp/160r, 1048576 cells, rtol 1e-8 atol 1e-14",
                        "cells_per_gpu": n, "path": "surrogate + FP64 BDF fallback",
                        "network": "MLP 33-256-256-256-256-32 GELU x2 (ensemble), bf16 mma.sync, fp32 accumulate",
-                       "l2": "flushed (256 MiB write) between timed steps"},
+                       "l2": "flushed (256 MiB write) between timed steps", "cuda_graph": graph_note},
             "surrogate": {"accepted": int(acc), "rejected": int(rej), "accept_frac": acc / max(acc + rej, 1),
                           "plain_fp64_cell_steps_per_s": plain, "plain_sample_cells": m,
                           "speedup_vs_plain": (n / t_sur) / plain,
@@ -410,11 +467,12 @@ def run_surrogate(args):
             "e2e": {"value": n * ws / t_e2e, "unit": "cell-steps/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
             "gpu_launches": launches, "clocks": clk,
-            "roofline": {"bound": "fp64", "kernel": "k_reactor (fallback cells)",
-                         "achieved": ops / t_sur / 1e12 if ops else 0.0, "peak": peak, "unit": "TFLOP/s",
-                         "frac": (ops / t_sur / 1e12) / peak if (peak and ops) else None, "traffic": None,
+            "roofline": {"bound": "fp64", "kernel": "k_reactor (the fallback: rejected cells, timed alone)",
+                         "achieved": ops / t_fb / 1e12, "peak": peak, "unit": "TFLOP/s",
+                         "frac": (ops / t_fb / 1e12) / peak if peak else None, "traffic": None,
                          "peak_source": "DFMA probe kernel measured in this run (MEASURED_PEAKS.json has no FP64 figure)",
-                         "events_per_launch": fb,
+                         "kernel_seconds": t_fb, "share_of_step": t_fb / t_sur, "fallback_cells": int(ridx.numel()),
+                         "events_per_launch": fbk, "ops_per_launch": ops,
                          "plain_leg": {"events": plain_stats, "seconds": t_plain}}}
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(chem.mech, T0, p0, Y0, dt0)
@@ -426,7 +484,9 @@ def run_surrogate(args):
 
 def run_kernel_workload(args):
     """Source-term workloads: c1-wdot (65,536 states, 2-step CH4/air: wdot, cp, h)
-    and c2-wdotjac (1,048,576 states, 31 species: wdot + 32x32 Jacobian).
+    and c2-wdotjac (1,048,576 states, 31 species: wdot + 32x32 Jacobian); c5-wdot /
+    c5-wdotjac the same on the 54-species mechanism (1,048,576 states: the 55x55
+    Jacobians of 1 M states are 25 GB)
     Metric states/s, device-timed, L2 flushed between steps."""
     import torch
     from flint_gb300 import mechgen
@@ -438,13 +498,13 @@ def run_kernel_workload(args):
         chem = Chemistry.from_config("c1")
     else:
         n = args.cells or 1048576
-        chem = Chemistry.from_config("c2")
+        chem = Chemistry.from_config("c5" if args.workload.startswith("c5") else "c2")
         T, p, Y = mechgen.c2_states(n, chem.mech)
     Td, pd, Yd = (torch.from_numpy(a).to(dev) for a in (T, p, Y))
     w = torch.empty_like(Yd)
     cp, h = torch.empty_like(Td), torch.empty_like(Td)
     jac = torch.empty((n, chem.ns + 1, chem.ns + 1), dtype=torch.float64, device=dev) \
-        if args.workload == "c2-wdotjac" else None
+        if args.workload.endswith("wdotjac") else None
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
     stream = torch.cuda.current_stream()
     gen = None
@@ -502,7 +562,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cells", type=int, default=None)
     ap.add_argument("--workload", default="reactor",
-                    choices=["reactor", "reactor-c5", "c1-wdot", "c2-wdot", "c2-wdotjac"])
+                    choices=["reactor", "reactor-c5", "c1-wdot", "c2-wdot", "c2-wdotjac", "c5-wdot", "c5-wdotjac"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--generated", action="store_true",
                     help="source-term workloads: run the per-mechanism generated kernel (ytf_cuda)")
@@ -510,6 +570,7 @@ def main():
     ap.add_argument("--path", default="auto", choices=["auto", "surrogate", "plain"],
                     help="surrogate+fallback (headline, needs the trained checkpoint) or the plain integrator")
     ap.add_argument("--checkpoint", default=SURROGATE_CKPT)
+    ap.add_argument("--no-graph", action="store_true", help="surrogate path: direct calls instead of a CUDA graph")
     args = ap.parse_args()
     if args.workload == "reactor-c5":
         args.cells = args.cells or CELLS

@@ -504,6 +504,12 @@ int flint_surrogate_advance(flint_surrogate_t s, int64_t n, double* T, const dou
   return FLINT_OK;
 }
 
+int flint_surrogate_counts(flint_surrogate_t s, int64_t* counts) {
+  if (!s || !counts) return fail(FLINT_ERR_ARG, "NULL argument");
+  int rc = surrogate_read_counts(s->s, &counts[0], &counts[1]);
+  return rc ? fail(rc, "flint_surrogate_counts: %s", cudaGetErrorString(cudaGetLastError())) : FLINT_OK;
+}
+
 int flint_surrogate_evaluate(flint_surrogate_t s, int64_t n, double* T, const double* p, double* Y,
                              const double* dt, const flint_surrogate_gate* gate, double* metrics, void* stream) {
   if (!s || !gate || !metrics) return fail(FLINT_ERR_ARG, "NULL argument");

@@ -57,6 +57,7 @@ int surrogate_advance(Surrogate* s, int64_t n, double* T, const double* p, doubl
                       const flint_reactor_opts& o, const flint_surrogate_gate* gate, int* status, int* nsteps,
                       double* jsave, int jslots, double* metrics, bool want_counts, cudaStream_t st);
 void surrogate_counts(Surrogate* s, int64_t* acc, int64_t* rej);
+int surrogate_read_counts(Surrogate* s, int64_t* acc, int64_t* rej);
 
 // tabulated (reference general-loop) path, flint_table.cu
 int table_create(const flint_table_desc* d, void** out, std::string& err);

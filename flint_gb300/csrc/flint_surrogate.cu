@@ -7,7 +7,7 @@
 //     onto the null space of the element matrix (mass fractions:
 //     sum_k a_ek dY_k / W_k = 0; total mass follows) by least squares over the
 //     species not clipped at zero, clipping negatives and repeating
-//     (an active-set projection, at most 4 passes);
+//     (an active-set projection, at most 8 passes);
 //   * energy conservation (adiabatic, constant p): T1 solves h(T1, Y1) = h(T0, Y0)
 //     by Newton on the NASA-7 enthalpy, started from the network's T0 + dT;
 //   (no clipping afterwards: a mass fraction below the gate's min_Y rejects
@@ -37,6 +37,7 @@ namespace flint {
 
 constexpr int MAXL = 8;
 constexpr int MAXS = 64;   // species of a surrogate mechanism (the reactor's limit, 63)
+constexpr int NPASS = 8;   // active-set passes of the conservative projection
 constexpr int SURR_THREADS = 128;
 
 struct Net {
@@ -75,6 +76,7 @@ struct Surrogate {
   double *cT = nullptr, *cp = nullptr, *cY = nullptr, *cdt = nullptr;
   int *cst = nullptr, *cns = nullptr;
   int64_t last_accepted = 0, last_rejected = 0, last_fallback_steps = 0;
+  int64_t last_n = 0;       // cells of the last advance (its rejected count stays on the device)
 };
 
 // ------------------------------------------------------------------ kernels
@@ -161,12 +163,13 @@ k_post(const uint8_t* __restrict__ img, ImageLayout L, int64_t n, int64_t base, 
     }
     // conservative, non-negative mass fractions: project dY onto element
     // conservation over the free species, clip negatives to zero (they leave
-    // the free set), repeat (active-set least-squares, at most 4 passes)
+    // the free set), repeat (active-set least-squares, at most NPASS passes;
+    // the last pass clips nothing, so a result still negative there is rejected)
     unsigned long long fixed = 0ull;   // bit k: species k clipped at zero
     double clipped = 0.0;
     for (int k = 0; k < ns; ++k) Y1[k] = Y[cell * ns + k] + dY[k];
     bool clean = false;
-    for (int pass = 0; pass < 4 && !clean; ++pass) {
+    for (int pass = 0; pass < NPASS && !clean; ++pass) {
       double r[8], G[8][8], lam[8];
       for (int e = 0; e < ne; ++e) {
         double se = 0.0;
@@ -208,7 +211,7 @@ k_post(const uint8_t* __restrict__ img, ImageLayout L, int64_t n, int64_t base, 
         double corr = 0.0;
         for (int e = 0; e < ne; ++e) corr += sB[e * ns + k] * lam[e];
         Y1[k] -= corr;
-        if (Y1[k] < 0.0 && pass < 3) {
+        if (Y1[k] < 0.0 && pass < NPASS - 1) {
           clipped += -Y1[k];
           Y1[k] = 0.0;
           fixed |= 1ull << k;
@@ -248,7 +251,8 @@ k_post(const uint8_t* __restrict__ img, ImageLayout L, int64_t n, int64_t base, 
       // evaluation mode: every cell takes the surrogate result, the gate
       // quantities are reported instead of applied
       double* mt = metrics + i * 6;
-      mt[0] = dTres; mt[1] = er; mt[2] = yreal; mt[3] = ensT; mt[4] = ens; mt[5] = ok ? 1.0 : 0.0;
+      mt[0] = dTres; mt[1] = er; mt[2] = yreal; mt[3] = ensT; mt[4] = ens;
+      mt[5] = (ok && ymin >= 0.0) ? 1.0 : 0.0;   // the gate's fixed conditions
       for (int k = 0; k < ns; ++k) Y[cell * ns + k] = Y1[k];
       T[cell] = conv ? T1 : T0 + dTn;
       continue;
@@ -585,6 +589,7 @@ int surrogate_advance(Surrogate* s, int64_t n, double* T, const double* p, doubl
                       const flint_reactor_opts& o, const flint_surrogate_gate* gate, int* status, int* nsteps,
                       double* jsave, int jslots, double* metrics, bool want_counts, cudaStream_t st) {
   s->last_accepted = s->last_rejected = 0;
+  s->last_n = 0;
   if (n <= 0) return 0;
   // inference in chunks of up to 1,048,576 cells; the rejected cells of all
   // chunks are listed on the device and re-solved by one reactor launch whose
@@ -623,6 +628,7 @@ int surrogate_advance(Surrogate* s, int64_t n, double* T, const double* p, doubl
   count_launch();
   if (cudaGetLastError()) return FLINT_ERR_CUDA;
   s->last_accepted = s->last_rejected = -1;
+  s->last_n = n;
   if (!want_counts) return 0;   // stays asynchronous on st (and capturable in a CUDA graph)
   unsigned long long nrej = 0;
   if (cudaMemcpyAsync(&nrej, s->rej_count, 8, cudaMemcpyDeviceToHost, st) || cudaStreamSynchronize(st))
@@ -633,5 +639,17 @@ int surrogate_advance(Surrogate* s, int64_t n, double* T, const double* p, doubl
 }
 
 void surrogate_counts(Surrogate* s, int64_t* acc, int64_t* rej) { *acc = s->last_accepted; *rej = s->last_rejected; }
+
+// Counts of the last advance read from the device (waits for the device; for
+// advances made without counts, e.g. replays of a captured graph).
+int surrogate_read_counts(Surrogate* s, int64_t* acc, int64_t* rej) {
+  unsigned long long nrej = 0;
+  if (s->last_n > 0) {
+    if (cudaDeviceSynchronize() || cudaMemcpy(&nrej, s->rej_count, 8, cudaMemcpyDeviceToHost)) return FLINT_ERR_CUDA;
+  }
+  *rej = (int64_t)nrej;
+  *acc = s->last_n - (int64_t)nrej;
+  return 0;
+}
 
 }  // namespace flint

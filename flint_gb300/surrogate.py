@@ -68,6 +68,7 @@ def _bind(L):
     L.flint_surrogate_state.argtypes = [vp, C.c_int, _fp, C.POINTER(C.c_int64), C.c_int]
     L.flint_surrogate_advance.argtypes = [vp, i64, vp, vp, vp, vp, C.POINTER(native.ReactorOpts),
                                           C.POINTER(SurrogateGate), vp, vp, C.POINTER(C.c_int64), vp]
+    L.flint_surrogate_counts.argtypes = [vp, C.POINTER(C.c_int64)]
     L.flint_surrogate_evaluate.argtypes = [vp, i64, vp, vp, vp, vp, C.POINTER(SurrogateGate), vp, vp]
     L._surrogate_bound = True
 
@@ -254,6 +255,12 @@ class Surrogate:
                      "flint_surrogate_advance")
         return status, nsteps, ((counts[0], counts[1]) if wait else None)
 
+    def counts(self):
+        """(accepted, rejected) of the last advance, read from the device."""
+        c = (C.c_int64 * 2)()
+        native.check(self.L.flint_surrogate_counts(self.h, c), "flint_surrogate_counts")
+        return c[0], c[1]
+
     def evaluate(self, T, p, Y, dt):
         """Surrogate result for every cell (T, Y in place) and the gate metrics (n, 6)."""
         import torch
@@ -366,11 +373,13 @@ def calibrate(sur, d, target_dT=1.0, target_dY=1e-4, margin=0.5):
     eY = (Y - d["Y1"]).abs().amax(dim=1).cpu().numpy()
     base = (M[:, 5] > 0) & (M[:, 1] <= sur.gate["max_elem_resid"]) & (M[:, 2] >= sur.gate["min_Y"])
     good = (eT <= margin * target_dT) & (eY <= margin * target_dY)
-    qs = np.concatenate([[0.0], np.quantile(M[base, 0], np.linspace(0.05, 1.0, 24))]) if base.any() else [0.0]
+    # quantile grid, denser towards the top where the accepted fraction is decided
+    grid = np.unique(np.concatenate([np.linspace(0.05, 0.9, 18), np.linspace(0.9, 1.0, 26)]))
+    qs = np.concatenate([[0.0], np.quantile(M[base, 0], grid)]) if base.any() else [0.0]
     cand_e = [(1e30, 1e30)]
     if sur.n_nets > 1 and base.any():
-        q3 = np.quantile(M[base, 3], np.linspace(0.05, 1.0, 20))
-        q4 = np.quantile(M[base, 4], np.linspace(0.05, 1.0, 20))
+        q3 = np.quantile(M[base, 3], grid)
+        q4 = np.quantile(M[base, 4], grid)
         cand_e = [(a, b) for a in q3 for b in q4]
     diag = {"eT_q": [float(x) for x in np.quantile(eT, [0.5, 0.9, 0.99, 0.999, 1.0])],
             "eY_q": [float(x) for x in np.quantile(eY, [0.5, 0.9, 0.99, 0.999, 1.0])],
@@ -401,7 +410,9 @@ def calibrate(sur, d, target_dT=1.0, target_dY=1e-4, margin=0.5):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("cmd", choices=["train"])
+    ap.add_argument("cmd", choices=["train", "calibrate"],
+                    help="train: generate, train, calibrate, save; calibrate: re-derive the gate of a checkpoint")
+    ap.add_argument("--checkpoint", help="calibrate: the checkpoint to re-calibrate")
     ap.add_argument("--out", required=True)
     ap.add_argument("--cells", type=int, default=524288)
     ap.add_argument("--val", type=int, default=65536)
@@ -419,6 +430,21 @@ def main():
     states = mechgen.fuel_air_states
     if args.config == "c5":
         states = lambda n, mech, seed: mechgen.c5_states(n, mech, seed)   # noqa: E731
+    if args.cmd == "calibrate":
+        sur = Surrogate.load(chem, args.checkpoint)
+        v = generate(chem, args.val, seed=6000 + args.seed, states=states)
+        best = calibrate(sur, v, margin=args.margin)
+        print("calibration diagnostics", json.dumps(getattr(calibrate, "diag", {})))
+        if best is not None:
+            sur.gate.update(best[1])
+        rep = dict(sur.header.get("extra", {}))
+        rep["calibration"] = None if best is None else {"accept_frac": best[0], "max_dT": best[2], "max_dY": best[3],
+                                                        "val_cells": int(v["T0"].shape[0]), "margin": args.margin}
+        rep["gate"] = sur.gate
+        rep["diagnostics"] = getattr(calibrate, "diag", {})
+        sur.save(args.out, extra=rep, inference_only=bool(sur.header.get("inference_only")))
+        print(json.dumps(rep["calibration"]))
+        return
     t0 = time.time()
     d = generate(chem, args.cells, seed=5000 + args.seed, states=states)
     v = generate(chem, args.val, seed=6000 + args.seed, states=states)

@@ -306,12 +306,17 @@ int flint_surrogate_advance(flint_surrogate_t s, int64_t n, double* T, const dou
                             const double* dt, const flint_reactor_opts* opts,
                             const flint_surrogate_gate* gate, int* status, int* nsteps,
                             int64_t* counts, void* stream);
+/* {accepted, rejected} of the last flint_surrogate_advance, read from the
+ * device after waiting for it (the form for advances made without counts, such
+ * as replays of a captured CUDA graph).  No reference counterpart. */
+int flint_surrogate_counts(flint_surrogate_t s, int64_t* counts);
 
 /* Apply the surrogate to every cell (no gate, no fallback; T, Y in place) and
  * write the gate quantities per cell, metrics[cell][6] = {energy residual [K],
- * element residual, -(clipped mass), ensemble |dT| spread, ensemble
- * max |dY| spread, 1 if the input is inside the gate's domain else 0}: the
- * calibration of the gate thresholds. */
+ * element residual, realizability (the smaller of -(clipped mass) and the
+ * smallest mass fraction), ensemble |dT| spread, ensemble max |dY| spread,
+ * 1 if the input is inside the gate's domain and the projected mass fractions
+ * are non-negative else 0}: the calibration of the gate thresholds. */
 int flint_surrogate_evaluate(flint_surrogate_t s, int64_t n, double* T, const double* p, double* Y,
                              const double* dt, const flint_surrogate_gate* gate, double* metrics,
                              void* stream);

@@ -210,6 +210,7 @@ def test_advance_captured_in_cuda_graph():
     Tg.copy_(T0); Yg.copy_(Y0)
     g.replay()
     torch.cuda.synchronize()
+    assert sur.counts() == (acc, rej)
     np.testing.assert_array_equal(Tg.cpu().numpy(), T.cpu().numpy())
     np.testing.assert_array_equal(Yg.cpu().numpy(), Y.cpu().numpy())
     np.testing.assert_array_equal(st.cpu().numpy(), st_ref.cpu().numpy())
