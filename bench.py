@@ -48,8 +48,8 @@ METRIC = "cell-steps/s on 1 GB300: surrogate+fallback vs plain FP64 at stated T/
 # predicated on) of the warp kernels, per state: k_wdot_warp<0> for one RHS and
 # k_wdot_warp<1> for one Jacobian, from ncu on the c2-wdot / c2-wdotjac and
 # c5-wdot / c5-wdotjac workloads (profiles/fp64_ops_per_state.md).
-KINETICS_FLOPS = {"synthetic-31sp-160r": {"rhs": 18500.0, "jac": 36000.0},
-                  "synthetic-54sp-320r": {"rhs": 37000.0, "jac": 72000.0}}
+KINETICS_FLOPS = {"synthetic-31sp-160r": {"rhs": 20645.0, "jac": 47315.0},
+                  "synthetic-54sp-320r": {"rhs": 36305.0, "jac": 97972.0}}
 
 
 def fp64_ops(ev, ns, mech_name="synthetic-31sp-160r"):
@@ -120,8 +120,10 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cpu_baseline(mech, T, p, Y, dt, target_s=12.0):
-    """Oracle reactor on all host cores over a bounded sample; cells/s."""
+def cpu_baseline(mech, T, p, Y, dt, target_s=12.0, want_state=False):
+    """Oracle reactor on all host cores over a bounded sample; cells/s.  With
+    want_state the oracle's end states of the sample come back too (the checker
+    of the GPU results on the same cells)."""
     from oracle.oracle import Oracle
     from flint_gb300.native import reactor_opts
     orc = Oracle(mech)
@@ -130,13 +132,16 @@ def cpu_baseline(mech, T, p, Y, dt, target_s=12.0):
     n = 256
     while True:
         t0 = time.perf_counter()
-        orc.reactor_advance(T[:n], p[:n], Y[:n], dt[:n], opts)
+        out = orc.reactor_advance(T[:n], p[:n], Y[:n], dt[:n], opts)
         el = time.perf_counter() - t0
         if el > 0.7 * target_s or n >= len(T):
             break
         n = min(len(T), int(n * min(8.0, max(1.5, target_s / max(el, 1e-3)))))
-    return {"value": n / el, "unit": "cell-steps/s", "cores": cores, "kind": "port",
-            "sample": f"{n} of the {len(T)} cells (first n), FP64 oracle BDF, {el:.1f} s"}
+    res = {"value": n / el, "unit": "cell-steps/s", "cores": cores, "kind": "port",
+           "sample": f"{n} of the {len(T)} cells (first n), FP64 oracle BDF, {el:.1f} s"}
+    if want_state:
+        return res, (out[0], out[1], out[2], n)
+    return res
 
 
 def run_reference(args):
@@ -302,6 +307,7 @@ def run_ours(args):
 
 
 SURROGATE_CKPT = os.path.join(REPO, "flint_gb300", "data", "surrogate_c3.bin")
+SURROGATE_CKPT_C5 = os.path.join(REPO, "flint_gb300", "data", "surrogate_c5.bin")
 SUR_CELLS = 1048576
 PLAIN_SAMPLE = 131072
 
@@ -319,10 +325,14 @@ def run_surrogate(args):
     from flint_gb300 import mechgen
     from flint_gb300.api import Chemistry, reactor_stats, kernel_launches
     from flint_gb300.surrogate import Surrogate
-    chem = Chemistry(mechgen.load("c2"))
+    c5 = args.workload == "reactor-c5"
+    chem = Chemistry(mechgen.load("c5" if c5 else "c2"))
     sur = Surrogate.load(chem, args.checkpoint, weights_only=True)
     n = args.cells or SUR_CELLS
-    T0, p0, Y0, dt0 = mechgen.c3_states(n, chem.mech, seed=1004 + rank)
+    if c5:
+        T0, p0, Y0, dt0 = mechgen.c5_states(n, chem.mech, seed=1005 + rank)
+    else:
+        T0, p0, Y0, dt0 = mechgen.c3_states(n, chem.mech, seed=1004 + rank)
     Td0, Yd0 = torch.from_numpy(T0).to(dev), torch.from_numpy(Y0).to(dev)
     pd, dtd = torch.from_numpy(p0).to(dev), torch.from_numpy(dt0).to(dev)
     Td, Yd = Td0.clone(), Yd0.clone()
@@ -453,9 +463,12 @@ def run_surrogate(args):
             "warmup": args.warmup, "ms_per_step": t_sur * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64 (integrator, gate) + bf16/fp32 (network)",
             "data": "synthetic (seeded states, seeded synthetic mechanism)",
-            "config": {"workload": "reactor-c4: surrogate+fallback, 31sp/160r, 1048576 cells, rtol 1e-8 atol 1e-14",
+            "config": {"workload": (f"reactor-c5: surrogate+fallback, 54sp/320r, {n} cells, rtol 1e-8 atol 1e-14"
+                                    if c5 else
+                                    f"reactor-c4: surrogate+fallback, 31sp/160r, {n} cells, rtol 1e-8 atol 1e-14"),
                        "cells_per_gpu": n, "path": "surrogate + FP64 BDF fallback",
-                       "network": "MLP 33-256-256-256-256-32 GELU x2 (ensemble), bf16 mma.sync, fp32 accumulate",
+                       "network": (f"MLP {'-'.join(str(d) for d in sur.dims)} GELU x{sur.n_nets} (ensemble), "
+                                   "split-bf16 mma.sync forward, fp32 accumulate"),
                        "l2": "flushed (256 MiB write) between timed steps", "cuda_graph": graph_note},
             "surrogate": {"accepted": int(acc), "rejected": int(rej), "accept_frac": acc / max(acc + rej, 1),
                           "plain_fp64_cell_steps_per_s": plain, "plain_sample_cells": m,
@@ -475,7 +488,18 @@ def run_surrogate(args):
                          "events_per_launch": fbk, "ops_per_launch": ops,
                          "plain_leg": {"events": plain_stats, "seconds": t_plain}}}
     if rank == 0 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(chem.mech, T0, p0, Y0, dt0)
+        cb, (To, Yo, so_, no) = cpu_baseline(chem.mech, T0, p0, Y0, dt0, want_state=True)
+        line["cpu_baseline"] = cb
+        # the same cells' end states from the FP64 oracle: the errors the target names
+        Tsn, Ysn = Ts[:no].cpu().numpy(), Ys[:no].cpu().numpy()
+        acc_o = ((sts[:no] == 0) & (nsts[:no] == 0)).cpu().numpy()
+        eTo = np.abs(Tsn - To)
+        eYo = np.abs(Ysn - Yo).max(axis=1)
+        line["surrogate"]["vs_oracle"] = {
+            "cells": int(no), "oracle_failed": int((so_ != 0).sum()),
+            "max_abs_dT_K": float(eTo.max()), "max_abs_dY": float(eYo.max()),
+            "max_abs_dT_accepted_K": float(eTo[acc_o].max()) if acc_o.any() else 0.0,
+            "max_abs_dY_accepted": float(eYo[acc_o].max()) if acc_o.any() else 0.0}
     if rank == 0:
         print(json.dumps(line))
     if ws > 1:
@@ -535,12 +559,22 @@ def run_kernel_workload(args):
     t = statistics.mean(times)
     nv = chem.ns + 1
     bytes_per_state = 8 * (2 + 2 * chem.ns) + (8 * nv * nv if jac is not None else 16)
+    roof = None
+    kf = KINETICS_FLOPS.get(chem.mech.name)
+    if kf is not None and gen is None:
+        fl = kf["jac" if jac is not None else "rhs"]
+        peak = chem_peak_fp64()
+        roof = {"bound": "fp64", "kernel": f"k_wdot_warp<{int(jac is not None)}>",
+                "flops_per_state": fl, "achieved": n * fl / t / 1e12, "peak": peak, "unit": "TFLOP/s",
+                "frac": (n * fl / t / 1e12) / peak if peak else None,
+                "peak_source": "DFMA probe kernel measured in this run",
+                "hbm_gbs_algorithmic": n * bytes_per_state / t / 1e9}
     print(json.dumps({"workload": args.workload, "kernel": "generated (ytf_cuda)" if gen else "data-driven",
                       "metric": "states/s", "value": n / t, "unit": "states/s",
                       "ms_per_step": t * 1e3, "states": n, "steps": args.steps, "warmup": args.warmup,
                       "gpu_launches": kernel_launches() - l0,
                       "hbm_gbs_algorithmic": n * bytes_per_state / t / 1e9,
-                      "bytes_per_state": bytes_per_state}))
+                      "bytes_per_state": bytes_per_state, "roofline": roof}))
 
 
 def chem_peak_fp64():
@@ -573,6 +607,10 @@ def main():
     ap.add_argument("--no-graph", action="store_true", help="surrogate path: direct calls instead of a CUDA graph")
     args = ap.parse_args()
     if args.workload == "reactor-c5":
+        if args.path == "surrogate":
+            args.checkpoint = args.checkpoint if args.checkpoint != SURROGATE_CKPT else SURROGATE_CKPT_C5
+            run_surrogate(args)
+            return
         args.cells = args.cells or CELLS
         run_ours(args)
         return

@@ -404,6 +404,9 @@ int flint_reactor_advance_noalloc(flint_mech_t h, int64_t n, double* T, const do
   if ((int64_t)(h->L.ns + 1) * (h->L.ns + 1) > 32 * 32)
     return fail(FLINT_ERR_MECH, "flint_reactor_advance_noalloc: %d unknowns exceed the 32 x 32 Jacobian slots of its "
                                 "static scratch (%zu bytes)", h->L.ns + 1, reactor_noalloc_bytes());
+  if (!reactor_noalloc_fits(h->L))
+    return fail(FLINT_ERR_MECH, "flint_reactor_advance_noalloc: this mechanism's Newton matrix does not fit shared "
+                                "memory and needs more scratch per warp than the static array holds");
   flint_reactor_opts o;
   if (opts) o = *opts; else flint_reactor_default_opts(&o);
   if (!(o.rtol > 0.0) || !(o.atol > 0.0) || o.max_steps < 1 || o.max_order < 1 || o.max_order > 5)

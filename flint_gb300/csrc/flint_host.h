@@ -13,6 +13,15 @@ cudaError_t probe_fp64(double* tflops);
 cudaError_t launch_exp_selftest(const uint8_t* img, const ImageLayout& L, int64_t n, const double* x, double* y,
                                 cudaStream_t st);
 int device_sms();
+// Largest dynamic shared memory a block may opt into on the current device.
+size_t device_smem_optin();
+// Opt a kernel into `bytes` of dynamic shared memory.  A refusal is returned
+// and consumed, so that it does not surface in a later cudaGetLastError.
+inline cudaError_t set_smem(const void* fn, size_t bytes) {
+  cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  if (e != cudaSuccess) (void)cudaGetLastError();
+  return e;
+}
 
 cudaError_t launch_wdot(const uint8_t* img, const ImageLayout& L, int64_t n, int layout, const double* T,
                         const double* p, const double* Y, double* wdot, double* cp, double* h, cudaStream_t st);
@@ -35,6 +44,7 @@ cudaError_t launch_reactor(const uint8_t* img, const ImageLayout& L, int64_t n, 
 
 size_t reactor_noalloc_bytes();
 int reactor_noalloc_slots();
+bool reactor_noalloc_fits(const ImageLayout& L);
 cudaError_t launch_reactor_noalloc(const uint8_t* img, const ImageLayout& L, int64_t n, double* T, const double* p,
                                    double* Y, const double* dt, const flint_reactor_opts& o, int* status,
                                    int* nsteps, cudaStream_t st);

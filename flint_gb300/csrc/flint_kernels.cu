@@ -138,7 +138,10 @@ k_wdot_small(const uint8_t* __restrict__ img, ImageLayout L, int64_t n, int layo
 }
 
 // ---------------------------------------------------------------- warp
-template <bool JAC, int SPL>
+// SPL species per lane; GJ: the Jacobian work area is a per-warp slot of
+// global memory (mechanisms of 33-63 species, and smaller ones whose shared
+// memory layout would not fit a block).
+template <bool JAC, int SPL, bool GJ>
 __global__ void __launch_bounds__(WARP_THREADS)
 k_wdot_warp(const uint8_t* __restrict__ img, ImageLayout L, int64_t n, int layout,
             const double* __restrict__ Tg, const double* __restrict__ pg,
@@ -151,11 +154,10 @@ k_wdot_warp(const uint8_t* __restrict__ img, ImageLayout L, int64_t n, int layou
   m.bind(L, smem);
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   WarpScratch s;
-  if (SPL == 1) {
+  if (!GJ) {
     const int sd = scratch_doubles(m.nsp, m.nrpad, JAC);
     s = carve(reinterpret_cast<double*>(smem + L.bytes) + wid * sd, m.nsp, m.nrpad, JAC);
   } else {
-    // 32-63 species: the Jacobian work area is a per-warp slot of global memory
     const int sd = scratch_small_doubles(m.nsp, m.nrpad);
     const int64_t gw = (int64_t)blockIdx.x * (blockDim.x >> 5) + wid;
     s = carve2(reinterpret_cast<double*>(smem + L.bytes) + wid * sd,
@@ -301,6 +303,17 @@ int device_sms() {
   return g_sms;
 }
 
+static int g_optin = 0;
+size_t device_smem_optin() {
+  if (g_optin == 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&g_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    if (g_optin <= 0) g_optin = 48 * 1024;
+  }
+  return (size_t)g_optin;
+}
+
 static int64_t grid_for(const void* fn, int threads, size_t smem, int64_t work_items) {
   int per_sm = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, smem);
@@ -312,23 +325,32 @@ static int64_t grid_for(const void* fn, int threads, size_t smem, int64_t work_i
 }
 
 size_t small_smem(const ImageLayout& L) { return L.bytes + 3 * SMALL_NSMAX * SMALL_THREADS * sizeof(double); }
+// Jacobian work area in global memory: 33-63 species, or a shared-memory
+// layout too large for a block.
+static bool warp_gj(const ImageLayout& L, bool jac) {
+  if (L.nsp > 32) return true;
+  if (!jac) return false;
+  return L.bytes + (WARP_THREADS / 32) * scratch_doubles(L.nsp, L.nrpad, true) * sizeof(double) > device_smem_optin();
+}
+
 size_t warp_smem(const ImageLayout& L, bool jac) {
-  if (L.nsp > 32) return L.bytes + (WARP_THREADS / 32) * scratch_small_doubles(L.nsp, L.nrpad) * sizeof(double);
+  if (warp_gj(L, jac)) return L.bytes + (WARP_THREADS / 32) * scratch_small_doubles(L.nsp, L.nrpad) * sizeof(double);
   return L.bytes + (WARP_THREADS / 32) * scratch_doubles(L.nsp, L.nrpad, jac) * sizeof(double);
 }
 
 template <bool JAC>
 static const void* warp_fn(const ImageLayout& L) {
-  return L.nsp > 32 ? (const void*)k_wdot_warp<JAC, 2> : (const void*)k_wdot_warp<JAC, 1>;
+  if (L.nsp > 32) return (const void*)k_wdot_warp<JAC, 2, true>;
+  return warp_gj(L, JAC) ? (const void*)k_wdot_warp<JAC, 1, true> : (const void*)k_wdot_warp<JAC, 1, false>;
 }
 
-// Global Jacobian work area needed by the warp kernels for 32-63 species
-// (doubles), for a grid of full waves.
+// Global Jacobian work area needed by the warp kernels (doubles), for a grid
+// of full waves; 0 when it lives in shared memory.
 int64_t warp_jac_scratch_doubles(const ImageLayout& L) {
-  if (L.nsp <= 32) return 0;
+  if (!warp_gj(L, true)) return 0;
   size_t sm = warp_smem(L, true);
   const void* fn = warp_fn<true>(L);
-  cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  if (set_smem(fn, sm) != cudaSuccess) return 0;
   int per_sm = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, WARP_THREADS, sm);
   if (per_sm < 1) per_sm = 1;
@@ -341,15 +363,20 @@ static cudaError_t launch_warp(const uint8_t* img, const ImageLayout& L, int64_t
                                double* rhs, double* gscratch, cudaStream_t st) {
   size_t sm = warp_smem(L, JAC);
   const void* fn = warp_fn<JAC>(L);
-  cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  cudaError_t e = set_smem(fn, sm);
   if (e != cudaSuccess) return e;
+  const bool gj = warp_gj(L, JAC);
+  if (gj && JAC && !gscratch) return cudaErrorInvalidValue;
   int64_t g = grid_for(fn, WARP_THREADS, sm, n * 32);
   if (L.nsp > 32)
-    k_wdot_warp<JAC, 2><<<(unsigned)g, WARP_THREADS, sm, st>>>(img, L, n, layout, T, p, Y, wdot, cp, h, jac, rhs,
-                                                                gscratch);
+    k_wdot_warp<JAC, 2, true><<<(unsigned)g, WARP_THREADS, sm, st>>>(img, L, n, layout, T, p, Y, wdot, cp, h, jac,
+                                                                      rhs, gscratch);
+  else if (gj)
+    k_wdot_warp<JAC, 1, true><<<(unsigned)g, WARP_THREADS, sm, st>>>(img, L, n, layout, T, p, Y, wdot, cp, h, jac,
+                                                                      rhs, gscratch);
   else
-    k_wdot_warp<JAC, 1><<<(unsigned)g, WARP_THREADS, sm, st>>>(img, L, n, layout, T, p, Y, wdot, cp, h, jac, rhs,
-                                                                nullptr);
+    k_wdot_warp<JAC, 1, false><<<(unsigned)g, WARP_THREADS, sm, st>>>(img, L, n, layout, T, p, Y, wdot, cp, h, jac,
+                                                                       rhs, nullptr);
   count_launch();
   return cudaGetLastError();
 }
@@ -362,7 +389,7 @@ cudaError_t launch_wdot(const uint8_t* img, const ImageLayout& L, int64_t n, int
   if (n <= 0) return cudaSuccess;
   if (use_small_kernel(L)) {
     size_t sm = small_smem(L);
-    cudaFuncSetAttribute(k_wdot_small, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    set_smem((const void*)k_wdot_small, sm);
     int64_t g = grid_for((const void*)k_wdot_small, SMALL_THREADS, sm, n);
     k_wdot_small<<<(unsigned)g, SMALL_THREADS, sm, st>>>(img, L, n, layout, T, p, Y, wdot, cp, h, 0, nullptr);
     count_launch();
@@ -375,7 +402,7 @@ cudaError_t launch_thermo(const uint8_t* img, const ImageLayout& L, int64_t n, i
                           const double* Y, double* cp, double* h, cudaStream_t st) {
   if (n <= 0) return cudaSuccess;
   size_t sm = L.bytes;
-  cudaFuncSetAttribute(k_thermo, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  set_smem((const void*)k_thermo, sm);
   int64_t g = grid_for((const void*)k_thermo, SMALL_THREADS, sm, n);
   k_thermo<<<(unsigned)g, SMALL_THREADS, sm, st>>>(img, L, n, layout, T, Y, cp, h);
   count_launch();
@@ -386,7 +413,7 @@ cudaError_t launch_chemistry_source(const uint8_t* img, const ImageLayout& L, in
                                     const double* T, double* omegadot, cudaStream_t st) {
   if (n <= 0) return cudaSuccess;
   size_t sm = small_smem(L);
-  cudaFuncSetAttribute(k_wdot_small, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  set_smem((const void*)k_wdot_small, sm);
   int64_t g = grid_for((const void*)k_wdot_small, SMALL_THREADS, sm, n);
   k_wdot_small<<<(unsigned)g, SMALL_THREADS, sm, st>>>(img, L, n, 0, T, nullptr, nullptr, omegadot, nullptr,
                                                          nullptr, 1, roi);

@@ -167,19 +167,82 @@ __device__ inline void warp_lu_solve(const double* A, int ld, int nv, int lane, 
   for (int j = 0; j < SPL; ++j) b[j] = x[j];
 }
 
-// Doubles per resident-warp slot of the reactor's global scratch: the saved
-// Jacobian (32*SPL)^2, and for SPL = 2 the Jacobian work area too.
-__host__ __device__ inline int64_t reactor_slot_doubles_of(const ImageLayout& L) {
-  const int spl = L.nsp / 32;
-  return (int64_t)(32 * spl) * (32 * spl) + (spl > 1 ? scratch_jac_doubles(L.nsp, L.nrpad) : 0);
+// Newton matrix refresh, kept out of line: the Jacobian evaluation (when asked
+// for; it also refreshes the saved copy Jg) or its reload from Jg, M = I -
+// gamma J, and the LU factorization.  It runs once every few steps, so keeping
+// its code out of the Newton loop leaves that loop's instructions in the
+// instruction cache.  The pivot order goes to pivs[0 .. 32 SPL) and each row's
+// pivot step to pivs[32 SPL + row].
+template <int SPL>
+__device__ __noinline__ void refresh_newton_matrix(MechView m, WarpScratch s, int lane, double p, double gamma,
+                                                   int eval_J, double ya, double yb, double* Jg, int* pivs) {
+  constexpr int JW = 32 * SPL;
+  const int ns = m.ns, nv = ns + 1, ld = s.ldj;
+  const int Tslot = ns >> 5, Tlane = ns & 31;
+  if (eval_J) {
+    const double Tv = __shfl_sync(FULL, (SPL == 1 || Tslot == 0) ? ya : yb, Tlane);
+    double yk[SPL];
+    yk[0] = (lane < ns) ? ya : 0.0;
+    if (SPL > 1) yk[SPL - 1] = (lane + 32 < ns) ? yb : 0.0;
+    CellOutT<SPL> co;
+    warp_kinetics<true, SPL>(m, s, lane, yk, Tv, p, co);
+#pragma unroll
+    for (int j = 0; j < SPL; ++j) {
+      const int r = lane + 32 * j;
+      if (r < nv) {
+        const double* row = s.Jr + r * ld;
+        for (int c = 0; c < nv; ++c) Jg[c * JW + r] = row[c];
+      }
+    }
+  } else {
+#pragma unroll
+    for (int j = 0; j < SPL; ++j) {
+      const int r = lane + 32 * j;
+      if (r < nv) {
+        double* row = s.Jr + r * ld;
+        for (int c = 0; c < nv; ++c) row[c] = Jg[c * JW + r];
+      }
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < SPL; ++j) {
+    const int r = lane + 32 * j;
+    if (r < nv) {
+      double* row = s.Jr + r * ld;
+      for (int c = 0; c < nv; ++c) row[c] = (c == r ? 1.0 : 0.0) - gamma * row[c];
+    }
+  }
+  __syncwarp();
+  int mystep[SPL];
+  warp_lu<SPL>(s.Jr, ld, nv, lane, pivs, mystep);
+#pragma unroll
+  for (int j = 0; j < SPL; ++j) pivs[32 * SPL + lane + 32 * j] = mystep[j];
+  __syncwarp();
 }
 
-template <int SPL>
+// Layout choice: the Newton matrix and the Jacobian work area live in shared
+// memory (SPL = 1 and the block fits), or in the warp's global slot (GJ).
+static int spl_of(const ImageLayout& L) { return L.nsp / 32; }
+
+static size_t reactor_smem_spl1(const ImageLayout& L) {
+  return L.bytes + (REACTOR_THREADS / 32) * (scratch_doubles(L.nsp, L.nrpad, true) * sizeof(double) + 64 * sizeof(int));
+}
+
+static bool reactor_gj(const ImageLayout& L) { return spl_of(L) > 1 || reactor_smem_spl1(L) > device_smem_optin(); }
+
+// Doubles per resident-warp slot of the reactor's global scratch: the saved
+// Jacobian (32*SPL)^2, and in GJ layout the Jacobian work area too.
+static int64_t reactor_slot_doubles_of(const ImageLayout& L) {
+  const int spl = spl_of(L);
+  return (int64_t)(32 * spl) * (32 * spl) + (reactor_gj(L) ? scratch_jac_doubles(L.nsp, L.nrpad) : 0);
+}
+
+template <int SPL, bool GJ>
 __global__ void __launch_bounds__(REACTOR_THREADS)
 k_reactor(const uint8_t* __restrict__ img, ImageLayout L, int64_t n, double* __restrict__ Tg,
           const double* __restrict__ pg, double* __restrict__ Yg, const double* __restrict__ dtg,
           flint_reactor_opts o, int* __restrict__ status_g, int* __restrict__ nsteps_g,
-          unsigned long long* __restrict__ counter, double* __restrict__ jsave,
+          unsigned long long* __restrict__ counter, double* __restrict__ jsave, int64_t slot_doubles,
           const unsigned long long* __restrict__ n_dev) {
   extern __shared__ __align__(16) uint8_t smem[];
   if (n_dev) n = min(n, (int64_t)*n_dev);   // cell count produced on the device
@@ -188,20 +251,20 @@ k_reactor(const uint8_t* __restrict__ img, ImageLayout L, int64_t n, double* __r
   m.bind(L, smem);
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int64_t slot = (int64_t)blockIdx.x * (blockDim.x >> 5) + wid;
-  double* Jg = jsave + slot * reactor_slot_doubles_of(L);
+  double* Jg = jsave + slot * slot_doubles;
   constexpr int JW = 32 * SPL;   // row stride of the saved Jacobian
   WarpScratch s;
   int* pivs;
-  if (SPL == 1) {
+  if (!GJ) {
     const int sd = scratch_doubles(m.nsp, m.nrpad, true);
     double* wbase = reinterpret_cast<double*>(smem + L.bytes) + wid * sd;
     s = carve(wbase, m.nsp, m.nrpad, true);
-    pivs = reinterpret_cast<int*>(reinterpret_cast<double*>(smem + L.bytes) + (blockDim.x >> 5) * sd) + wid * 32;
+    pivs = reinterpret_cast<int*>(reinterpret_cast<double*>(smem + L.bytes) + (blockDim.x >> 5) * sd) + wid * 64;
   } else {
     const int sd = scratch_small_doubles(m.nsp, m.nrpad);
     double* wbase = reinterpret_cast<double*>(smem + L.bytes) + wid * sd;
     s = carve2(wbase, Jg + JW * JW, m.nsp, m.nrpad);
-    pivs = reinterpret_cast<int*>(reinterpret_cast<double*>(smem + L.bytes) + (blockDim.x >> 5) * sd) + wid * 64;
+    pivs = reinterpret_cast<int*>(reinterpret_cast<double*>(smem + L.bytes) + (blockDim.x >> 5) * sd) + wid * 64 * SPL;
   }
   const int ns = m.ns, nv = ns + 1;
   const int ld = s.ldj;
@@ -318,43 +381,15 @@ k_reactor(const uint8_t* __restrict__ img, ImageLayout L, int64_t n, double* __r
 #pragma unroll
           for (int j = 0; j < SPL; ++j) ypred[j] = z[0][j];
           if (!have_J || need_J || fabs(gamma / gammaJ - 1.0) > DGMAX || nst >= nstP + MSBP) {
-            if (!have_J || need_J || nst >= nstJ + MSBJ) {
-              const double Tv = __shfl_sync(FULL, (SPL == 1 || Tslot == 0) ? ypred[0] : ypred[SPL - 1], Tlane);
+            const int eval_J = (!have_J || need_J || nst >= nstJ + MSBJ) ? 1 : 0;
+            if (eval_J) {
               ++n_jac;
-              double yk[SPL];
-#pragma unroll
-              for (int j = 0; j < SPL; ++j) yk[j] = (lane + 32 * j < ns) ? ypred[j] : 0.0;
-              warp_kinetics<true, SPL>(m, s, lane, yk, Tv, p, co);
-#pragma unroll
-              for (int j = 0; j < SPL; ++j) {
-                const int r = lane + 32 * j;
-                if (r < nv) {
-                  const double* row = s.Jr + r * ld;
-                  for (int c = 0; c < nv; ++c) Jg[c * JW + r] = row[c];
-                }
-              }
               have_J = 1; jfresh = 1; nstJ = nst; need_J = 0;
-            } else {
-#pragma unroll
-              for (int j = 0; j < SPL; ++j) {
-                const int r = lane + 32 * j;
-                if (r < nv) {
-                  double* row = s.Jr + r * ld;
-                  for (int c = 0; c < nv; ++c) row[c] = Jg[c * JW + r];
-                }
-              }
             }
+            refresh_newton_matrix<SPL>(m, s, lane, p, gamma, eval_J, ypred[0], ypred[SPL - 1], Jg, pivs);
 #pragma unroll
-            for (int j = 0; j < SPL; ++j) {
-              const int r = lane + 32 * j;
-              if (r < nv) {
-                double* row = s.Jr + r * ld;
-                for (int c = 0; c < nv; ++c) row[c] = (c == r ? 1.0 : 0.0) - gamma * row[c];
-              }
-            }
-            __syncwarp();
+            for (int j = 0; j < SPL; ++j) mystep[j] = pivs[32 * SPL + lane + 32 * j];
             ++n_lu;
-            warp_lu<SPL>(s.Jr, ld, nv, lane, pivs, mystep);
             gammaJ = gamma; nstP = nst; crate = 1.0;
           }
           const double gamrat = gamma / gammaJ;
@@ -520,23 +555,22 @@ k_reactor(const uint8_t* __restrict__ img, ImageLayout L, int64_t n, double* __r
   }
 }
 
-static int spl_of(const ImageLayout& L) { return L.nsp / 32; }
-
 size_t reactor_smem(const ImageLayout& L) {
-  if (spl_of(L) == 1)
-    return L.bytes + (REACTOR_THREADS / 32) * (scratch_doubles(L.nsp, L.nrpad, true) * sizeof(double) + 32 * sizeof(int));
-  return L.bytes + (REACTOR_THREADS / 32) * (scratch_small_doubles(L.nsp, L.nrpad) * sizeof(double) + 64 * sizeof(int));
+  if (!reactor_gj(L)) return reactor_smem_spl1(L);
+  return L.bytes + (REACTOR_THREADS / 32) *
+                       (scratch_small_doubles(L.nsp, L.nrpad) * sizeof(double) + 64 * spl_of(L) * sizeof(int));
 }
 
 static const void* reactor_fn(const ImageLayout& L) {
-  return spl_of(L) == 1 ? (const void*)k_reactor<1> : (const void*)k_reactor<2>;
+  if (spl_of(L) > 1) return (const void*)k_reactor<2, true>;
+  return reactor_gj(L) ? (const void*)k_reactor<1, true> : (const void*)k_reactor<1, false>;
 }
 
 int reactor_slots(const ImageLayout& L) {
   if (spl_of(L) < 1 || spl_of(L) > 2) return 0;
   size_t sm = reactor_smem(L);
   const void* fn = reactor_fn(L);
-  if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) != cudaSuccess) return 0;
+  if (set_smem(fn, sm) != cudaSuccess) return 0;
   int per_sm = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, REACTOR_THREADS, sm);
   return per_sm * device_sms() * (REACTOR_THREADS / 32);
@@ -552,7 +586,7 @@ cudaError_t launch_reactor(const uint8_t* img, const ImageLayout& L, int64_t n, 
   if (spl_of(L) < 1 || spl_of(L) > 2) return cudaErrorInvalidValue;
   size_t sm = reactor_smem(L);
   const void* fn = reactor_fn(L);
-  cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  cudaError_t e = set_smem(fn, sm);
   if (e != cudaSuccess) return e;
   int per_sm = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, REACTOR_THREADS, sm);
@@ -582,14 +616,17 @@ cudaError_t launch_reactor(const uint8_t* img, const ImageLayout& L, int64_t n, 
   }
   e = cudaMemsetAsync(work_counter, 0, NCOUNTERS * sizeof(unsigned long long), st);
   if (e != cudaSuccess) return e;
-  if (spl_of(L) == 1)
-    k_reactor<1><<<(unsigned)blocks, REACTOR_THREADS, sm, st>>>(img, L, n, T, p, Y, dt, o, status, nsteps,
-                                                                 reinterpret_cast<unsigned long long*>(work_counter), jsave,
-                                                                 n_dev);
+  const int64_t sd = reactor_slot_doubles_of(L);
+  unsigned long long* wc = reinterpret_cast<unsigned long long*>(work_counter);
+  if (spl_of(L) > 1)
+    k_reactor<2, true><<<(unsigned)blocks, REACTOR_THREADS, sm, st>>>(img, L, n, T, p, Y, dt, o, status, nsteps, wc,
+                                                                       jsave, sd, n_dev);
+  else if (reactor_gj(L))
+    k_reactor<1, true><<<(unsigned)blocks, REACTOR_THREADS, sm, st>>>(img, L, n, T, p, Y, dt, o, status, nsteps, wc,
+                                                                       jsave, sd, n_dev);
   else
-    k_reactor<2><<<(unsigned)blocks, REACTOR_THREADS, sm, st>>>(img, L, n, T, p, Y, dt, o, status, nsteps,
-                                                                 reinterpret_cast<unsigned long long*>(work_counter), jsave,
-                                                                 n_dev);
+    k_reactor<1, false><<<(unsigned)blocks, REACTOR_THREADS, sm, st>>>(img, L, n, T, p, Y, dt, o, status, nsteps, wc,
+                                                                        jsave, sd, n_dev);
   count_launch();
   return cudaGetLastError();
 }
@@ -633,11 +670,13 @@ static cudaError_t noalloc_scratch_address(void** out) {
 }
 
 size_t reactor_noalloc_bytes() { return NOALLOC_BYTES; }
+bool reactor_noalloc_fits(const ImageLayout& L) { return reactor_slot_doubles_of(L) <= JSLOT; }
 int reactor_noalloc_slots() { return NOALLOC_SLOTS; }
 
 cudaError_t launch_reactor_noalloc(const uint8_t* img, const ImageLayout& L, int64_t n, double* T, const double* p,
                                    double* Y, const double* dt, const flint_reactor_opts& o, int* status,
                                    int* nsteps, cudaStream_t st) {
+  if (!reactor_noalloc_fits(L)) return cudaErrorInvalidValue;
   void* base = nullptr;
   cudaError_t e = noalloc_scratch_address(&base);
   if (e != cudaSuccess) return e;

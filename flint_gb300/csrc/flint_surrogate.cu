@@ -603,7 +603,7 @@ int surrogate_advance(Surrogate* s, int64_t n, double* T, const double* p, doubl
   gp.Tlo = gate->T_lo; gp.Thi = gate->T_hi; gp.lpl = gate->log10p_lo; gp.lph = gate->log10p_hi;
   gp.ldl = gate->log10dt_lo; gp.ldh = gate->log10dt_hi;
   const size_t psm = s->L.bytes + (size_t)(std::max(s->ne, 1) * s->ns) * sizeof(double);
-  if (cudaFuncSetAttribute(k_post, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)psm)) return FLINT_ERR_CUDA;
+  if (set_smem((const void*)k_post, psm)) return FLINT_ERR_CUDA;
   if (cudaMemsetAsync(s->rej_count, 0, 8, st)) return FLINT_ERR_CUDA;
   for (int64_t b = 0; b < n; b += s->cap) {
     const int64_t m = std::min<int64_t>(s->cap, n - b);

@@ -298,7 +298,7 @@ cudaError_t launch_general(const uint8_t* img, const TableLayout& L, const doubl
   if (n <= 0) return cudaSuccess;
   size_t sm = table_smem(L);
   const void* fn = rhs ? (const void*)k_general_warp<1> : (const void*)k_general_warp<0>;
-  cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  cudaError_t e = set_smem(fn, sm);
   if (e != cudaSuccess) return e;
   int per_sm = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, TABLE_THREADS, sm);
