@@ -309,12 +309,12 @@ def run_ours(args):
 SURROGATE_CKPT = os.path.join(REPO, "flint_gb300", "data", "surrogate_c3.bin")
 SURROGATE_CKPT_C5 = os.path.join(REPO, "flint_gb300", "data", "surrogate_c5.bin")
 SUR_CELLS = 1048576
-PLAIN_SAMPLE = 131072
+PLAIN_SAMPLE = 262144
 
 
 def run_surrogate(args):
     """Headline: surrogate + fallback advance of 1,048,576 reactor cells vs the
-    plain FP64 integrator, errors judged by the integrator on a 131,072-cell sample."""
+    plain FP64 integrator, errors judged by the integrator on a 262,144-cell sample."""
     import torch
     ws, rank, local = dist_env()
     if ws > 1:

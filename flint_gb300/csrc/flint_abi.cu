@@ -262,6 +262,18 @@ int flint_rhs_native_batch(flint_mech_t h, int64_t n, const double* Z, double* F
   return e == cudaSuccess ? FLINT_OK : cuda_fail(e, "flint_rhs_native_batch");
 }
 
+int flint_transport_batch(flint_mech_t h, int64_t n, const double* rhoi, const double* T, double* mu, double* lambda,
+                          void* stream) {
+  if (!h) return fail(FLINT_ERR_ARG, "NULL handle");
+  if (n < 0) return fail(FLINT_ERR_ARG, "negative cell count");
+  if (!h->table) return fail(FLINT_ERR_MECH, "flint_transport_batch needs a tabulated mechanism");
+  if (!table_has_transport(h->table)) return fail(FLINT_ERR_MECH, "the handle was created without transport tables");
+  if (n == 0) return FLINT_OK;
+  if (!rhoi || !T || !mu || !lambda) return fail(FLINT_ERR_ARG, "NULL array");
+  cudaError_t e = table_transport(h->table, n, rhoi, T, mu, lambda, (cudaStream_t)stream);
+  return e == cudaSuccess ? FLINT_OK : cuda_fail(e, "flint_transport_batch");
+}
+
 int flint_cons2prim_batch(flint_mech_t h, int64_t n, int ndim, const double* cons, const double* T, double* prim,
                           double* T_out, void* stream) {
   if (!h) return fail(FLINT_ERR_ARG, "NULL handle");

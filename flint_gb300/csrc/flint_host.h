@@ -76,6 +76,9 @@ int table_ns(void* th);
 int table_nr(void* th);
 cudaError_t table_run(void* th, int64_t n, int rhs, const double* roi, const double* T, double* out,
                       cudaStream_t st);
+int table_has_transport(void* p);
+cudaError_t table_transport(void* p, int64_t n, const double* rhoi, const double* T, double* mu, double* lam,
+                            cudaStream_t st);
 cudaError_t table_cons2prim(void* p, int64_t n, int np, const double* cons, const double* T, double* prim,
                             double* Tout, cudaStream_t st);
 

@@ -32,6 +32,10 @@ struct TableLayout {
   int o_wm, o_ri, o_kind, o_tb, o_rsp, o_rex, o_psp, o_pex, o_eff, o_cstart, o_lr, o_lnu;
   // global tables (doubles offsets into the table buffer)
   size_t g_k1, g_k2, g_k3, g_k4, g_cp, g_h;
+  // transport (when given): species viscosity and conductivity [row][nsp],
+  // and Wilke's species-pair factors (W_i/W_j)^(1/4) and sqrt(8 (1 + W_i/W_j)) [ns][ns]
+  int has_tr;
+  size_t g_mu, g_kt, g_p4, g_s8;
 };
 
 struct TableView {
@@ -128,7 +132,10 @@ int table_pack(const flint_table_desc* d, TableLayout& L, std::vector<uint8_t>& 
   // transposed tables: rate tables [row][reaction], thermo tables [row][species]
   const size_t RR = (size_t)L.nrow_r * P, TT = (size_t)L.nrow_t * S;
   L.g_k1 = 0; L.g_k2 = RR; L.g_k3 = 2 * RR; L.g_k4 = 3 * RR; L.g_cp = 4 * RR; L.g_h = 4 * RR + TT;
-  tabs.assign(4 * RR + 2 * TT, 0.0);
+  L.has_tr = (d->mi_tab && d->k_tab) ? 1 : 0;
+  const size_t PP = (size_t)ns * ns;
+  L.g_mu = 4 * RR + 2 * TT; L.g_kt = L.g_mu + TT; L.g_p4 = L.g_kt + TT; L.g_s8 = L.g_p4 + PP;
+  tabs.assign(L.has_tr ? L.g_s8 + PP : 4 * RR + 2 * TT, 0.0);
   auto put = [&](size_t base, const double* src, int nrj, int r0) {
     for (int j = 0; j < nrj; ++j)
       for (int row = 0; row < L.nrow_r; ++row) tabs[base + (size_t)row * P + r0 + j] = src[(size_t)j * L.nrow_r + row];
@@ -143,7 +150,21 @@ int table_pack(const flint_table_desc* d, TableLayout& L, std::vector<uint8_t>& 
     for (int row = 0; row < L.nrow_t; ++row) {
       tabs[L.g_cp + (size_t)row * S + s] = d->cp_tab[(size_t)s * L.nrow_t + row];
       tabs[L.g_h + (size_t)row * S + s] = d->h_tab[(size_t)s * L.nrow_t + row];
+      if (L.has_tr) {
+        tabs[L.g_mu + (size_t)row * S + s] = d->mi_tab[(size_t)s * L.nrow_t + row];
+        tabs[L.g_kt + (size_t)row * S + s] = d->k_tab[(size_t)s * L.nrow_t + row];
+      }
     }
+  if (L.has_tr) {
+    // T-independent parts of co_fiij, evaluated once on the host as the
+    // reference evaluates them per call: Mi_Mj**0.25d0 and dsqrt(8*(1+Mi_Mj))
+    for (int i = 0; i < ns; ++i)
+      for (int j = 0; j < ns; ++j) {
+        const double MiMj = d->wm[i] / d->wm[j];
+        tabs[L.g_p4 + (size_t)i * ns + j] = std::pow(MiMj, 0.25);
+        tabs[L.g_s8 + (size_t)i * ns + j] = std::sqrt(8.0 * (1.0 + MiMj));
+      }
+  }
   return FLINT_OK;
 }
 
@@ -398,6 +419,65 @@ __global__ void k_cons2prim(C2PView v, int64_t n, int np, const double* __restri
   }
 }
 
+// ------------------------------------------------------------- transport
+// co_k_mi_lam_Wilke (Lib_ThermoTransport.f90:407-462) with f_molecularWeight
+// (:200-214) and co_fiij (:350-362): warp per cell, species i on lane i.  Each
+// lane forms its own Wilke denominator over j in order; the mixture sums run
+// over the species in order through shuffles, so every sum has the Fortran
+// loop's order and the result matches the oracle bit for bit (the
+// T-independent pair factors are the host's pow / sqrt, as in the oracle).
+struct TransView {
+  const double *mu, *kt, *p4, *s8, *wm;
+  int ns, nsp, tmin, nrow;
+};
+
+__device__ inline double ordered_sum(double v, int ns) {
+  double acc = 0.0;
+  for (int s = 0; s < ns; ++s) acc = __dadd_rn(acc, __shfl_sync(FULL, v, s));
+  return acc;
+}
+
+__global__ void k_transport(TransView v, int64_t n, const double* __restrict__ rhoi, const double* __restrict__ Tg,
+                            double* __restrict__ mu, double* __restrict__ lam) {
+  const int lane = threadIdx.x & 31;
+  const int64_t nwarps = (int64_t)gridDim.x * (blockDim.x >> 5);
+  const int ns = v.ns;
+  const bool act = lane < ns;
+  for (int64_t cell = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); cell < n; cell += nwarps) {
+    const double T = Tg[cell];
+    const double r = act ? rhoi[cell * ns + lane] : 0.0;
+    const double W = act ? v.wm[lane] : 1.0;
+    const double rho = ordered_sum(r, ns);
+    const double Wmtot = __ddiv_rn(1.0, ordered_sum(act ? __ddiv_rn(__ddiv_rn(r, rho), W) : 0.0, ns));
+    const double Xi = act ? __ddiv_rn(__dmul_rn(r, Wmtot), __dmul_rn(rho, W)) : 0.0;
+    const int Ti = (int)T;
+    int row = Ti - v.tmin;
+    row = row < 0 ? 0 : (row > v.nrow - 2 ? v.nrow - 2 : row);
+    const double Tdiff = __dsub_rn(T, (double)Ti);
+    double mi = 0.0, ki = 0.0;
+    if (act) {
+      const double* a = v.mu + (size_t)row * v.nsp + lane;
+      const double* b = v.kt + (size_t)row * v.nsp + lane;
+      mi = lerp_rn(a[0], a[v.nsp], Tdiff);
+      ki = lerp_rn(b[0], b[v.nsp], Tdiff);
+    }
+    double den = 0.0;
+    for (int j = 0; j < ns; ++j) {
+      const double mj = __shfl_sync(FULL, mi, j), Xj = __shfl_sync(FULL, Xi, j);
+      if (act) {
+        const double q = __dsqrt_rn(__ddiv_rn(mi, __dadd_rn(mj, 1e-20)));
+        const double a = __dadd_rn(1.0, __ddiv_rn(q, v.p4[lane * ns + j]));
+        const double fi = __ddiv_rn(__dmul_rn(a, a), v.s8[lane * ns + j]);
+        den = __dadd_rn(den, __dmul_rn(Xj, fi));
+      }
+    }
+    const double inv = act ? __ddiv_rn(1.0, den) : 0.0;
+    const double mil = ordered_sum(act ? __dmul_rn(__dmul_rn(Xi, mi), inv) : 0.0, ns);
+    const double kl = ordered_sum(act ? __dmul_rn(__dmul_rn(Xi, ki), inv) : 0.0, ns);
+    if (lane == 0) { mu[cell] = mil; lam[cell] = kl; }
+  }
+}
+
 // ------------------------------------------------------------ handle glue
 struct TableHandle {
   TableLayout L;
@@ -451,6 +531,25 @@ cudaError_t table_cons2prim(void* p, int64_t n, int np, const double* cons, cons
   const int64_t cap = (int64_t)device_sms() * 16;
   if (blocks > cap) blocks = cap;
   k_cons2prim<<<(unsigned)blocks, 128, 0, st>>>(v, n, np, cons, T, prim, Tout);
+  count_launch();
+  return cudaGetLastError();
+}
+
+int table_has_transport(void* p) { return static_cast<TableHandle*>(p)->L.has_tr; }
+
+cudaError_t table_transport(void* p, int64_t n, const double* rhoi, const double* T, double* mu, double* lam,
+                            cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  auto* th = static_cast<TableHandle*>(p);
+  const TableLayout& L = th->L;
+  TransView v;
+  v.mu = th->dtabs + L.g_mu; v.kt = th->dtabs + L.g_kt; v.p4 = th->dtabs + L.g_p4; v.s8 = th->dtabs + L.g_s8;
+  v.wm = reinterpret_cast<const double*>(th->dimg + L.o_wm);
+  v.ns = L.ns; v.nsp = L.nsp; v.tmin = L.tmin; v.nrow = L.nrow_t;
+  int64_t blocks = (n + 7) / 8;
+  const int64_t cap = (int64_t)device_sms() * 8;
+  if (blocks > cap) blocks = cap;
+  k_transport<<<(unsigned)blocks, 256, 0, st>>>(v, n, rhoi, T, mu, lam);
   count_launch();
   return cudaGetLastError();
 }

@@ -43,7 +43,7 @@ class TableDesc(C.Structure):
                 ("ni1_arrh", _dp), ("ni2_arrh", _dp), ("eps_arrh", _dp),
                 ("ni1_troe", _dp), ("ni2_troe", _dp), ("eps_troe", _dp),
                 ("ni1_lind", _dp), ("ni2_lind", _dp), ("eps_lind", _dp),
-                ("runiv", C.c_double)]
+                ("runiv", C.c_double), ("mi_tab", _dp), ("k_tab", _dp)]
 
 
 class ReactorOpts(C.Structure):
@@ -114,6 +114,7 @@ def lib():
     L.flint_mech_create_tables.argtypes = [C.POINTER(TableDesc), C.POINTER(vp)]
     L.flint_rhs_native_batch.argtypes = [vp, i64, vp, vp, vp]
     L.flint_cons2prim_batch.argtypes = [vp, i64, C.c_int, vp, vp, vp, vp, vp]
+    L.flint_transport_batch.argtypes = [vp, i64, vp, vp, vp, vp, vp]
     L.flint_wdot_batch_host.argtypes = [vp, i64, C.c_int, vp, vp, vp, vp, vp, vp]
     L.flint_wdot_jac_batch_host.argtypes = [vp, i64, C.c_int, vp, vp, vp, vp, vp]
     L.flint_reactor_advance_host.argtypes = [vp, i64, vp, vp, vp, vp, C.POINTER(ReactorOpts), vp, vp]

@@ -39,7 +39,7 @@ _dp = C.POINTER(C.c_double)
 
 ARRAYS = ("wm", "cp_tab", "h_tab", "kf_tab", "kb_tab", "kinf_troe", "k0_troe", "kc_troe", "fcent_troe",
           "kinf_lind", "k0_lind", "kc_lind", "ni1_arrh", "ni2_arrh", "eps_arrh", "ni1_troe", "ni2_troe",
-          "eps_troe", "ni1_lind", "ni2_lind", "eps_lind")
+          "eps_troe", "ni1_lind", "ni2_lind", "eps_lind", "mi_tab", "k_tab")
 
 
 def table_desc(t):
@@ -280,6 +280,15 @@ def read_folder(folder, prefix=""):
         z = read_tecplot_points(P("chemistry-Lindemann.dat"))
         for i, nm in enumerate(("kinf_lind", "k0_lind", "kc_lind")):
             t[nm] = np.array([zz[1][:, 1 + i] for zz in z[:t["nr_lind"]]])
+    # transport.dat (read_idealgas_transport, Load_ThermoTransport.f90:129-174):
+    # optional; mu and k per species on the thermo rows (row 0 cloned likewise)
+    if os.path.exists(P("transport.dat")):
+        tr = read_tecplot_points(P("transport.dat"))
+        mu = np.array([z[1][:, 1] for z in tr[:ns]])
+        kt = np.array([z[1][:, 2] for z in tr[:ns]])
+        if mu.shape[1] == t["tmax"] - t["tmin"]:
+            mu = np.hstack([mu[:, :1], mu]); kt = np.hstack([kt[:, :1], kt])
+        t["mi_tab"], t["k_tab"] = mu, kt
     return t
 
 
@@ -327,6 +336,19 @@ class Tables:
         native.check(self.L.flint_rhs_native_batch(self.h, Z.shape[0], C.c_void_p(Z.data_ptr()),
                                                    C.c_void_p(F.data_ptr()), s), "flint_rhs_native_batch")
         return F
+
+    def transport(self, rhoi, T, mu=None, lam=None):
+        """Wilke mixture viscosity and conductivity over N cells: rhoi (N, ns), T (N,)."""
+        import torch
+        if mu is None:
+            mu = torch.empty_like(T)
+        if lam is None:
+            lam = torch.empty_like(T)
+        s = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+        native.check(self.L.flint_transport_batch(self.h, rhoi.shape[0], C.c_void_p(rhoi.data_ptr()),
+                                                  C.c_void_p(T.data_ptr()), C.c_void_p(mu.data_ptr()),
+                                                  C.c_void_p(lam.data_ptr()), s), "flint_transport_batch")
+        return mu, lam
 
     def cons2prim(self, cons, T, prim=None, T_out=None):
         """cons2prim over N cells: cons (N, ns+ndim+1) = (rho_i, rho u, rho E0) and

@@ -53,6 +53,14 @@ module FLINT_GPU
       integer(c_int64_t), value :: n
     end function
 
+    ! Wilke viscosity and conductivity over ncells on device arrays (rhoi: (ns, ncells))
+    integer(c_int) function flint_transport_batch(mech, n, rhoi, temp, mu, lambda, stream) &
+        bind(C, name='flint_transport_batch')
+      import :: c_int, c_int64_t, c_ptr
+      type(c_ptr), value :: mech, rhoi, temp, mu, lambda, stream
+      integer(c_int64_t), value :: n
+    end function
+
     ! cons2prim over ncells on device arrays (cons, prim: (ns+ndim+1, ncells))
     integer(c_int) function flint_cons2prim_batch(mech, n, ndim, cons, temp, prim, temp_out, stream) &
         bind(C, name='flint_cons2prim_batch')

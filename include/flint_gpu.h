@@ -130,6 +130,11 @@ typedef struct {
   const double* ni2_lind;
   const double* eps_lind;
   double runiv;                /* Runiv of the EOS terms (8314.51)             */
+  /* optional transport tables as read_idealgas_transport leaves them
+   * (Load_ThermoTransport.f90:129-174), rows tmin..tmax like cp_tab; NULL when
+   * the caller has none (flint_transport_batch then refuses)                  */
+  const double* mi_tab;        /* mi_tab(tmin:tmax, ns)  laminar viscosity, Pa s */
+  const double* k_tab;         /* k_tab(tmin:tmax, ns)   conductivity, W/m/K    */
 } flint_table_desc;
 
 /* Integrator options of the batched 0D reactor. */
@@ -189,6 +194,13 @@ int flint_chemistry_source_batch(flint_mech_t mech, int64_t n, double* roi,
  * energy equation from the tabulated h and cp; F = -1 for a cell whose T is
  * outside the thermo table or NaN, as the reference returns.  Tabulated handles. */
 int flint_rhs_native_batch(flint_mech_t mech, int64_t n, const double* Z, double* F, void* stream);
+
+/* Mixture laminar viscosity and conductivity by Wilke's rule over N cells:
+ * co_k_mi_lam_Wilke(rhoi, rho, T, milam, klam) (Lib_ThermoTransport.f90:407-462)
+ * with rho = sum(rhoi); rhoi cell-major (ns, N), T, mu, lambda (N).  Species
+ * values from the handle's mi_tab / k_tab.  Tabulated handles with transport. */
+int flint_transport_batch(flint_mech_t mech, int64_t n, const double* rhoi, const double* T, double* mu,
+                          double* lambda, void* stream);
 
 /* cons2prim(cons, T) over N cells (Lib_ThermoTransport.f90:129-165):
  * cons, prim cell-major, np = ns + ndim + 1 per cell; cons = (rho_1..rho_ns,

@@ -973,3 +973,51 @@ void orc_cons2prim_batch(const orc_table_mech* m, int64_t n, int np, const doubl
   for (int64_t i = 0; i < n; ++i)
     orc_cons2prim(m, np, cons + i * np, T[i], prim + i * np, Tout ? Tout + i : NULL, NULL);
 }
+
+/* ------------------------------------------------------------- transport */
+/* f_molecularWeight (Lib_ThermoTransport.f90:200-214): 1 / sum_s rhoi_s / rho / W_s. */
+static double wmol_f(const orc_table_mech* m, const double* r) {
+  double rho = sum_f(m->ns, r), res = 0.0;
+  for (int s = 0; s < m->ns; ++s) res = res + r[s] / rho / m->wm[s];
+  return 1.0 / res;
+}
+
+/* co_k_mi_lam_Wilke(rhoi, rho, T, milam, klam), Lib_ThermoTransport.f90:407-462,
+ * with its co_fiij (:350-362): Wilke's mixing rule on the tabulated species
+ * viscosities and conductivities. */
+void orc_transport(const orc_table_mech* m, const double* rhoi, double T, double* mu, double* lam) {
+  int ns = m->ns, nrows = m->tmax - m->tmin + 1, Ti = (int)T;
+  double Tdiff = T - Ti;
+  double rho = sum_f(ns, rhoi);
+  double Wmtot = wmol_f(m, rhoi);
+  double Xi[MAXNS], mi[MAXNS], ki[MAXNS], den[MAXNS];
+  for (int s = 0; s < ns; ++s) {
+    Xi[s] = rhoi[s] * Wmtot / (rho * m->wm[s]);
+    mi[s] = lerp_tab(m->mi_tab, m->tmin, nrows, s, Ti, Tdiff);
+    ki[s] = lerp_tab(m->k_tab, m->tmin, nrows, s, Ti, Tdiff);
+  }
+  for (int i = 0; i < ns; ++i) {
+    den[i] = 0.0;
+    for (int j = 0; j < ns; ++j) {
+      double MiMj = m->wm[i] / m->wm[j];
+      double a = 1.0 + sqrt(mi[i] / (mi[j] + 1e-20)) / pow(MiMj, 0.25);
+      double fi = a * a / sqrt(8.0 * (1.0 + MiMj));
+      den[i] = den[i] + Xi[j] * fi;
+    }
+  }
+  double mil = 0.0, kl = 0.0;
+  for (int s = 0; s < ns; ++s) {
+    double inv = 1.0 / den[s];
+    mil = mil + Xi[s] * mi[s] * inv;
+    kl = kl + Xi[s] * ki[s] * inv;
+  }
+  *mu = mil;
+  *lam = kl;
+}
+
+void orc_transport_batch(const orc_table_mech* m, int64_t n, const double* rhoi, const double* T, double* mu,
+                         double* lam, int nthreads) {
+  set_threads(nthreads);
+#pragma omp parallel for schedule(static)
+  for (int64_t i = 0; i < n; ++i) orc_transport(m, rhoi + i * m->ns, T[i], mu + i, lam + i);
+}

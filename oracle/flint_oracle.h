@@ -80,6 +80,12 @@ void orc_cons2prim(const orc_table_mech* m, int np, const double* cons, double T
 void orc_cons2prim_batch(const orc_table_mech* m, int64_t n, int np, const double* cons,
                          const double* T, double* prim, double* Tout, int nthreads);
 
+/* co_k_mi_lam_Wilke (Lib_ThermoTransport.f90:407-462): Wilke viscosity and
+ * conductivity from the tabulated species values; rho = sum(rhoi). */
+void orc_transport(const orc_table_mech* m, const double* rhoi, double T, double* mu, double* lam);
+void orc_transport_batch(const orc_table_mech* m, int64_t n, const double* rhoi, const double* T, double* mu,
+                         double* lam, int nthreads);
+
 int orc_max_threads(void);
 
 #ifdef __cplusplus

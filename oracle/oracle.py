@@ -44,6 +44,7 @@ def lib():
         L.orc_general_batch.argtypes = [td, i64, vp, vp, vp, C.c_int]
         L.orc_rhs_native_batch.argtypes = [td, i64, vp, vp, C.c_int]
         L.orc_cons2prim_batch.argtypes = [td, i64, C.c_int, vp, vp, vp, vp, C.c_int]
+        L.orc_transport_batch.argtypes = [td, i64, vp, vp, vp, vp, C.c_int]
         _lib = L
     return _lib
 
@@ -140,6 +141,14 @@ class TableOracle:
         F = np.zeros_like(Z)
         self.L.orc_rhs_native_batch(C.byref(self.desc), Z.shape[0], _vp(Z), _vp(F), nthreads)
         return F
+
+    def transport(self, rhoi, T, nthreads=0):
+        """co_k_mi_lam_Wilke over cells: rhoi (n, ns), T (n,) -> (mu, lambda)."""
+        rhoi = np.ascontiguousarray(rhoi, dtype=np.float64)
+        T = np.ascontiguousarray(T, dtype=np.float64)
+        mu, lam = np.zeros_like(T), np.zeros_like(T)
+        self.L.orc_transport_batch(C.byref(self.desc), rhoi.shape[0], _vp(rhoi), _vp(T), _vp(mu), _vp(lam), nthreads)
+        return mu, lam
 
     def cons2prim(self, cons, T, nthreads=0):
         """cons (n, ns + ndim + 1) -> (prim (same shape), last Newton T (n,))."""
