@@ -52,6 +52,12 @@ KINETICS_FLOPS = {"synthetic-31sp-160r": {"rhs": 20645.0, "jac": 47315.0},
                   "synthetic-54sp-320r": {"rhs": 36305.0, "jac": 97972.0}}
 
 
+# DRAM bytes (read + write) per cell of one k_reactor launch, from ncu
+# (profiles/k_reactor_c3_8192cells.md: 3.01 MB for 8,192 cells of the
+# 31-species workload); the traffic field scales it by the launch's cells.
+REACTOR_DRAM_BYTES_PER_CELL = {"synthetic-31sp-160r": 3.012608e6 / 8192}
+
+
 def fp64_ops(ev, ns, mech_name="synthetic-31sp-160r"):
     """FP64 FLOPs of a reactor launch from its event counters: kinetics per RHS
     and Jacobian evaluation (measured per state), (2/3) n^3 per LU factorization
@@ -279,7 +285,9 @@ def run_ours(args):
     peak = chem_peak_fp64()
     achieved = ops / t_step / 1e12
     roof = {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-            "frac": achieved / peak if peak else None, "traffic": None,
+            "frac": achieved / peak if peak else None,
+            "traffic": (REACTOR_DRAM_BYTES_PER_CELL[mech.name] * n if mech.name in REACTOR_DRAM_BYTES_PER_CELL
+                        else None),
             "kernel": "k_reactor", "peak_source": "DFMA probe kernel measured in this run (MEASURED_PEAKS.json has no FP64 figure)",
             "ops_per_launch": ops, "events_per_launch": s}
     line = {"metric": METRIC, "value": value, "unit": "cell-steps/s", "n_gpus": ws, "steps": args.steps,
@@ -482,7 +490,10 @@ def run_surrogate(args):
             "gpu_launches": launches, "clocks": clk,
             "roofline": {"bound": "fp64", "kernel": "k_reactor (the fallback: rejected cells, timed alone)",
                          "achieved": ops / t_fb / 1e12, "peak": peak, "unit": "TFLOP/s",
-                         "frac": (ops / t_fb / 1e12) / peak if peak else None, "traffic": None,
+                         "frac": (ops / t_fb / 1e12) / peak if peak else None,
+                         "traffic": (REACTOR_DRAM_BYTES_PER_CELL[chem.mech.name] * int(ridx.numel())
+                                     if chem.mech.name in REACTOR_DRAM_BYTES_PER_CELL else None),
+                         "traffic_note": "ncu DRAM bytes per cell of a k_reactor launch x cells of this launch",
                          "peak_source": "DFMA probe kernel measured in this run (MEASURED_PEAKS.json has no FP64 figure)",
                          "kernel_seconds": t_fb, "share_of_step": t_fb / t_sur, "fallback_cells": int(ridx.numel()),
                          "events_per_launch": fbk, "ops_per_launch": ops,
