@@ -56,6 +56,7 @@ struct flint_mech_s {
   // saved-Jacobian scratch of the reactor, one slot per resident warp
   double* djsave = nullptr;
   int jslots = 0;
+  int rx_layout = 0;       // reactor layout chosen by flint_reactor_autotune (0: by size)
   // Jacobian work area of the warp kernels for 32-63 species
   double* dwscratch = nullptr;
   // staging buffers of the *_host entry points (grow only)
@@ -212,6 +213,8 @@ static int ensure_stage(flint_mech_s* h, size_t bytes) {
 }  // namespace flint
 
 extern "C" {
+
+static int ensure_jsave(flint_mech_t h);   // the reactor's per-warp scratch, allocated on first use
 
 const char* flint_last_error(void) { return g_err.c_str(); }
 const char* flint_version(void) { return "flint_gb300 0.1.0 sm_103a"; }
@@ -395,16 +398,61 @@ int flint_reactor_advance(flint_mech_t h, int64_t n, double* T, const double* p,
   if (!(o.rtol > 0.0) || !(o.atol > 0.0) || o.max_steps < 1 || o.max_order < 1 || o.max_order > 5)
     return fail(FLINT_ERR_ARG, "reactor options out of range");
   if (o.constant_volume) return fail(FLINT_ERR_ARG, "constant-volume reactor is not in this build");
-  if (!h->djsave) {
-    int slots = reactor_slots(h->L);
-    if (slots < 1) return fail(FLINT_ERR_MECH, "reactor kernel does not fit this mechanism (shared memory)");
-    cudaError_t ea = cudaMalloc(&h->djsave, (size_t)slots * reactor_slot_bytes(h->L));
-    if (ea != cudaSuccess) { h->djsave = nullptr; return fail(FLINT_ERR_NOMEM, "reactor scratch: %s", cudaGetErrorString(ea)); }
-    h->jslots = slots;
-  }
+  rc = ensure_jsave(h);
+  if (rc) return rc;
   cudaError_t e = launch_reactor(h->dimg, h->L, n, T, p, Y, dt, o, status, nsteps, h->dcounter, h->djsave,
-                                 h->jslots, (cudaStream_t)stream);
+                                 h->jslots, (cudaStream_t)stream, nullptr, h->rx_layout);
   return e == cudaSuccess ? FLINT_OK : cuda_fail(e, "flint_reactor_advance");
+}
+
+int flint_reactor_autotune(flint_mech_t h, int64_t n, const double* T, const double* p, const double* Y,
+                           const double* dt, const flint_reactor_opts* opts, int* layout_out, void* stream) {
+  int rc = check_common(h, n, FLINT_CELL_MAJOR);
+  if (rc) return rc;
+  if (!T || !p || !Y || !dt) return fail(FLINT_ERR_ARG, "NULL array");
+  flint_reactor_opts o;
+  if (opts) o = *opts; else flint_reactor_default_opts(&o);
+  if (!(o.rtol > 0.0) || !(o.atol > 0.0) || o.max_steps < 1 || o.max_order < 1 || o.max_order > 5)
+    return fail(FLINT_ERR_ARG, "reactor options out of range");
+  rc = ensure_jsave(h);
+  if (rc) return rc;
+  h->rx_layout = REACTOR_LAYOUT_AUTO;
+  if (n > 0 && reactor_layout_choice(h->L)) {
+    // time the sample under each layout on private copies (the caller's arrays stay as they are)
+    cudaStream_t st = (cudaStream_t)stream;
+    const int ns = h->L.ns;
+    double *Tc = nullptr, *Yc = nullptr;
+    int *sc = nullptr, *nc = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    cudaError_t e = cudaMalloc(&Tc, n * sizeof(double));
+    if (!e) e = cudaMalloc(&Yc, n * ns * sizeof(double));
+    if (!e) e = cudaMalloc(&sc, n * sizeof(int));
+    if (!e) e = cudaMalloc(&nc, n * sizeof(int));
+    if (!e) e = cudaEventCreate(&e0);
+    if (!e) e = cudaEventCreate(&e1);
+    const int cand[2] = {REACTOR_LAYOUT_SHARED, REACTOR_LAYOUT_GLOBAL};
+    float best = 0.f;
+    for (int c = 0; c < 2 && !e; ++c) {
+      for (int rep = 0; rep < 2 && !e; ++rep) {   // the first run of each layout warms up
+        e = cudaMemcpyAsync(Tc, T, n * sizeof(double), cudaMemcpyDeviceToDevice, st);
+        if (!e) e = cudaMemcpyAsync(Yc, Y, n * ns * sizeof(double), cudaMemcpyDeviceToDevice, st);
+        if (!e) e = cudaEventRecord(e0, st);
+        if (!e) e = launch_reactor(h->dimg, h->L, n, Tc, p, Yc, dt, o, sc, nc, h->dcounter, h->djsave, h->jslots,
+                                   st, nullptr, cand[c]);
+        if (!e) e = cudaEventRecord(e1, st);
+        if (!e) e = cudaEventSynchronize(e1);
+      }
+      float ms = 0.f;
+      if (!e) e = cudaEventElapsedTime(&ms, e0, e1);
+      if (!e && (c == 0 || ms < best)) { best = ms; h->rx_layout = cand[c]; }
+    }
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    cudaFree(Tc); cudaFree(Yc); cudaFree(sc); cudaFree(nc);
+    if (e) { h->rx_layout = REACTOR_LAYOUT_AUTO; return cuda_fail(e, "flint_reactor_autotune"); }
+  }
+  if (layout_out) *layout_out = h->rx_layout;
+  return FLINT_OK;
 }
 
 int flint_reactor_advance_noalloc(flint_mech_t h, int64_t n, double* T, const double* p, double* Y, const double* dt,
@@ -513,7 +561,7 @@ int flint_surrogate_advance(flint_surrogate_t s, int64_t n, double* T, const dou
   rc = ensure_jsave(s->mech);
   if (rc) return rc;
   rc = surrogate_advance(s->s, n, T, p, Y, dt, o, gate, status, nsteps, s->mech->djsave, s->mech->jslots,
-                         nullptr, counts != nullptr, (cudaStream_t)stream);
+                         nullptr, counts != nullptr, (cudaStream_t)stream, s->mech->rx_layout);
   if (rc) return fail(rc, "flint_surrogate_advance failed: %s", cudaGetErrorString(cudaGetLastError()));
   if (counts) surrogate_counts(s->s, &counts[0], &counts[1]);
   return FLINT_OK;

@@ -37,10 +37,15 @@ cudaError_t launch_rhs(const uint8_t* img, const ImageLayout& L, int64_t n, cons
                        const double* Y, double* f, cudaStream_t st);
 int reactor_slots(const ImageLayout& L);
 size_t reactor_slot_bytes(const ImageLayout& L);
+// Reactor layouts: the Newton matrix in shared memory or in the warp's global slot.
+enum { REACTOR_LAYOUT_AUTO = 0, REACTOR_LAYOUT_SHARED = 1, REACTOR_LAYOUT_GLOBAL = 2 };
+// true when both layouts are possible for this mechanism (what the autotuner chooses between)
+bool reactor_layout_choice(const ImageLayout& L);
 cudaError_t launch_reactor(const uint8_t* img, const ImageLayout& L, int64_t n, double* T, const double* p,
                            double* Y, const double* dt, const flint_reactor_opts& o, int* status, int* nsteps,
                            unsigned int* work_counter, double* jsave, int slots, cudaStream_t st,
-                           const unsigned long long* n_dev = nullptr);   // optional device-side cell count <= n
+                           const unsigned long long* n_dev = nullptr,   // optional device-side cell count <= n
+                           int layout = REACTOR_LAYOUT_AUTO);
 
 size_t reactor_noalloc_bytes();
 int reactor_noalloc_slots();
@@ -65,7 +70,8 @@ int surrogate_train_step(Surrogate* s, int net, int64_t n, const float* X, const
 int surrogate_state(Surrogate* s, int net, float* host, int64_t* step, int get);
 int surrogate_advance(Surrogate* s, int64_t n, double* T, const double* p, double* Y, const double* dt,
                       const flint_reactor_opts& o, const flint_surrogate_gate* gate, int* status, int* nsteps,
-                      double* jsave, int jslots, double* metrics, bool want_counts, cudaStream_t st);
+                      double* jsave, int jslots, double* metrics, bool want_counts, cudaStream_t st,
+                      int reactor_layout = REACTOR_LAYOUT_AUTO);
 void surrogate_counts(Surrogate* s, int64_t* acc, int64_t* rej);
 int surrogate_read_counts(Surrogate* s, int64_t* acc, int64_t* rej);
 

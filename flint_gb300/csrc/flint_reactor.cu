@@ -25,6 +25,7 @@
 // pivot order instead of swapping rows.  Step-size factors eta = (c*dsm)^(-1/(q+1))
 // are heuristics and are evaluated in FP32 (the oracle does the same); every
 // quantity of the solution itself stays FP64.
+#include <algorithm>
 #include <mutex>
 
 #include "flint_dev.cuh"
@@ -228,13 +229,18 @@ static size_t reactor_smem_spl1(const ImageLayout& L) {
   return L.bytes + (REACTOR_THREADS / 32) * (scratch_doubles(L.nsp, L.nrpad, true) * sizeof(double) + 64 * sizeof(int));
 }
 
-static bool reactor_gj(const ImageLayout& L) { return spl_of(L) > 1 || reactor_smem_spl1(L) > device_smem_optin(); }
+// layout: REACTOR_LAYOUT_AUTO picks shared memory whenever the block fits;
+// REACTOR_LAYOUT_SHARED / _GLOBAL force one (the autotuner times both).
+static bool reactor_gj(const ImageLayout& L, int layout = REACTOR_LAYOUT_AUTO) {
+  if (spl_of(L) > 1 || reactor_smem_spl1(L) > device_smem_optin()) return true;
+  return layout == REACTOR_LAYOUT_GLOBAL;
+}
 
 // Doubles per resident-warp slot of the reactor's global scratch: the saved
 // Jacobian (32*SPL)^2, and in GJ layout the Jacobian work area too.
-static int64_t reactor_slot_doubles_of(const ImageLayout& L) {
+static int64_t reactor_slot_doubles_of(const ImageLayout& L, int layout = REACTOR_LAYOUT_AUTO) {
   const int spl = spl_of(L);
-  return (int64_t)(32 * spl) * (32 * spl) + (reactor_gj(L) ? scratch_jac_doubles(L.nsp, L.nrpad) : 0);
+  return (int64_t)(32 * spl) * (32 * spl) + (reactor_gj(L, layout) ? scratch_jac_doubles(L.nsp, L.nrpad) : 0);
 }
 
 template <int SPL, bool GJ>
@@ -555,37 +561,49 @@ k_reactor(const uint8_t* __restrict__ img, ImageLayout L, int64_t n, double* __r
   }
 }
 
-size_t reactor_smem(const ImageLayout& L) {
-  if (!reactor_gj(L)) return reactor_smem_spl1(L);
+size_t reactor_smem(const ImageLayout& L, int layout = REACTOR_LAYOUT_AUTO) {
+  if (!reactor_gj(L, layout)) return reactor_smem_spl1(L);
   return L.bytes + (REACTOR_THREADS / 32) *
                        (scratch_small_doubles(L.nsp, L.nrpad) * sizeof(double) + 64 * spl_of(L) * sizeof(int));
 }
 
-static const void* reactor_fn(const ImageLayout& L) {
+static const void* reactor_fn(const ImageLayout& L, int layout = REACTOR_LAYOUT_AUTO) {
   if (spl_of(L) > 1) return (const void*)k_reactor<2, true>;
-  return reactor_gj(L) ? (const void*)k_reactor<1, true> : (const void*)k_reactor<1, false>;
+  return reactor_gj(L, layout) ? (const void*)k_reactor<1, true> : (const void*)k_reactor<1, false>;
 }
 
-int reactor_slots(const ImageLayout& L) {
-  if (spl_of(L) < 1 || spl_of(L) > 2) return 0;
-  size_t sm = reactor_smem(L);
-  const void* fn = reactor_fn(L);
+static int slots_of(const ImageLayout& L, int layout) {
+  size_t sm = reactor_smem(L, layout);
+  const void* fn = reactor_fn(L, layout);
   if (set_smem(fn, sm) != cudaSuccess) return 0;
   int per_sm = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, REACTOR_THREADS, sm);
   return per_sm * device_sms() * (REACTOR_THREADS / 32);
 }
 
-size_t reactor_slot_bytes(const ImageLayout& L) { return (size_t)reactor_slot_doubles_of(L) * sizeof(double); }
+// Resident-warp slots and bytes per slot that serve every layout.
+int reactor_slots(const ImageLayout& L) {
+  if (spl_of(L) < 1 || spl_of(L) > 2) return 0;
+  return std::max(slots_of(L, REACTOR_LAYOUT_AUTO), slots_of(L, REACTOR_LAYOUT_GLOBAL));
+}
+
+size_t reactor_slot_bytes(const ImageLayout& L) {
+  return (size_t)std::max(reactor_slot_doubles_of(L, REACTOR_LAYOUT_AUTO), reactor_slot_doubles_of(L, REACTOR_LAYOUT_GLOBAL)) *
+         sizeof(double);
+}
+
+bool reactor_layout_choice(const ImageLayout& L) {
+  return spl_of(L) == 1 && reactor_smem_spl1(L) <= device_smem_optin();
+}
 
 cudaError_t launch_reactor(const uint8_t* img, const ImageLayout& L, int64_t n, double* T, const double* p,
                            double* Y, const double* dt, const flint_reactor_opts& o, int* status, int* nsteps,
                            unsigned int* work_counter, double* jsave, int slots, cudaStream_t st,
-                           const unsigned long long* n_dev) {
+                           const unsigned long long* n_dev, int layout) {
   if (n <= 0) return cudaSuccess;
   if (spl_of(L) < 1 || spl_of(L) > 2) return cudaErrorInvalidValue;
-  size_t sm = reactor_smem(L);
-  const void* fn = reactor_fn(L);
+  size_t sm = reactor_smem(L, layout);
+  const void* fn = reactor_fn(L, layout);
   cudaError_t e = set_smem(fn, sm);
   if (e != cudaSuccess) return e;
   int per_sm = 0;
@@ -616,12 +634,12 @@ cudaError_t launch_reactor(const uint8_t* img, const ImageLayout& L, int64_t n, 
   }
   e = cudaMemsetAsync(work_counter, 0, NCOUNTERS * sizeof(unsigned long long), st);
   if (e != cudaSuccess) return e;
-  const int64_t sd = reactor_slot_doubles_of(L);
+  const int64_t sd = reactor_slot_doubles_of(L, layout);
   unsigned long long* wc = reinterpret_cast<unsigned long long*>(work_counter);
   if (spl_of(L) > 1)
     k_reactor<2, true><<<(unsigned)blocks, REACTOR_THREADS, sm, st>>>(img, L, n, T, p, Y, dt, o, status, nsteps, wc,
                                                                        jsave, sd, n_dev);
-  else if (reactor_gj(L))
+  else if (reactor_gj(L, layout))
     k_reactor<1, true><<<(unsigned)blocks, REACTOR_THREADS, sm, st>>>(img, L, n, T, p, Y, dt, o, status, nsteps, wc,
                                                                        jsave, sd, n_dev);
   else

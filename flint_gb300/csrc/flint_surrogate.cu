@@ -587,7 +587,8 @@ int64_t surrogate_nparams(Surrogate* s) { return s->net[0].P; }
 
 int surrogate_advance(Surrogate* s, int64_t n, double* T, const double* p, double* Y, const double* dt,
                       const flint_reactor_opts& o, const flint_surrogate_gate* gate, int* status, int* nsteps,
-                      double* jsave, int jslots, double* metrics, bool want_counts, cudaStream_t st) {
+                      double* jsave, int jslots, double* metrics, bool want_counts, cudaStream_t st,
+                      int reactor_layout) {
   s->last_accepted = s->last_rejected = 0;
   s->last_n = 0;
   if (n <= 0) return 0;
@@ -621,7 +622,7 @@ int surrogate_advance(Surrogate* s, int64_t n, double* T, const double* p, doubl
                                                 s->cdt);
   count_launch();
   cudaError_t e = launch_reactor(s->mimg, s->L, n, s->cT, s->cp, s->cY, s->cdt, o, s->cst, s->cns, s->counter, jsave,
-                                 jslots, st, s->rej_count);
+                                 jslots, st, s->rej_count, reactor_layout);
   if (e) return FLINT_ERR_CUDA;
   k_scatter<<<blocks_for(n, 256), 256, 0, st>>>(s->rej_count, s->rej_idx, s->ns, T, Y, s->cT, s->cY, s->cst, s->cns,
                                                  status, nsteps);

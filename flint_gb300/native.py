@@ -106,6 +106,7 @@ def lib():
     L.flint_wdot_jac_batch.argtypes = [vp, i64, C.c_int, vp, vp, vp, vp, vp, vp]
     L.flint_rhs_constp_batch.argtypes = [vp, i64, vp, vp, vp, vp, vp]
     L.flint_reactor_advance.argtypes = [vp, i64, vp, vp, vp, vp, C.POINTER(ReactorOpts), vp, vp, vp]
+    L.flint_reactor_autotune.argtypes = [vp, i64, vp, vp, vp, vp, C.POINTER(ReactorOpts), C.POINTER(C.c_int), vp]
     L.flint_reactor_default_opts.argtypes = [C.POINTER(ReactorOpts)]
     L.flint_reactor_advance_noalloc.argtypes = [vp, i64, vp, vp, vp, vp, C.POINTER(ReactorOpts), vp, vp, vp]
     L.flint_reactor_stats.argtypes = [vp, C.POINTER(C.c_int64)]

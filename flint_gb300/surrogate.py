@@ -442,6 +442,8 @@ def main():
                                                         "val_cells": int(v["T0"].shape[0]), "margin": args.margin}
         rep["gate"] = sur.gate
         rep["diagnostics"] = getattr(calibrate, "diag", {})
+        if getattr(calibrate, "data", None) is not None:
+            np.savez_compressed(os.path.splitext(args.out)[0] + "_val.npz", **calibrate.data)
         sur.save(args.out, extra=rep, inference_only=bool(sur.header.get("inference_only")))
         print(json.dumps(rep["calibration"]))
         return

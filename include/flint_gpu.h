@@ -234,6 +234,16 @@ int flint_reactor_advance(flint_mech_t mech, int64_t n, double* T, const double*
                           double* Y, const double* dt, const flint_reactor_opts* opts,
                           int* status, int* nsteps, void* stream);
 
+/* Empirical choice of the reactor's layout for this mechanism: the Newton
+ * matrix and Jacobian work area in shared memory (one block of 8 warps per SM)
+ * or in each warp's global slot (shared memory left to the L1 cache).  Times
+ * flint_reactor_advance under each on a sample of cells (n of them, device
+ * arrays; the caller's arrays are not modified), keeps the faster for later
+ * calls on this handle, and reports it in *layout (1 shared, 2 global; 0 when
+ * the mechanism allows only one).  No reference counterpart. */
+int flint_reactor_autotune(flint_mech_t mech, int64_t n, const double* T, const double* p, const double* Y,
+                           const double* dt, const flint_reactor_opts* opts, int* layout, void* stream);
+
 /* flint_reactor_advance without any device allocation.  No counterpart in the
  * reference.  For callers that must not have a library call cudaMalloc: CFD
  * codes that hand their whole device memory to their own pool at start-up and

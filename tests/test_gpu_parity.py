@@ -348,3 +348,25 @@ def tsr_rich_states(mech, n, seed):
     p = rng.uniform(1.0, 20.0, n) * 101325.0
     dt = 10.0 ** rng.uniform(-5.0, -3.0, n)
     return T, p, Y, dt
+
+
+@pytest.mark.parametrize("cfg", ["c2", "c5"])
+def test_reactor_autotune(cfg):
+    """The autotuner times the shared-memory and global-slot layouts and keeps
+    the faster; both layouts compute the same numbers."""
+    mech = mechgen.load(cfg)
+    states = mechgen.c5_states if cfg == "c5" else mechgen.c3_states
+    T, p, Y, dt = states(256, mech, seed=91)
+    chem = Chemistry(mech)
+    Tt, pt, Yt, dtt = cuda(T, p, Y, dt)
+    Ta, Ya = Tt.clone(), Yt.clone()
+    sa, na = chem.reactor_advance(Ta, pt, Ya, dtt)
+    lay = chem.reactor_autotune(Tt, pt, Yt, dtt)
+    torch.cuda.synchronize()
+    assert np.array_equal(Tt.cpu().numpy(), T) and np.array_equal(Yt.cpu().numpy(), Y)   # inputs untouched
+    assert lay in ((1, 2) if cfg == "c2" else (0,))
+    sb, nb = chem.reactor_advance(Tt, pt, Yt, dtt)
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(Tt.cpu().numpy(), Ta.cpu().numpy())
+    np.testing.assert_array_equal(Yt.cpu().numpy(), Ya.cpu().numpy())
+    np.testing.assert_array_equal(nb.cpu().numpy(), na.cpu().numpy())
