@@ -581,6 +581,16 @@ def run_kernel_workload(args):
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
     stream = torch.cuda.current_stream()
     gen = None
+    tab = None
+    if args.workload == "c2-general":
+        # FLINT's tabulated path: the general loop on 1-K tables of the same mechanism
+        from flint_gb300 import tables
+        tab = tables.Tables(tables.generate(chem.mech, 300, 3000))
+        Tc = np.clip(T, 300.0, 2990.0)
+        W = np.array([sp.mw for sp in chem.mech.species])
+        rho = p / (chem.mech.r_eos * Tc * (Y / W).sum(1))
+        roi_d = torch.from_numpy(rho[:, None] * Y).to(dev)
+        Tc_d = torch.from_numpy(Tc).to(dev)
     if args.generated:
         if jac is not None:
             raise SystemExit("--generated covers wdot/cp/h only")
@@ -588,7 +598,9 @@ def run_kernel_workload(args):
         gen = GeneratedMechanism(chem.mech)
 
     def step():
-        if gen is not None:
+        if tab is not None:
+            tab.chemistry_source(roi_d, Tc_d, omegadot=w)
+        elif gen is not None:
             gen.wdot(Td, pd, Yd, wdot=w, cp=cp, h=h)
         elif jac is None:
             chem.wdot(Td, pd, Yd, wdot=w, cp=cp, h=h)
@@ -610,7 +622,7 @@ def run_kernel_workload(args):
     bytes_per_state = 8 * (2 + 2 * chem.ns) + (8 * nv * nv if jac is not None else 16)
     roof = None
     kf = KINETICS_FLOPS.get(chem.mech.name)
-    if kf is not None and gen is None:
+    if kf is not None and gen is None and tab is None:
         fl = kf["jac" if jac is not None else "rhs"]
         peak = chem_peak_fp64()
         roof = {"bound": "fp64", "kernel": f"k_wdot_warp<{int(jac is not None)}>",
@@ -618,7 +630,8 @@ def run_kernel_workload(args):
                 "frac": (n * fl / t / 1e12) / peak if peak else None,
                 "peak_source": "DFMA probe kernel measured in this run",
                 "hbm_gbs_algorithmic": n * bytes_per_state / t / 1e9}
-    print(json.dumps({"workload": args.workload, "kernel": "generated (ytf_cuda)" if gen else "data-driven",
+    print(json.dumps({"workload": args.workload,
+                      "kernel": "generated (ytf_cuda)" if gen else ("tabulated general loop" if tab else "data-driven"),
                       "metric": "states/s", "value": n / t, "unit": "states/s",
                       "ms_per_step": t * 1e3, "states": n, "steps": args.steps, "warmup": args.warmup,
                       "gpu_launches": kernel_launches() - l0,
@@ -645,7 +658,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cells", type=int, default=None)
     ap.add_argument("--workload", default="reactor",
-                    choices=["reactor", "reactor-c5", "c1-wdot", "c2-wdot", "c2-wdotjac", "c5-wdot", "c5-wdotjac"])
+                    choices=["reactor", "reactor-c5", "c1-wdot", "c2-wdot", "c2-wdotjac", "c5-wdot", "c5-wdotjac",
+                             "c2-general"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--generated", action="store_true",
                     help="source-term workloads: run the per-mechanism generated kernel (ytf_cuda)")
