@@ -331,7 +331,7 @@ def run_ours(args):
                         "cells_per_gpu": n, "mechanism": "synthetic-31sp-160r (12 third-body, 6 Troe)"})
                       | {"path": "plain FP64 integrator", "l2": "flushed (256 MiB write) between timed steps",
                          "cuda_graph": graph_note,
-                         "reactor_layout": {0: "only one", 1: "shared memory", 2: "global slot"}[layout]
+                         "reactor_layout": {0: "by size", 1: "shared memory", 2: "global slot, 8 warps/block", 3: "global slot, 4 warps/block"}[layout]
                          + " (autotuned on 16,384 cells)"},
             "e2e": {"value": n * ws / e2e_t, "unit": "cell-steps/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
@@ -514,7 +514,7 @@ def run_surrogate(args):
                        "network": (f"MLP {'-'.join(str(d) for d in sur.dims)} GELU x{sur.n_nets} (ensemble), "
                                    "split-bf16 mma.sync forward, fp32 accumulate"),
                        "l2": "flushed (256 MiB write) between timed steps", "cuda_graph": graph_note,
-                       "reactor_layout": {0: "only one", 1: "shared memory", 2: "global slot"}[layout]
+                       "reactor_layout": {0: "by size", 1: "shared memory", 2: "global slot, 8 warps/block", 3: "global slot, 4 warps/block"}[layout]
                        + " (autotuned on 16,384 cells)"},
             "surrogate": {"accepted": int(acc), "rejected": int(rej), "accept_frac": acc / max(acc + rej, 1),
                           "plain_fp64_cell_steps_per_s": plain, "plain_sample_cells": m,

@@ -143,9 +143,9 @@ class Chemistry:
 
     # --------------------------------------------------------------- reactor
     def reactor_autotune(self, T, p, Y, dt, rtol=1e-8, atol=1e-14, max_steps=20000, max_order=5):
-        """Time the reactor's two layouts on these cells (device tensors, left
-        unchanged) and keep the faster for this handle; returns the layout
-        (1 shared memory, 2 global slot, 0 when only one exists)."""
+        """Time the reactor's layouts on these cells (device tensors, left
+        unchanged) and keep the fastest for this handle; returns the layout
+        (1 shared memory, 2 global slot / 8 warps per block, 3 global slot / 4 warps)."""
         opts = native.reactor_opts(rtol, atol, max_steps, max_order)
         lay = C.c_int(0)
         native.check(self.L.flint_reactor_autotune(self.h, T.shape[0], _dptr(T), _dptr(p), _dptr(Y), _dptr(dt),

@@ -417,27 +417,28 @@ int flint_reactor_autotune(flint_mech_t h, int64_t n, const double* T, const dou
   rc = ensure_jsave(h);
   if (rc) return rc;
   h->rx_layout = REACTOR_LAYOUT_AUTO;
-  if (n > 0 && reactor_layout_choice(h->L)) {
+  int cand[4];
+  const int nc = reactor_layout_candidates(h->L, cand);
+  if (n > 0) {
     // time the sample under each layout on private copies (the caller's arrays stay as they are)
     cudaStream_t st = (cudaStream_t)stream;
     const int ns = h->L.ns;
     double *Tc = nullptr, *Yc = nullptr;
-    int *sc = nullptr, *nc = nullptr;
+    int *sc = nullptr, *nsc = nullptr;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     cudaError_t e = cudaMalloc(&Tc, n * sizeof(double));
     if (!e) e = cudaMalloc(&Yc, n * ns * sizeof(double));
     if (!e) e = cudaMalloc(&sc, n * sizeof(int));
-    if (!e) e = cudaMalloc(&nc, n * sizeof(int));
+    if (!e) e = cudaMalloc(&nsc, n * sizeof(int));
     if (!e) e = cudaEventCreate(&e0);
     if (!e) e = cudaEventCreate(&e1);
-    const int cand[2] = {REACTOR_LAYOUT_SHARED, REACTOR_LAYOUT_GLOBAL};
     float best = 0.f;
-    for (int c = 0; c < 2 && !e; ++c) {
+    for (int c = 0; c < nc && !e; ++c) {
       for (int rep = 0; rep < 2 && !e; ++rep) {   // the first run of each layout warms up
         e = cudaMemcpyAsync(Tc, T, n * sizeof(double), cudaMemcpyDeviceToDevice, st);
         if (!e) e = cudaMemcpyAsync(Yc, Y, n * ns * sizeof(double), cudaMemcpyDeviceToDevice, st);
         if (!e) e = cudaEventRecord(e0, st);
-        if (!e) e = launch_reactor(h->dimg, h->L, n, Tc, p, Yc, dt, o, sc, nc, h->dcounter, h->djsave, h->jslots,
+        if (!e) e = launch_reactor(h->dimg, h->L, n, Tc, p, Yc, dt, o, sc, nsc, h->dcounter, h->djsave, h->jslots,
                                    st, nullptr, cand[c]);
         if (!e) e = cudaEventRecord(e1, st);
         if (!e) e = cudaEventSynchronize(e1);
@@ -448,7 +449,7 @@ int flint_reactor_autotune(flint_mech_t h, int64_t n, const double* T, const dou
     }
     if (e0) cudaEventDestroy(e0);
     if (e1) cudaEventDestroy(e1);
-    cudaFree(Tc); cudaFree(Yc); cudaFree(sc); cudaFree(nc);
+    cudaFree(Tc); cudaFree(Yc); cudaFree(sc); cudaFree(nsc);
     if (e) { h->rx_layout = REACTOR_LAYOUT_AUTO; return cuda_fail(e, "flint_reactor_autotune"); }
   }
   if (layout_out) *layout_out = h->rx_layout;

@@ -37,10 +37,11 @@ cudaError_t launch_rhs(const uint8_t* img, const ImageLayout& L, int64_t n, cons
                        const double* Y, double* f, cudaStream_t st);
 int reactor_slots(const ImageLayout& L);
 size_t reactor_slot_bytes(const ImageLayout& L);
-// Reactor layouts: the Newton matrix in shared memory or in the warp's global slot.
-enum { REACTOR_LAYOUT_AUTO = 0, REACTOR_LAYOUT_SHARED = 1, REACTOR_LAYOUT_GLOBAL = 2 };
-// true when both layouts are possible for this mechanism (what the autotuner chooses between)
-bool reactor_layout_choice(const ImageLayout& L);
+// Reactor layouts: the Newton matrix in shared memory (8 warps per block) or in
+// the warp's global slot (8 or 4 warps per block).
+enum { REACTOR_LAYOUT_AUTO = 0, REACTOR_LAYOUT_SHARED = 1, REACTOR_LAYOUT_GLOBAL = 2, REACTOR_LAYOUT_GLOBAL4 = 3 };
+// The layouts possible for this mechanism (what the autotuner chooses between); returns their count.
+int reactor_layout_candidates(const ImageLayout& L, int* out);
 cudaError_t launch_reactor(const uint8_t* img, const ImageLayout& L, int64_t n, double* T, const double* p,
                            double* Y, const double* dt, const flint_reactor_opts& o, int* status, int* nsteps,
                            unsigned int* work_counter, double* jsave, int slots, cudaStream_t st,

@@ -233,8 +233,12 @@ static size_t reactor_smem_spl1(const ImageLayout& L) {
 // REACTOR_LAYOUT_SHARED / _GLOBAL force one (the autotuner times both).
 static bool reactor_gj(const ImageLayout& L, int layout = REACTOR_LAYOUT_AUTO) {
   if (spl_of(L) > 1 || reactor_smem_spl1(L) > device_smem_optin()) return true;
-  return layout == REACTOR_LAYOUT_GLOBAL;
+  return layout == REACTOR_LAYOUT_GLOBAL || layout == REACTOR_LAYOUT_GLOBAL4;
 }
+
+// Threads per block: 8 warps, or 4 in the GLOBAL4 layout (half the resident
+// warps, twice the L1 per warp for the global Newton matrices).
+static int reactor_threads(int layout) { return layout == REACTOR_LAYOUT_GLOBAL4 ? 128 : REACTOR_THREADS; }
 
 // Doubles per resident-warp slot of the reactor's global scratch: the saved
 // Jacobian (32*SPL)^2, and in GJ layout the Jacobian work area too.
@@ -563,7 +567,7 @@ k_reactor(const uint8_t* __restrict__ img, ImageLayout L, int64_t n, double* __r
 
 size_t reactor_smem(const ImageLayout& L, int layout = REACTOR_LAYOUT_AUTO) {
   if (!reactor_gj(L, layout)) return reactor_smem_spl1(L);
-  return L.bytes + (REACTOR_THREADS / 32) *
+  return L.bytes + (reactor_threads(layout) / 32) *
                        (scratch_small_doubles(L.nsp, L.nrpad) * sizeof(double) + 64 * spl_of(L) * sizeof(int));
 }
 
@@ -577,14 +581,15 @@ static int slots_of(const ImageLayout& L, int layout) {
   const void* fn = reactor_fn(L, layout);
   if (set_smem(fn, sm) != cudaSuccess) return 0;
   int per_sm = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, REACTOR_THREADS, sm);
-  return per_sm * device_sms() * (REACTOR_THREADS / 32);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, reactor_threads(layout), sm);
+  return per_sm * device_sms() * (reactor_threads(layout) / 32);
 }
 
 // Resident-warp slots and bytes per slot that serve every layout.
 int reactor_slots(const ImageLayout& L) {
   if (spl_of(L) < 1 || spl_of(L) > 2) return 0;
-  return std::max(slots_of(L, REACTOR_LAYOUT_AUTO), slots_of(L, REACTOR_LAYOUT_GLOBAL));
+  return std::max(slots_of(L, REACTOR_LAYOUT_AUTO),
+                  std::max(slots_of(L, REACTOR_LAYOUT_GLOBAL), slots_of(L, REACTOR_LAYOUT_GLOBAL4)));
 }
 
 size_t reactor_slot_bytes(const ImageLayout& L) {
@@ -592,8 +597,12 @@ size_t reactor_slot_bytes(const ImageLayout& L) {
          sizeof(double);
 }
 
-bool reactor_layout_choice(const ImageLayout& L) {
-  return spl_of(L) == 1 && reactor_smem_spl1(L) <= device_smem_optin();
+int reactor_layout_candidates(const ImageLayout& L, int* out) {
+  int k = 0;
+  if (spl_of(L) == 1 && reactor_smem_spl1(L) <= device_smem_optin()) out[k++] = REACTOR_LAYOUT_SHARED;
+  out[k++] = REACTOR_LAYOUT_GLOBAL;
+  out[k++] = REACTOR_LAYOUT_GLOBAL4;
+  return k;
 }
 
 cudaError_t launch_reactor(const uint8_t* img, const ImageLayout& L, int64_t n, double* T, const double* p,
@@ -606,14 +615,15 @@ cudaError_t launch_reactor(const uint8_t* img, const ImageLayout& L, int64_t n, 
   const void* fn = reactor_fn(L, layout);
   cudaError_t e = set_smem(fn, sm);
   if (e != cudaSuccess) return e;
+  const int threads = reactor_threads(layout), wpb = threads / 32;
   int per_sm = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, REACTOR_THREADS, sm);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, sm);
   if (per_sm < 1) return cudaErrorInvalidConfiguration;
   int64_t warps_needed = n;
-  int64_t blocks = (warps_needed + REACTOR_THREADS / 32 - 1) / (REACTOR_THREADS / 32);
+  int64_t blocks = (warps_needed + wpb - 1) / wpb;
   int64_t full = (int64_t)device_sms() * per_sm;
   if (blocks > full) blocks = full;
-  if (blocks * (REACTOR_THREADS / 32) > slots) blocks = slots / (REACTOR_THREADS / 32);
+  if (blocks * wpb > slots) blocks = slots / wpb;
   if (blocks < 1) return cudaErrorInvalidValue;
   // the BDF coefficient table lives in __constant__ memory, one copy per device
   static std::mutex bdf_mu;
@@ -637,13 +647,13 @@ cudaError_t launch_reactor(const uint8_t* img, const ImageLayout& L, int64_t n, 
   const int64_t sd = reactor_slot_doubles_of(L, layout);
   unsigned long long* wc = reinterpret_cast<unsigned long long*>(work_counter);
   if (spl_of(L) > 1)
-    k_reactor<2, true><<<(unsigned)blocks, REACTOR_THREADS, sm, st>>>(img, L, n, T, p, Y, dt, o, status, nsteps, wc,
+    k_reactor<2, true><<<(unsigned)blocks, threads, sm, st>>>(img, L, n, T, p, Y, dt, o, status, nsteps, wc,
                                                                        jsave, sd, n_dev);
   else if (reactor_gj(L, layout))
-    k_reactor<1, true><<<(unsigned)blocks, REACTOR_THREADS, sm, st>>>(img, L, n, T, p, Y, dt, o, status, nsteps, wc,
+    k_reactor<1, true><<<(unsigned)blocks, threads, sm, st>>>(img, L, n, T, p, Y, dt, o, status, nsteps, wc,
                                                                        jsave, sd, n_dev);
   else
-    k_reactor<1, false><<<(unsigned)blocks, REACTOR_THREADS, sm, st>>>(img, L, n, T, p, Y, dt, o, status, nsteps, wc,
+    k_reactor<1, false><<<(unsigned)blocks, threads, sm, st>>>(img, L, n, T, p, Y, dt, o, status, nsteps, wc,
                                                                         jsave, sd, n_dev);
   count_launch();
   return cudaGetLastError();

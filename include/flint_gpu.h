@@ -235,12 +235,13 @@ int flint_reactor_advance(flint_mech_t mech, int64_t n, double* T, const double*
                           int* status, int* nsteps, void* stream);
 
 /* Empirical choice of the reactor's layout for this mechanism: the Newton
- * matrix and Jacobian work area in shared memory (one block of 8 warps per SM)
- * or in each warp's global slot (shared memory left to the L1 cache).  Times
- * flint_reactor_advance under each on a sample of cells (n of them, device
- * arrays; the caller's arrays are not modified), keeps the faster for later
- * calls on this handle, and reports it in *layout (1 shared, 2 global; 0 when
- * the mechanism allows only one).  No reference counterpart. */
+ * matrix and Jacobian work area in shared memory (blocks of 8 warps), or in
+ * each warp's global slot with blocks of 8 or of 4 warps (shared memory left to
+ * the L1 cache that holds the slots).  Times flint_reactor_advance under each
+ * possible layout on a sample of cells (n of them, device arrays; the caller's
+ * arrays are not modified), keeps the fastest for later calls on this handle,
+ * and reports it in *layout (1 shared, 2 global / 8 warps, 3 global / 4 warps).
+ * No reference counterpart. */
 int flint_reactor_autotune(flint_mech_t mech, int64_t n, const double* T, const double* p, const double* Y,
                            const double* dt, const flint_reactor_opts* opts, int* layout, void* stream);
 

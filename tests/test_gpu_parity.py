@@ -353,7 +353,7 @@ def tsr_rich_states(mech, n, seed):
 @pytest.mark.parametrize("cfg", ["c2", "c5"])
 def test_reactor_autotune(cfg):
     """The autotuner times the shared-memory and global-slot layouts and keeps
-    the faster; both layouts compute the same numbers."""
+    the fastest; every layout computes the same numbers."""
     mech = mechgen.load(cfg)
     states = mechgen.c5_states if cfg == "c5" else mechgen.c3_states
     T, p, Y, dt = states(256, mech, seed=91)
@@ -364,7 +364,7 @@ def test_reactor_autotune(cfg):
     lay = chem.reactor_autotune(Tt, pt, Yt, dtt)
     torch.cuda.synchronize()
     assert np.array_equal(Tt.cpu().numpy(), T) and np.array_equal(Yt.cpu().numpy(), Y)   # inputs untouched
-    assert lay in ((1, 2) if cfg == "c2" else (0,))
+    assert lay in ((1, 2, 3) if cfg == "c2" else (2, 3))
     sb, nb = chem.reactor_advance(Tt, pt, Yt, dtt)
     torch.cuda.synchronize()
     np.testing.assert_array_equal(Tt.cpu().numpy(), Ta.cpu().numpy())
