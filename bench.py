@@ -38,6 +38,8 @@ sys.path.insert(0, REPO)
 
 import numpy as np  # noqa: E402
 
+from flint_gb300 import dist as fdist  # noqa: E402
+
 CELLS = 262144
 METRIC = "cell-steps/s on 1 GB300: surrogate+fallback vs plain FP64 at stated T/Y error"
 # FP64 pipe ops (DADD + DMUL + 2*DFMA, thread level) per event of the reactor
@@ -69,10 +71,8 @@ def fp64_ops(ev, ns, mech_name="synthetic-31sp-160r"):
 
 
 def dist_env():
-    ws = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return ws, rank, local
+    from flint_gb300.dist import env
+    return env()
 
 
 class ClockSampler:
@@ -151,24 +151,33 @@ def cpu_baseline(mech, T, p, Y, dt, target_s=12.0, want_state=False):
 
 
 def run_reference(args):
+    """The reference's CPU implementation of the path (the FP64 oracle port: FLINT's
+    Fortran cannot be compiled on these machines) on the default arm's workload:
+    the same seeded cells (the 1,048,576-cell C4 set, or the plain path's
+    262,144), all host threads, each step a bounded sample scaled per cell."""
     ws, rank, _ = dist_env()
     if rank != 0:
         return
     from flint_gb300 import mechgen
     mech = mechgen.load("c2")
-    T, p, Y, dt = mechgen.c3_states(args.cells, mech)
+    surrogate = args.path != "plain" and os.path.exists(args.checkpoint)
+    n = args.cells or (SUR_CELLS if surrogate else CELLS)
+    T, p, Y, dt = mechgen.c3_states(n, mech, seed=1004 if surrogate else 1003)
     vals = []
     for i in range(args.warmup + args.steps):
         r = cpu_baseline(mech, T, p, Y, dt, target_s=args.ref_seconds)
         if i >= args.warmup:
             vals.append(r["value"])
     v = statistics.mean(vals)
+    wl = (f"reactor-c4: surrogate+fallback, 31sp/160r, {n} cells, rtol 1e-8 atol 1e-14" if surrogate else
+          f"reactor-c3: 31sp/160r constant-p BDF/Newton, {n} cells, rtol 1e-8 atol 1e-14")
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "cell-steps/s", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * args.cells / v,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * n / v,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic (seeded)",
-            "config": {"workload": "reactor-c3: 31sp/160r BDF, 262144 cells, rtol 1e-8 atol 1e-14",
-                       "cells": args.cells, "note": "each step times a bounded sample and scales per cell"},
+            "data": "synthetic (seeded states, seeded synthetic mechanism)",
+            "config": {"workload": wl, "cells": n,
+                       "path": "FP64 BDF oracle (the reference path restated in C; no surrogate)",
+                       "note": "each step times a bounded sample of the same cells and scales per cell"},
             "cpu_baseline": {"value": v, "unit": "cell-steps/s", "cores": r["cores"], "kind": "port",
                              "sample": r["sample"]},
             "e2e": {"value": v, "unit": "cell-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -273,10 +282,7 @@ def run_ours(args):
     status = st.cpu().numpy()
     steps_per_cell = nst.cpu().numpy()
     t_step = statistics.mean(times)
-    if ws > 1:
-        tt = torch.tensor([t_step], device=dev, dtype=torch.float64)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        t_step = float(tt.item())
+    t_step = fdist.max_over_ranks(t_step, dev)
     value = n * ws / t_step
 
     # ---- end to end through the public API with pinned host buffers --------
@@ -303,10 +309,7 @@ def run_ours(args):
         if i >= args.warmup:
             e2e_times.append(time.perf_counter() - t0)
     e2e_t = statistics.mean(e2e_times)
-    if ws > 1:
-        tt = torch.tensor([e2e_t], device=dev, dtype=torch.float64)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        e2e_t = float(tt.item())
+    e2e_t = fdist.max_over_ranks(e2e_t, dev)
     assert np.array_equal(so.numpy(), status), "e2e run disagrees with the device-timed run"
 
     # ---- roofline: FP64 pipe ------------------------------------------------
@@ -443,10 +446,7 @@ def run_surrogate(args):
         launches = per_replay * args.steps   # the library kernels captured in one replay
     fb = reactor_stats(chem)
     t_sur = statistics.mean(times)
-    if ws > 1:
-        tt = torch.tensor([t_sur], device=dev, dtype=torch.float64)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        t_sur = float(tt.item())
+    t_sur = fdist.max_over_ranks(t_sur, dev)
     acc, rej = counts["c"]
     Ts, Ys, sts, nsts = Td.clone(), Yd.clone(), st.clone(), nst.clone()
     # ---- plain FP64 integrator on a sample of the same cells (timed) + errors
@@ -484,10 +484,7 @@ def run_surrogate(args):
         if i >= args.warmup:
             e2e.append(time.perf_counter() - t0)
     t_e2e = statistics.mean(e2e)
-    if ws > 1:
-        tt = torch.tensor([t_e2e], device=dev, dtype=torch.float64)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        t_e2e = float(tt.item())
+    t_e2e = fdist.max_over_ranks(t_e2e, dev)
     # ---- the dominant kernel alone: the fallback reactor on the rejected cells
     ridx = torch.nonzero((sts != 0) | (nsts != 0)).squeeze(1)
     Tf, Yf = Td0[ridx].contiguous(), Yd0[ridx].contiguous()
@@ -681,7 +678,6 @@ def main():
         run_kernel_workload(args)
         return
     if args.impl == "reference":
-        args.cells = args.cells or CELLS
         run_reference(args)
         return
     path = args.path
