@@ -413,6 +413,8 @@ def main():
     ap.add_argument("cmd", choices=["train", "calibrate"],
                     help="train: generate, train, calibrate, save; calibrate: re-derive the gate of a checkpoint")
     ap.add_argument("--checkpoint", help="calibrate: the checkpoint to re-calibrate")
+    ap.add_argument("--save-val", action="store_true",
+                    help="also write the per-cell validation metrics and errors (<out>_val.npz, tens of MB)")
     ap.add_argument("--out", required=True)
     ap.add_argument("--cells", type=int, default=524288)
     ap.add_argument("--val", type=int, default=65536)
@@ -442,7 +444,7 @@ def main():
                                                         "val_cells": int(v["T0"].shape[0]), "margin": args.margin}
         rep["gate"] = sur.gate
         rep["diagnostics"] = getattr(calibrate, "diag", {})
-        if getattr(calibrate, "data", None) is not None:
+        if args.save_val and getattr(calibrate, "data", None) is not None:
             np.savez_compressed(os.path.splitext(args.out)[0] + "_val.npz", **calibrate.data)
         sur.save(args.out, extra=rep, inference_only=bool(sur.header.get("inference_only")))
         print(json.dumps(rep["calibration"]))
@@ -476,7 +478,7 @@ def main():
            "gate": sur.gate, "diagnostics": getattr(calibrate, "diag", {}),
            "calibration": None if best is None else
            {"accept_frac": best[0], "max_dT": best[2], "max_dY": best[3]}}
-    if getattr(calibrate, "data", None) is not None:
+    if args.save_val and getattr(calibrate, "data", None) is not None:
         np.savez_compressed(os.path.splitext(args.out)[0] + "_val.npz", **calibrate.data)
     sur.save(args.out, extra=rep)
     sur.save(os.path.splitext(args.out)[0] + "_inference.bin", extra=rep, inference_only=True)
