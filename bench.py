@@ -633,7 +633,34 @@ def run_kernel_workload(args):
                       "ms_per_step": t * 1e3, "states": n, "steps": args.steps, "warmup": args.warmup,
                       "gpu_launches": kernel_launches() - l0,
                       "hbm_gbs_algorithmic": n * bytes_per_state / t / 1e9,
-                      "bytes_per_state": bytes_per_state, "roofline": roof}))
+                      "bytes_per_state": bytes_per_state, "roofline": roof,
+                      "cpu_baseline": None if args.no_cpu_baseline else
+                      cpu_baseline_kernels(chem.mech, T, p, Y, jac is not None, tab)}))
+
+
+def cpu_baseline_kernels(mech, T, p, Y, with_jac, tab=None, target_s=5.0):
+    """The oracle's source terms (and Jacobian) on all host cores over a bounded
+    sample of the same states; states/s."""
+    from oracle.oracle import Oracle, TableOracle
+    n = 1024
+    while True:
+        t0 = time.perf_counter()
+        if tab is not None:
+            W = np.array([sp.mw for sp in mech.species])
+            Tc = np.clip(T[:n], 300.0, 2990.0)
+            rho = p[:n] / (mech.r_eos * Tc * (Y[:n] / W).sum(1))
+            TableOracle(tab.t).general(rho[:, None] * Y[:n], Tc)
+        elif with_jac:
+            Oracle(mech).wdot_jac_batch(T[:n], p[:n], Y[:n])
+        else:
+            Oracle(mech).wdot_batch(T[:n], p[:n], Y[:n])
+        el = time.perf_counter() - t0
+        if el > 0.5 * target_s or n >= len(T):
+            break
+        n = min(len(T), int(n * min(8.0, max(1.5, target_s / max(el, 1e-3)))))
+    from oracle.oracle import Oracle as _O
+    return {"value": n / el, "unit": "states/s", "cores": _O.max_threads(), "kind": "port",
+            "sample": f"{n} of the {len(T)} states (first n), FP64 oracle, {el:.2f} s"}
 
 
 def chem_peak_fp64():

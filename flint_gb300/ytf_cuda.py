@@ -14,7 +14,7 @@ and launches it through a C entry point:
 
 The arithmetic is the analytic path's (NASA-7 thermo, Arrhenius, third body,
 Lindemann / Troe falloff, reverse rates from Kc = exp(-dG/RT)(p_ref/RT)^dnu,
-integer orders as products, other orders as pow on max(c, 0)), so the oracle
+integer orders as products, other orders as exp(o ln c) on c > 0), so the oracle
 that checks the data-driven kernels checks this one too.  Nothing is looked up
 at run time: no mechanism image, no shared memory, no loops over reactions.
 That suits mechanisms small enough for a thread to hold the cell (tens of
@@ -57,7 +57,8 @@ def _powexpr(c, order):
         if n == 0:
             return None
         return "*".join([c] * n)
-    return f"pow(fmax({c}, 0.0), {_d(o)})"
+    # c^o = exp(o ln c) for c > 0, 0 otherwise (pow on max(c, 0) of the analytic path)
+    return f"({c} > 0.0 ? exp({_d(o)} * log({c})) : 0.0)"
 
 
 def emit(m: mechmod.Mechanism, ident=None):
