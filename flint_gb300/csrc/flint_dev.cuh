@@ -504,6 +504,7 @@ __device__ void warp_kinetics(const MechView& m, const WarpScratch& s, int lane,
   const double Q = warp_sum(Ql);
   const double D = warp_sum(Dl);
   const double fT = -T * Q / D;
+  const double irho = 1.0 / rho;   // one division for the warp instead of one per lane
   out.rho = rho;
   out.fT = fT;
 #pragma unroll
@@ -511,7 +512,7 @@ __device__ void warp_kinetics(const MechView& m, const WarpScratch& s, int lane,
     const int k = lane + 32 * j;
     out.wmol[j] = wm[j];
     out.cpR[j] = my_cpR[j];
-    out.f[j] = (k < ns) ? m.mw[k] * wm[j] / rho : (k == ns ? fT : 0.0);
+    out.f[j] = (k < ns) ? m.mw[k] * wm[j] * irho : (k == ns ? fT : 0.0);
   }
   // mixture cp and h (mass)
   out.cp_mass = warp_sum(cpl) * m.r_thermo;

@@ -92,7 +92,9 @@ __device__ inline double wmax(const double (&v)[SPL], const double (&w)[SPL], in
 
 // LU of the rows (row r = lane + 32 j) held at A[r*ld ...], partial pivoting by
 // the largest |a| (lowest row on ties); the pivot order goes to piv[step] and
-// each row remembers its step in mystep (rows are not swapped).
+// each row remembers its step in mystep (rows are not swapped).  U's diagonal
+// is stored as its reciprocal, so a solve has no division (an FP64 division is
+// a dozen FP64-pipe instructions; a solve would otherwise carry one per column).
 template <int SPL>
 __device__ inline void warp_lu(double* A, int ld, int nv, int lane, int* piv, int (&mystep)[SPL]) {
 #pragma unroll
@@ -118,8 +120,11 @@ __device__ inline void warp_lu(double* A, int ld, int nv, int lane, int* piv, in
     for (int j = 0; j < SPL; ++j)
       if (lane + 32 * j == who) mystep[j] = k;
     if (lane == 0) piv[k] = who;
-    const double* prow = A + who * ld;
+    double* prow = A + who * ld;
     const double inv = 1.0 / prow[k];
+    __syncwarp();
+    // the pivot's reciprocal replaces U's diagonal entry: the solves multiply
+    if (lane == (who & 31)) prow[k] = inv;
 #pragma unroll
     for (int j = 0; j < SPL; ++j) {
       const int r = lane + 32 * j;
@@ -156,7 +161,7 @@ __device__ inline void warp_lu_solve(const double* A, int ld, int nv, int lane, 
   for (int c = nv - 1; c >= 0; --c) {
     const int pc = piv[c];
     const double src = (SPL == 1 || (pc >> 5) == 0) ? b[0] : b[SPL - 1];
-    const double xc = __shfl_sync(FULL, src, pc & 31) / A[pc * ld + c];
+    const double xc = __shfl_sync(FULL, src, pc & 31) * A[pc * ld + c];
 #pragma unroll
     for (int j = 0; j < SPL; ++j) {
       const int r = lane + 32 * j;
@@ -409,12 +414,13 @@ k_reactor(const uint8_t* __restrict__ img, ImageLayout L, int64_t n, double* __r
           int conv = 0;
           double delp = 0.0;
           const double Eq = 1.0 / ((double)(q + 1) * l1 + 1.0);
+          const double il1 = 1.0 / l1;
           for (int mi = 0; mi < 3; ++mi) {
             ++n_newt;
             rhs(yv, f);
             double bv[SPL];
 #pragma unroll
-            for (int j = 0; j < SPL; ++j) bv[j] = (lane + 32 * j < nv) ? gamma * f[j] - z[1][j] / l1 - e[j] : 0.0;
+            for (int j = 0; j < SPL; ++j) bv[j] = (lane + 32 * j < nv) ? gamma * f[j] - z[1][j] * il1 - e[j] : 0.0;
             warp_lu_solve<SPL>(s.Jr, ld, nv, lane, pivs, mystep, bv);
             if (gamrat != 1.0) {
               const double sc = 2.0 / (1.0 + gamrat);
@@ -425,7 +431,7 @@ k_reactor(const uint8_t* __restrict__ img, ImageLayout L, int64_t n, double* __r
 #pragma unroll
             for (int j = 0; j < SPL; ++j) { e[j] += bv[j]; yv[j] = ypred[j] + e[j]; }
             if (mi > 0) { const double r = del / delp; crate = (0.3 * crate > r) ? 0.3 * crate : r; }
-            const double dcon = del * (crate < 1.0 ? crate : 1.0) * Eq / 0.1;
+            const double dcon = del * (crate < 1.0 ? crate : 1.0) * Eq * 10.0;   // test constant 0.1
             if (dcon <= 1.0) { conv = 1; break; }
             if (mi > 0 && !(del <= 2.0 * delp)) break;
             delp = del;

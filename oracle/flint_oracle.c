@@ -485,6 +485,7 @@ static int lu_factor(int n, double* a, int* piv) {
     if (amax == 0.0) return 1;
     if (p != k) for (int j = 0; j < n; ++j) { double t = a[j * n + k]; a[j * n + k] = a[j * n + p]; a[j * n + p] = t; }
     double inv = 1.0 / a[k * n + k];
+    a[k * n + k] = inv;   /* U's diagonal kept as its reciprocal: solves multiply */
     for (int i = k + 1; i < n; ++i) a[k * n + i] *= inv;
     for (int j = k + 1; j < n; ++j) {
       double akj = a[j * n + k];
@@ -498,7 +499,7 @@ static void lu_solve(int n, const double* a, const int* piv, double* b) {
   for (int k = 0; k < n; ++k) { int p = piv[k]; if (p != k) { double t = b[k]; b[k] = b[p]; b[p] = t; } }
   for (int k = 0; k < n; ++k) for (int i = k + 1; i < n; ++i) b[i] -= a[k * n + i] * b[k];
   for (int k = n - 1; k >= 0; --k) {
-    b[k] /= a[k * n + k];
+    b[k] *= a[k * n + k];
     for (int i = 0; i < k; ++i) b[i] -= a[k * n + i] * b[k];
   }
 }
@@ -597,15 +598,16 @@ static int bdf_cell(const rhs_ctx* cx, int n, double* y, double tout, const flin
       int conv = 0;
       double delp = 0.0;
       double Eq = 1.0 / ((double)(q + 1) * l1 + 1.0);
+      double il1 = 1.0 / l1;
       for (int mi = 0; mi < 3; ++mi) {
         rhs_y(cx, y, f);
-        for (int i = 0; i < n; ++i) b[i] = gamma * f[i] - z[1][i] / l1 - e[i];
+        for (int i = 0; i < n; ++i) b[i] = gamma * f[i] - z[1][i] * il1 - e[i];
         lu_solve(n, Mlu, piv, b);
         if (gamrat != 1.0) { double s = 2.0 / (1.0 + gamrat); for (int i = 0; i < n; ++i) b[i] *= s; }
         double del = wmax(n, b, ewt);
         for (int i = 0; i < n; ++i) { e[i] += b[i]; y[i] = ypred[i] + e[i]; }
         if (mi > 0) { double r = del / delp; crate = (0.3 * crate > r) ? 0.3 * crate : r; }
-        double dcon = del * (crate < 1.0 ? crate : 1.0) * Eq / 0.1;
+        double dcon = del * (crate < 1.0 ? crate : 1.0) * Eq * 10.0;   /* test constant 0.1 */
         if (dcon <= 1.0) { conv = 1; break; }
         if (mi > 0 && !(del <= 2.0 * delp)) break;
         delp = del;
