@@ -158,7 +158,14 @@ static int pack(const flint_mech_desc* d, ImageLayout& L, std::vector<uint8_t>& 
       D(L.o_b0)[rr] = d->arrh0[3 * r + 1] - d->arrh[3 * r + 1];
       D(L.o_E0)[rr] = d->arrh0[3 * r + 2] - d->arrh[3 * r + 2];
     }
-    if (t == 3) for (int j = 0; j < 4; ++j) D(L.o_tr)[j * P + rr] = d->troe[4 * r + j];
+    if (t == 3) {
+      // Troe a, 1/T3, 1/T1, T2: the kernels multiply by the reciprocals
+      const double* tr = d->troe + 4 * r;
+      D(L.o_tr)[rr] = tr[0];
+      D(L.o_tr)[P + rr] = 1.0 / tr[1];
+      D(L.o_tr)[2 * P + rr] = 1.0 / tr[2];
+      D(L.o_tr)[3 * P + rr] = tr[3];
+    }
     uint32_t w = (uint32_t)t | ((d->reversible[r] ? 1u : 0u) << 2);
     double dn = 0.0;
     for (int s = 0; s < 3; ++s) {

@@ -42,7 +42,7 @@ struct ImageLayout {
   // species
   int o_mw, o_invmw, o_nasa;     // nasa: [16][nsp] : low a0..a6, high a0..a6, tmid, unused
   // reactions (nrpad each)
-  int o_A, o_b, o_E, o_A0, o_b0, o_E0, o_tr;   // tr: [4][nrpad]
+  int o_A, o_b, o_E, o_A0, o_b0, o_E0, o_tr;   // tr: [4][nrpad] = a, 1/T3, 1/T1, T2
   // falloff: the image stores the low-pressure limit relative to the high-
   // pressure one, k0/kinf = A0r T^b0r exp(-E0r/T) with A0r = A0/A, b0r = b0-b,
   // E0r = (Ea0-Ea)/R, so Pr = (k0/kinf) M costs one exp and no division.
@@ -245,10 +245,10 @@ __device__ inline Falloff falloff_eval(const MechView& m, int r, int type, doubl
   double F = 1.0, G = 0.0, dlnF_T = 0.0;
   if (type == 3) {
     const int P = m.nrpad;
-    double a = m.tr[r], T3 = m.tr[P + r], T1 = m.tr[2 * P + r], T2 = m.tr[3 * P + r];
-    double e3 = fexp(-T / T3, tab), e1 = fexp(-T / T1, tab);
+    double a = m.tr[r], iT3 = m.tr[P + r], iT1 = m.tr[2 * P + r], T2 = m.tr[3 * P + r];   // 1/T3, 1/T1
+    double e3 = fexp(-T * iT3, tab), e1 = fexp(-T * iT1, tab);
     double Fc = (1.0 - a) * e3 + a * e1;
-    double dFc = -(1.0 - a) / T3 * e3 - a / T1 * e1;
+    double dFc = -(1.0 - a) * iT3 * e3 - a * iT1 * e1;
     if (T2 != 0.0) {
       double e2 = fexp(-T2 * invT, tab);
       Fc += e2;
@@ -329,8 +329,8 @@ __device__ void warp_kinetics(const MechView& m, const WarpScratch& s, int lane,
       switch (kind) {
         case 0: arg = m.b[r] * lnT - m.E[r] * invT; pre = m.A[r]; break;
         case 1: arg = m.b0[r] * lnT - m.E0[r] * invT; pre = m.A0[r]; break;   // k0 / kinf
-        case 2: arg = troe ? -T / m.tr[P + r] : 0.0; break;
-        case 3: arg = troe ? -T / m.tr[2 * P + r] : 0.0; break;
+        case 2: arg = troe ? -T * m.tr[P + r] : 0.0; break;       // tr rows 1, 2 hold 1/T3, 1/T1
+        case 3: arg = troe ? -T * m.tr[2 * P + r] : 0.0; break;
         default: {
           const double T2 = m.tr[3 * P + r];
           arg = (troe && T2 != 0.0) ? -T2 * invT : 0.0;
@@ -361,8 +361,8 @@ __device__ void warp_kinetics(const MechView& m, const WarpScratch& s, int lane,
         const double e3 = fo[2 * WARP + lane], e1 = fo[3 * WARP + lane], e2 = fo[4 * WARP + lane];
         Fc = (1.0 - a) * e3 + a * e1 + e2;
         if (JAC) {
-          const double T3 = m.tr[P + r], T1 = m.tr[2 * P + r], T2 = m.tr[3 * P + r];
-          dFc = -(1.0 - a) / T3 * e3 - a / T1 * e1 + (T2 != 0.0 ? T2 * invT * invT * e2 : 0.0);
+          const double iT3 = m.tr[P + r], iT1 = m.tr[2 * P + r], T2 = m.tr[3 * P + r];
+          dFc = -(1.0 - a) * iT3 * e3 - a * iT1 * e1 + (T2 != 0.0 ? T2 * invT * invT * e2 : 0.0);
         }
       }
     }
@@ -371,28 +371,37 @@ __device__ void warp_kinetics(const MechView& m, const WarpScratch& s, int lane,
     lg_in = lg_in > 1e-300 ? lg_in : 1e-300;
     const double lg = log10(lg_in);
     const double logPr = __shfl_sync(FULL, lg, lane < NF ? lane + NF : 0);
+    // two divisions per lane for the blend: 1/(den (1 + Pr)) yields both
+    // 1/den and 1/(1 + Pr); 1/opf the other
     double Fb = 1.0, G = 0.0, dlnF_T = 0.0, fexp_arg = 0.0;
-    double opf = 1.0, x = 0.0, nn = 0.0, logFc = 0.0, den = 1.0, f1 = 0.0;
+    double opf = 1.0, iopf = 1.0, x = 0.0, nn = 0.0, logFc = 0.0, den = 1.0, iden = 1.0, f1 = 0.0;
+    double iopr = 1.0;
     if (lane < NF && troe) {
       logFc = lg;
       const double cc = -0.4 - 0.67 * logFc;
       nn = 0.75 - 1.27 * logFc;
       x = logPr + cc;
       den = nn - 0.14 * x;
-      f1 = x / den;
+      const double opr = 1.0 + Pr;
+      const double rr = 1.0 / (den * opr);
+      iden = rr * opr;
+      iopr = rr * den;
+      f1 = x * iden;
       opf = 1.0 + f1 * f1;
-      fexp_arg = 2.302585092994045684 * (logFc / opf);
+      iopf = 1.0 / opf;
+      fexp_arg = 2.302585092994045684 * (logFc * iopf);
+    } else if (lane < NF) {
+      iopr = 1.0 / (1.0 + Pr);
     }
     Fb = fexp(fexp_arg, tab);
     if (lane < NF) {
       if (!troe) Fb = 1.0;
-      const double iopr = 1.0 / (1.0 + Pr);
       fo[5 * WARP + lane] = kinf * (Pr * iopr) * Fb;
       if (JAC) {
         if (troe) {
-          const double Aq = 2.0 * logFc * f1 / (opf * opf * den * den);
+          const double Aq = 2.0 * logFc * f1 * (iopf * iopf) * (iden * iden);
           G = -Aq * nn;
-          dlnF_T = (1.0 / opf + Aq * (0.67 * nn - 1.27 * x)) * dFc / Fc;
+          dlnF_T = (iopf + Aq * (0.67 * nn - 1.27 * x)) * dFc / Fc;
         }
         fo[6 * WARP + lane] = dlnkinf + dlnPr * iopr + G * dlnPr + dlnF_T;
         fo[7 * WARP + lane] = kinf * Fb * iopr * (iopr + G) * kratio;

@@ -135,7 +135,7 @@ def emit(m: mechmod.Mechanism, ident=None):
             if r.rtype == TYPE_TROE:
                 a, T3, T1 = r.troe[0], r.troe[1], r.troe[2]
                 T2 = r.troe[3] if len(r.troe) > 3 else 0.0
-                fc = f"(1.0 - {_d(a)}) * exp(-t / {_d(T3)}) + {_d(a)} * exp(-t / {_d(T1)})"
+                fc = f"(1.0 - {_d(a)}) * exp(-t * {_d(1.0 / T3)}) + {_d(a)} * exp(-t * {_d(1.0 / T1)})"
                 if T2 != 0.0:
                     fc += f" + exp(-{_d(T2)} * invT)"
                 w(f"      const double logFc = log10({fc});")
