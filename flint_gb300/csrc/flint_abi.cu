@@ -103,7 +103,7 @@ static int pack(const flint_mech_desc* d, ImageLayout& L, std::vector<uint8_t>& 
   if (nfall > 16) return fail(FLINT_ERR_MECH, "%d falloff reactions: this build supports up to 16", nfall);
   L = ImageLayout{};
   L.ns = ns; L.nr = nr; L.nsp = rup(ns, 32); L.nrpad = rup(std::max(nr, 1), 32); L.ntb = std::max(ntb, 1);
-  L.r_eos = d->r_eos; L.r_thermo = d->r_thermo;
+  L.r_eos = d->r_eos; L.r_thermo = d->r_thermo; L.inv_r_eos = 1.0 / d->r_eos;
   L.lnpref_rth = std::log(d->p_ref / d->r_thermo);
   // CSR species -> (reaction, net nu)
   std::vector<std::vector<std::pair<int, double>>> lists(ns);

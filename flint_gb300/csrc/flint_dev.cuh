@@ -39,6 +39,7 @@ struct ImageLayout {
   int nlist;                     // CSR entries (species -> reactions)
   int bytes;                     // total image size
   double r_eos, r_thermo, lnpref_rth;   // ln(p_ref / r_thermo)
+  double inv_r_eos;                     // 1 / r_eos
   // species
   int o_mw, o_invmw, o_nasa;     // nasa: [16][nsp] : low a0..a6, high a0..a6, tmid, unused
   // reactions (nrpad each)
@@ -61,7 +62,7 @@ struct ImageLayout {
 
 struct MechView {
   int ns, nr, nrpad, nsp, ntb;
-  double r_eos, r_thermo, lnpref_rth;
+  double r_eos, r_thermo, lnpref_rth, inv_r_eos;
   const double *mw, *invmw, *nasa;
   const double *A, *b, *E, *A0, *b0, *E0, *tr;
   const double *rnu, *rord, *pnu, *dnu;
@@ -74,7 +75,7 @@ struct MechView {
   __host__ __device__ void bind(const ImageLayout& L, const uint8_t* base) {
     ns = L.ns; nr = L.nr; nrpad = L.nrpad; nsp = L.nsp; ntb = L.ntb; nfall = L.nfall;
     exptab = (const double*)(base + L.o_exptab);
-    r_eos = L.r_eos; r_thermo = L.r_thermo; lnpref_rth = L.lnpref_rth;
+    r_eos = L.r_eos; r_thermo = L.r_thermo; lnpref_rth = L.lnpref_rth; inv_r_eos = L.inv_r_eos;
     mw = (const double*)(base + L.o_mw); invmw = (const double*)(base + L.o_invmw);
     nasa = (const double*)(base + L.o_nasa);
     A = (const double*)(base + L.o_A); b = (const double*)(base + L.o_b); E = (const double*)(base + L.o_E);
@@ -293,8 +294,8 @@ __device__ void warp_kinetics(const MechView& m, const WarpScratch& s, int lane,
     if (k < ns) yw += Yk[j] * m.invmw[k];
   }
   double sumYW = warp_sum(yw);
-  double rho = p / (m.r_eos * T * sumYW);
   double wbar = 1.0 / sumYW;
+  double rho = p * m.inv_r_eos * invT * wbar;   // p / (R T sum Y/W) without another division
   // species-parallel: concentrations and thermo, species k = lane + 32 j
   double my_cpR[SPL], my_hRT[SPL], my_dcpR[SPL], my_c[SPL];
 #pragma unroll
