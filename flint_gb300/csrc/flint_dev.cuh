@@ -284,7 +284,7 @@ template <bool JAC, int SPL>
 __device__ void warp_kinetics(const MechView& m, const WarpScratch& s, int lane, const double (&Yk)[SPL],
                               double T, double p, CellOutT<SPL>& out) {
   const int ns = m.ns, nsp = m.nsp, nrpad = m.nrpad;
-  const double lnT = log(T), invT = 1.0 / T;
+  const double lnT = log(T);
   const double lnC0 = m.lnpref_rth - lnT;        // ln(p_ref / (R T))
   // mixture molar mass and density
   double yw = 0.0;
@@ -294,8 +294,13 @@ __device__ void warp_kinetics(const MechView& m, const WarpScratch& s, int lane,
     if (k < ns) yw += Yk[j] * m.invmw[k];
   }
   double sumYW = warp_sum(yw);
-  double wbar = 1.0 / sumYW;
-  double rho = p * m.inv_r_eos * invT * wbar;   // p / (R T sum Y/W) without another division
+  // 1/T, 1/sumYW and 1/p from one division (an FP64 division costs a dozen
+  // pipe instructions; the warp would otherwise pay for three)
+  const double rr = 1.0 / (T * sumYW * p);
+  const double invT = rr * sumYW * p;
+  double wbar = rr * T * p;
+  const double invp = rr * T * sumYW;
+  double rho = p * m.inv_r_eos * invT * wbar;   // p / (R T sum Y/W)
   // species-parallel: concentrations and thermo, species k = lane + 32 j
   double my_cpR[SPL], my_hRT[SPL], my_dcpR[SPL], my_c[SPL];
 #pragma unroll
@@ -513,8 +518,9 @@ __device__ void warp_kinetics(const MechView& m, const WarpScratch& s, int lane,
   }
   const double Q = warp_sum(Ql);
   const double D = warp_sum(Dl);
-  const double fT = -T * Q / D;
-  const double irho = 1.0 / rho;   // one division for the warp instead of one per lane
+  const double invD = 1.0 / D;
+  const double fT = -T * Q * invD;
+  const double irho = m.r_eos * T * sumYW * invp;   // 1 / rho
   out.rho = rho;
   out.fT = fT;
 #pragma unroll
@@ -578,9 +584,10 @@ __device__ void warp_kinetics(const MechView& m, const WarpScratch& s, int lane,
   }
   const double HS = warp_sum(HSl);
   __syncwarp();
-  const double wr = wbar / rho;
+  const double wr = wbar * irho;
   const double dQT = warp_sum(dQTl), dDT = warp_sum(dDTl);
-  const double JTT = -Q / D - (T / D) * (dQT - (Q / D) * dDT);
+  const double QD = Q * invD, TD = T * invD;
+  const double JTT = -QD - TD * (dQT - QD * dDT);
   double JTm[SPL];
 #pragma unroll
   for (int j = 0; j < SPL; ++j) {
@@ -590,13 +597,13 @@ __device__ void warp_kinetics(const MechView& m, const WarpScratch& s, int lane,
       const double rw = rho * m.invmw[k], ww = wbar * m.invmw[k];
       const double dQ = rw * HJ[j] - ww * HS;
       const double dD = rw * my_cpR[j] - ww * D;
-      JTm[j] = -(T / D) * (dQ - (Q / D) * dD);
+      JTm[j] = -TD * (dQ - QD * dD);
       // species row k in (Y, T) variables
       const double tk = Sk[j] - wm[j];
       const double Wk = m.mw[k];
       double* Jrow = s.Jr + k * ld;
       for (int jj = 0; jj < ns; ++jj) Jrow[jj] = Wk * m.invmw[jj] * (Jrow[jj] - wr * tk);
-      Jrow[ns] = (Wk / rho) * (JT[j] - tk * invT);
+      Jrow[ns] = (Wk * irho) * (JT[j] - tk * invT);
     }
   }
   __syncwarp();
