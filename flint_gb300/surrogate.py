@@ -390,10 +390,13 @@ def calibrate(sur, d, target_dT=1.0, target_dY=1e-4, margin=0.5):
             "minY_q": [float(x) for x in np.quantile(M[:, 2], [0.0, 0.01, 0.5])],
             "base_frac": float(base.mean()), "good_frac": float(good.mean())}
     calibrate.diag = diag
-    calibrate.data = {"M": M, "eT": eT, "eY": eY,
-                      "eYk": (Y - d["Y1"]).abs().cpu().numpy().astype(np.float32),
-                      "T0": d["T0"].cpu().numpy(), "p": d["p"].cpu().numpy(), "dt": d["dt"].cpu().numpy(),
-                      "Y0": d["Y0"].cpu().numpy().astype(np.float32)}
+    calibrate.data = {"M": M.astype(np.float32), "eT": eT.astype(np.float32), "eY": eY.astype(np.float32),
+                      "T0": d["T0"].cpu().numpy().astype(np.float32), "p": d["p"].cpu().numpy().astype(np.float32),
+                      "dt": d["dt"].cpu().numpy().astype(np.float32),
+                      "pred_dT": (T - d["T0"]).cpu().numpy().astype(np.float32),
+                      "pred_dY": (Y - d["Y0"]).abs().amax(dim=1).cpu().numpy().astype(np.float32),
+                      "true_dT": (d["T1"] - d["T0"]).cpu().numpy().astype(np.float32),
+                      "worst_species": (Y - d["Y1"]).abs().argmax(dim=1).cpu().numpy().astype(np.int16)}
     best = None
     for a in qs:
         acc_a = base & (M[:, 0] <= a)
