@@ -359,28 +359,73 @@ def errors_vs_integrator(Tsur, Ysur, Tref, Yref):
     return dT, dY
 
 
+def search_gate(M, eT, eY, T0, log10dt, gate, n_nets, target_dT=1.0, target_dY=1e-4, margin=0.5):
+    """Largest accepted set of validation cells whose every member is within
+    margin * (target_dT, target_dY) of the integrator, over gate thresholds on
+    the energy residual, the ensemble spreads of dT and dY, and the upper ends
+    of the input domain in dt and T0 (the long steps and hot starts where the
+    network's errors concentrate).
+
+    For each domain cut and residual threshold the two spread thresholds are
+    found exactly: sweeping the dT-spread threshold b over the cells' own
+    values, the dY-spread threshold must stay below the smallest dY spread of
+    the out-of-tolerance cells with dT spread <= b.  Returns (accepted
+    fraction, gate update, max dT, max dY) or None."""
+    good = (eT <= margin * target_dT) & (eY <= margin * target_dY)
+    bad = ~good
+    base = (M[:, 5] > 0) & (M[:, 1] <= gate["max_elem_resid"]) & (M[:, 2] >= gate["min_Y"])
+    if not base.any():
+        return None
+    n = len(eT)
+    ens = n_nets > 1
+    x = M[:, 3] if ens else np.zeros(n)
+    y = M[:, 4] if ens else np.zeros(n)
+    dt_cuts = np.unique(np.concatenate([[log10dt.max()], np.quantile(log10dt, [0.95, 0.9, 0.85, 0.8, 0.75, 0.7])]))
+    T_cuts = np.unique(np.concatenate([[T0.max()], np.quantile(T0, [0.95, 0.9, 0.85])]))
+    rgrid = np.unique(np.concatenate([np.linspace(0.05, 0.9, 10), np.linspace(0.9, 1.0, 21)]))
+    bgrid = np.unique(np.concatenate([np.linspace(0.05, 0.9, 12), np.linspace(0.9, 1.0, 29)]))
+    best = None
+    for dth in dt_cuts:
+        for Th in T_cuts:
+            dom = base & (log10dt <= dth) & (T0 <= Th)
+            if not dom.any():
+                continue
+            for a in np.quantile(M[dom, 0], rgrid):
+                S = dom & (M[:, 0] <= a)
+                if not S.any():
+                    continue
+                cands = np.quantile(x[S], bgrid) if ens else [0.0]
+                for bthr in cands:
+                    sel = S & (x <= bthr)
+                    yb = y[sel & bad]
+                    cmax = yb.min() if yb.size else np.inf
+                    ok = sel & (y < cmax)
+                    cnt = int(ok.sum())
+                    if cnt == 0 or (best is not None and cnt <= best[0]):
+                        continue
+                    c = float(y[ok].max())
+                    best = (cnt, {"max_dT_resid": float(a), "max_ens_dT": float(bthr) if ens else 1e30,
+                                  "max_ens_dY": c if ens else 1e30, "log10dt_hi": float(dth), "T_hi": float(Th)},
+                            float(eT[ok].max()), float(eY[ok].max()))
+    if best is None:
+        return None
+    return (best[0] / n, best[1], best[2], best[3])
+
+
 def calibrate(sur, d, target_dT=1.0, target_dY=1e-4, margin=0.5):
     """Gate thresholds from held-out samples judged by the integrator.
 
-    The surrogate is applied to every validation cell (``evaluate``); a grid
-    over the energy-residual and ensemble-spread thresholds (their quantiles)
-    is searched for the largest accepted fraction such that every accepted
-    validation cell is within margin * (target_dT, target_dY) of the FP64
-    integrator.  Returns (accept_fraction, gate dict, max dT, max dY)."""
+    The surrogate is applied to every validation cell (``evaluate``) and
+    ``search_gate`` picks the thresholds with the largest accepted fraction such
+    that every accepted validation cell is within margin * (target_dT,
+    target_dY) of the FP64 integrator.  Returns (accept_fraction, gate dict,
+    max dT, max dY)."""
     T = d["T0"].clone(); Y = d["Y0"].clone()
     M = sur.evaluate(T, d["p"], Y, d["dt"]).cpu().numpy()
     eT = (T - d["T1"]).abs().cpu().numpy()
     eY = (Y - d["Y1"]).abs().amax(dim=1).cpu().numpy()
     base = (M[:, 5] > 0) & (M[:, 1] <= sur.gate["max_elem_resid"]) & (M[:, 2] >= sur.gate["min_Y"])
     good = (eT <= margin * target_dT) & (eY <= margin * target_dY)
-    # quantile grid, denser towards the top where the accepted fraction is decided
-    grid = np.unique(np.concatenate([np.linspace(0.05, 0.9, 18), np.linspace(0.9, 1.0, 26)]))
-    qs = np.concatenate([[0.0], np.quantile(M[base, 0], grid)]) if base.any() else [0.0]
-    cand_e = [(1e30, 1e30)]
-    if sur.n_nets > 1 and base.any():
-        q3 = np.quantile(M[base, 3], grid)
-        q4 = np.quantile(M[base, 4], grid)
-        cand_e = [(a, b) for a in q3 for b in q4]
     diag = {"eT_q": [float(x) for x in np.quantile(eT, [0.5, 0.9, 0.99, 0.999, 1.0])],
             "eY_q": [float(x) for x in np.quantile(eY, [0.5, 0.9, 0.99, 0.999, 1.0])],
             "resid_q": [float(x) for x in np.quantile(M[:, 0], [0.5, 0.9, 0.99, 1.0])],
@@ -397,18 +442,8 @@ def calibrate(sur, d, target_dT=1.0, target_dY=1e-4, margin=0.5):
                       "pred_dY": (Y - d["Y0"]).abs().amax(dim=1).cpu().numpy().astype(np.float32),
                       "true_dT": (d["T1"] - d["T0"]).cpu().numpy().astype(np.float32),
                       "worst_species": (Y - d["Y1"]).abs().argmax(dim=1).cpu().numpy().astype(np.int16)}
-    best = None
-    for a in qs:
-        acc_a = base & (M[:, 0] <= a)
-        for (b, c) in cand_e:
-            acc = acc_a & (M[:, 3] <= b) & (M[:, 4] <= c)
-            if not acc.any() or not good[acc].all():
-                continue
-            frac = acc.mean()
-            if best is None or frac > best[0]:
-                best = (float(frac), {"max_dT_resid": float(a), "max_ens_dT": float(b), "max_ens_dY": float(c)},
-                        float(eT[acc].max()), float(eY[acc].max()))
-    return best
+    return search_gate(M, eT, eY, d["T0"].cpu().numpy(), np.log10(d["dt"].cpu().numpy()), sur.gate, sur.n_nets,
+                       target_dT, target_dY, margin)
 
 
 def main():
