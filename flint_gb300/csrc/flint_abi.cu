@@ -132,6 +132,7 @@ static int pack(const flint_mech_desc* d, ImageLayout& L, std::vector<uint8_t>& 
   L.o_eff = sec(8 * L.ntb * S);
   L.o_cstart = sec(4 * (S + 1)); L.o_lr = sec(4 * std::max(nlist, 1)); L.o_lnu = sec(8 * std::max(nlist, 1));
   L.o_exptab = sec(8 * 64);
+  L.o_nasa9 = d->nasa9 ? sec(8 * 32 * S) : -1;
   L.nfall = nfall;
   L.bytes = off;
   img.assign(off, 0);
@@ -146,6 +147,8 @@ static int pack(const flint_mech_desc* d, ImageLayout& L, std::vector<uint8_t>& 
       D(L.o_nasa)[(7 + j) * S + k] = c[10 + j];
     }
     D(L.o_nasa)[14 * S + k] = c[1];
+    if (d->nasa9)
+      for (int j = 0; j < 32; ++j) D(L.o_nasa9)[j * S + k] = d->nasa9[32 * k + j];
   }
   for (int i = 0; i < 3 * P; ++i) { I(L.o_rsp)[i] = -1; I(L.o_psp)[i] = -1; }
   int tb = 0;

@@ -58,6 +58,7 @@ struct ImageLayout {
   int o_lnu;                     // double [nlist]
   int o_exptab;                  // double [64]: 2^(j/64)
   int nfall;                     // falloff reactions (the last nfall after sorting; <= 16)
+  int o_nasa9;                   // NASA-9 thermo [32][nsp] (nranges, T0..T3, 3 x 9 coefficients); -1 = none
 };
 
 struct MechView {
@@ -70,6 +71,7 @@ struct MechView {
   const uint32_t* code;
   const uint32_t* pcode;
   const double *eff, *lnu, *exptab;
+  const double* nasa9;   // null: NASA-7 (nasa)
   int nfall;
 
   __host__ __device__ void bind(const ImageLayout& L, const uint8_t* base) {
@@ -89,6 +91,7 @@ struct MechView {
     eff = (const double*)(base + L.o_eff);
     cstart = (const int*)(base + L.o_cstart); lr = (const int*)(base + L.o_lr);
     lnu = (const double*)(base + L.o_lnu);
+    nasa9 = L.o_nasa9 >= 0 ? (const double*)(base + L.o_nasa9) : nullptr;
   }
 };
 
@@ -139,7 +142,31 @@ __device__ inline double warp_max(double v) {
 // NASA-7 thermo of species k at T (lane-local).
 struct SpThermo { double cpR, hRT, sR, dcpR; };
 
+// NASA-9 thermo of species k at T: range r holds (a1..a7, b1, b2);
+// cp/R = a1/T^2 + a2/T + a3 + a4 T + ... + a7 T^4 and its h, s integrals.
+static __device__ __noinline__ SpThermo nasa9(const MechView& m, int k, double T, double lnT, double invT) {
+  const int S = m.nsp;
+  const double* c = m.nasa9 + k;
+  const int nr = (int)c[0];
+  int r = 0;
+  if (nr > 1 && T > c[2 * S]) r = 1;
+  if (nr > 2 && T > c[3 * S]) r = 2;
+  const double* a = c + (5 + 9 * r) * S;
+  const double a1 = a[0], a2 = a[S], a3 = a[2 * S], a4 = a[3 * S], a5 = a[4 * S], a6 = a[5 * S], a7 = a[6 * S];
+  const double b1 = a[7 * S], b2 = a[8 * S];
+  const double iT2 = invT * invT;
+  SpThermo t;
+  t.cpR = a1 * iT2 + a2 * invT + a3 + T * (a4 + T * (a5 + T * (a6 + T * a7)));
+  t.hRT = -a1 * iT2 + a2 * lnT * invT + a3 + T * (a4 * 0.5 + T * (a5 * (1.0 / 3.0) + T * (a6 * 0.25 + T * a7 * 0.2))) +
+          b1 * invT;
+  t.sR = -0.5 * a1 * iT2 - a2 * invT + a3 * lnT + T * (a4 + T * (a5 * 0.5 + T * (a6 * (1.0 / 3.0) + T * a7 * 0.25))) +
+         b2;
+  t.dcpR = -2.0 * a1 * iT2 * invT - a2 * iT2 + a4 + T * (2.0 * a5 + T * (3.0 * a6 + T * 4.0 * a7));
+  return t;
+}
+
 __device__ inline SpThermo nasa7(const MechView& m, int k, double T, double lnT, double invT) {
+  if (m.nasa9) return nasa9(m, k, T, lnT, invT);   // warp-uniform: a property of the mechanism
   const int S = m.nsp;
   const double tmid = m.nasa[14 * S + k];
   const double* a = m.nasa + ((T <= tmid) ? 0 : 7 * S) + k;

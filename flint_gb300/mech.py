@@ -58,6 +58,9 @@ class Species:
     thigh: float
     low: list   # 7 NASA coefficients valid in [tlow, tmid]
     high: list  # 7 NASA coefficients valid in [tmid, thigh]
+    # NASA-9 polynomials instead (1-3 ranges): [[T_lo, T_hi, a1..a7, b1, b2], ...];
+    # low/high are then unused
+    nasa9: list = None
 
 
 @dataclass
@@ -156,7 +159,30 @@ class Mechanism:
         a.update(arrh=arr, arrh0=arr0, troe=troe, rsp=rsp, rnu=rnu, rord=rord,
                  psp=psp, pnu=pnu, eff=eff)
         a["consts"] = np.array([self.r_eos, self.r_thermo, self.p_ref], dtype=np.float64)
+        if any(sp.nasa9 for sp in self.species):
+            a["nasa9"] = self.nasa9_array()
         return a
+
+    def nasa9_array(self):
+        """(ns, 32) NASA-9 rows: [nranges, T0, T1, T2, T3, 3 x (a1..a7, b1, b2)];
+        NASA-7 species in their exact NASA-9 form (a1 = a2 = 0)."""
+        out = np.zeros((self.ns, 32))
+        for k, sp in enumerate(self.species):
+            if sp.nasa9:
+                rng = [list(r) for r in sp.nasa9]
+            else:
+                lo, hi = list(sp.low), list(sp.high)
+                rng = [[sp.tlow, sp.tmid, 0.0, 0.0] + lo[:5] + [lo[5], lo[6]],
+                       [sp.tmid, sp.thigh, 0.0, 0.0] + hi[:5] + [hi[5], hi[6]]]
+            if not 1 <= len(rng) <= 3:
+                raise ValueError(f"species {sp.name}: 1-3 NASA-9 ranges supported")
+            out[k, 0] = len(rng)
+            bps = [rng[0][0]] + [r[1] for r in rng]
+            for i in range(4):
+                out[k, 1 + i] = bps[i] if i < len(bps) else np.inf
+            for i, r in enumerate(rng):
+                out[k, 5 + 9 * i:14 + 9 * i] = r[2:11]
+        return out
 
     def element_matrix(self):
         """(ne, ns) element counts; row order = self.elements."""
@@ -240,7 +266,7 @@ def _mw(comp):
 
 
 def from_yaml(path, phase_mw=None, name=None):
-    """Build a Mechanism from a Cantera-style YAML file (NASA7 species only).
+    """Build a Mechanism from a Cantera-style YAML file (NASA-7 or NASA-9 species).
 
     ``phase_mw`` optionally maps species -> molar mass as read from FLINT's
     ``phase.txt`` (the loader takes molar masses from there, not from the YAML).
@@ -249,18 +275,25 @@ def from_yaml(path, phase_mw=None, name=None):
     phase = d["phases"][0]
     conc_f, eaf = _unit_factors(d.get("units"))
     names = phase["species"]
+    if names == "all":   # Cantera's shorthand: every species of the file, in order
+        names = [s["name"] for s in d["species"]]
     spd = {s["name"]: s for s in d["species"]}
     species = []
     for n in names:
         s = spd[n]
         th = s["thermo"]
+        mw = phase_mw[n] if phase_mw and n in phase_mw else _mw(s["composition"])
+        tr = [float(x) for x in th["temperature-ranges"]]
+        if th["model"] == "NASA9":
+            rng = [[tr[i], tr[i + 1]] + [float(x) for x in th["data"][i]] for i in range(len(tr) - 1)]
+            species.append(Species(n, float(mw), dict(s["composition"]), tr[0], tr[1], tr[-1], [0.0] * 7,
+                                   [0.0] * 7, nasa9=rng))
+            continue
         if th["model"] != "NASA7":
-            raise ValueError(f"species {n}: thermo model {th['model']} is not NASA7")
-        tr = th["temperature-ranges"]
+            raise ValueError(f"species {n}: thermo model {th['model']} is neither NASA7 nor NASA9")
         low, high = th["data"][0], th["data"][-1]
         if len(tr) == 2:
             tr = [tr[0], tr[1], tr[1]]
-        mw = phase_mw[n] if phase_mw and n in phase_mw else _mw(s["composition"])
         species.append(Species(n, float(mw), dict(s["composition"]), float(tr[0]), float(tr[1]),
                                float(tr[2]), [float(x) for x in low], [float(x) for x in high]))
     reactions = []

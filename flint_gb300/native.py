@@ -30,7 +30,7 @@ class MechDesc(C.Structure):
                 ("arrh", _dp), ("arrh0", _dp), ("troe", _dp),
                 ("rsp", _ip), ("rnu", _dp), ("rord", _dp),
                 ("psp", _ip), ("pnu", _dp), ("eff", _dp),
-                ("r_eos", C.c_double), ("r_thermo", C.c_double), ("p_ref", C.c_double)]
+                ("r_eos", C.c_double), ("r_thermo", C.c_double), ("p_ref", C.c_double), ("nasa9", _dp)]
 
 
 class TableDesc(C.Structure):
@@ -78,6 +78,7 @@ def mech_desc(mech):
                  "rsp", "rnu", "rord", "psp", "pnu", "eff"):
         setattr(d, name, ptr(keep[name]))
     d.r_eos, d.r_thermo, d.p_ref = (float(x) for x in keep["consts"])
+    d.nasa9 = ptr(keep["nasa9"]) if "nasa9" in keep else None
     return d, keep
 
 

@@ -62,6 +62,21 @@ def table_desc(t):
 
 # ---------------------------------------------------------------- generator
 def _nasa(sp, T):
+    if sp.nasa9:
+        rng = sp.nasa9
+        idx = np.zeros(T.size, dtype=int)
+        for i, r in enumerate(rng[:-1]):
+            idx += (T > r[1]).astype(int)
+        a = np.array([r[2:11] for r in rng])[idx]
+        iT = 1.0 / T
+        cpR = a[:, 0] * iT ** 2 + a[:, 1] * iT + a[:, 2] + a[:, 3] * T + a[:, 4] * T ** 2 + a[:, 5] * T ** 3 + a[:, 6] * T ** 4
+        hRT = (-a[:, 0] * iT ** 2 + a[:, 1] * np.log(T) * iT + a[:, 2] + a[:, 3] * T / 2 + a[:, 4] * T ** 2 / 3
+               + a[:, 5] * T ** 3 / 4 + a[:, 6] * T ** 4 / 5 + a[:, 7] * iT)
+        sR = (-a[:, 0] * iT ** 2 / 2 - a[:, 1] * iT + a[:, 2] * np.log(T) + a[:, 3] * T + a[:, 4] * T ** 2 / 2
+              + a[:, 5] * T ** 3 / 3 + a[:, 6] * T ** 4 / 4 + a[:, 8])
+        dcpR = (-2 * a[:, 0] * iT ** 3 - a[:, 1] * iT ** 2 + a[:, 3] + 2 * a[:, 4] * T + 3 * a[:, 5] * T ** 2
+                + 4 * a[:, 6] * T ** 3)
+        return cpR, hRT, sR, dcpR
     a = np.where((T <= sp.tmid)[:, None], np.array(sp.low)[None, :], np.array(sp.high)[None, :])
     cpR = a[:, 0] + a[:, 1] * T + a[:, 2] * T ** 2 + a[:, 3] * T ** 3 + a[:, 4] * T ** 4
     hRT = a[:, 0] + a[:, 1] * T / 2 + a[:, 2] * T ** 2 / 3 + a[:, 3] * T ** 3 / 4 + a[:, 4] * T ** 4 / 5 + a[:, 5] / T

@@ -109,6 +109,21 @@ def _balanced(s: str) -> bool:
     return depth <= 0
 
 
+def _open_quote(content: str) -> bool:
+    """True when the value of a `key: value` or `- value` line opens a quoted
+    scalar that does not close on this line (it continues on the next)."""
+    m = re.match(r"^(?:-\s+)?(?:[^'\"\s][^:]*:\s+)?(['\"])", content)
+    if not m:
+        return False
+    q = m.group(1)
+    body = content[m.end():]
+    if q == "'":
+        body = body.replace("''", "")
+    else:
+        body = body.replace('\\"', "")
+    return q not in body
+
+
 class _Lines:
     def __init__(self, text: str):
         raw = text.splitlines()
@@ -134,11 +149,11 @@ class _Lines:
                 self.items.append((indent, content))
                 i = j
                 continue
-            # join multi-line flow collections
+            # join multi-line flow collections and quoted scalars
             j = i
-            while not _balanced(content) and j + 1 < len(raw):
+            while (not _balanced(content) or _open_quote(content)) and j + 1 < len(raw):
                 j += 1
-                content += " " + _strip_comment(raw[j]).strip()
+                content += " " + (raw[j].strip() if _open_quote(content) else _strip_comment(raw[j]).strip())
             self.items.append((indent, content))
             i = j + 1
 

@@ -70,15 +70,30 @@ def emit(m: mechmod.Mechanism, ident=None):
     # --- thermo: every species' NASA-7 pieces at this T
     w("    const double T2 = t * t, T3 = T2 * t, T4 = T3 * t;")
     for k, s in enumerate(m.species):
-        lo, hi = s.low, s.high
-        sel = [f"(t <= {_d(s.tmid)} ? {_d(a)} : {_d(b)})" for a, b in zip(lo, hi)]
         w(f"    double cpR{k}, hRT{k}, gRT{k};")
         w("    {")
-        for i in range(7):
-            w(f"      const double a{i} = {sel[i]};")
-        w(f"      cpR{k} = a0 + a1 * t + a2 * T2 + a3 * T3 + a4 * T4;")
-        w(f"      hRT{k} = a0 + a1 * t / 2.0 + a2 * T2 / 3.0 + a3 * T3 / 4.0 + a4 * T4 / 5.0 + a5 * invT;")
-        w(f"      const double sR = a0 * lnT + a1 * t + a2 * T2 / 2.0 + a3 * T3 / 3.0 + a4 * T4 / 4.0 + a6;")
+        if s.nasa9:
+            # NASA-9: pick the range, then the 9-coefficient forms
+            rng = s.nasa9
+            for i in range(9):
+                expr = _d(rng[-1][2 + i])
+                for r in reversed(rng[:-1]):
+                    expr = f"(t <= {_d(r[1])} ? {_d(r[2 + i])} : {expr})"
+                w(f"      const double c{i} = {expr};")
+            w("      const double iT2 = invT * invT;")
+            w(f"      cpR{k} = c0 * iT2 + c1 * invT + c2 + c3 * t + c4 * T2 + c5 * T3 + c6 * T4;")
+            w(f"      hRT{k} = -c0 * iT2 + c1 * lnT * invT + c2 + c3 * t / 2.0 + c4 * T2 / 3.0 + c5 * T3 / 4.0"
+              f" + c6 * T4 / 5.0 + c7 * invT;")
+            w("      const double sR = -c0 * iT2 / 2.0 - c1 * invT + c2 * lnT + c3 * t + c4 * T2 / 2.0"
+              " + c5 * T3 / 3.0 + c6 * T4 / 4.0 + c8;")
+        else:
+            lo, hi = s.low, s.high
+            sel = [f"(t <= {_d(s.tmid)} ? {_d(a)} : {_d(b)})" for a, b in zip(lo, hi)]
+            for i in range(7):
+                w(f"      const double a{i} = {sel[i]};")
+            w(f"      cpR{k} = a0 + a1 * t + a2 * T2 + a3 * T3 + a4 * T4;")
+            w(f"      hRT{k} = a0 + a1 * t / 2.0 + a2 * T2 / 3.0 + a3 * T3 / 4.0 + a4 * T4 / 5.0 + a5 * invT;")
+            w("      const double sR = a0 * lnT + a1 * t + a2 * T2 / 2.0 + a3 * T3 / 3.0 + a4 * T4 / 4.0 + a6;")
         w(f"      gRT{k} = hRT{k} - sR;")
         w("    }")
     # --- state

@@ -96,6 +96,11 @@ typedef struct {
   double r_eos;           /* gas constant of the EOS and energy equation (FLINT Runiv 8314.51) */
   double r_thermo;        /* gas constant of NASA-7 -> cp,h,s and Kc (8314.46261815324) */
   double p_ref;           /* standard pressure of Kc, Pa (101325)            */
+  /* optional NASA-9 thermo (NULL: nasa7 serves): [ns][32] = nranges (1-3),
+   * T0..T3 (range i is [T_i, T_i+1]; unused +inf), 3 x (a1..a7, b1, b2);
+   * when given it replaces nasa7 for every species (NASA-7 data enter it as
+   * a1 = a2 = 0) */
+  const double* nasa9;
 } flint_mech_desc;
 
 /* Tabulated mechanism: FLINT's own module arrays as read_idealgas_thermo and

@@ -48,9 +48,33 @@ static void set_threads(int nthreads) {
 }
 
 /* ------------------------------------------------------------------ thermo */
+/* NASA-9: cp/R = a1/T^2 + a2/T + a3 + a4 T + a5 T^2 + a6 T^3 + a7 T^4,
+ * h/RT = -a1/T^2 + a2 ln(T)/T + a3 + a4 T/2 + ... + a7 T^4/5 + b1/T,
+ * s/R = -a1/(2 T^2) - a2/T + a3 ln T + a4 T + ... + a7 T^4/4 + b2. */
+static void nasa9_thermo(const double* c, double T, double lnT, double* cpR, double* hRT, double* sR,
+                         double* dcpR) {
+  int nr = (int)c[0], r = 0;
+  if (nr > 1 && T > c[2]) r = 1;
+  if (nr > 2 && T > c[3]) r = 2;
+  const double* a = c + 5 + 9 * r;
+  double T2 = T * T, T3 = T2 * T, T4 = T3 * T, iT = 1.0 / T, iT2 = iT * iT;
+  if (cpR) cpR[0] = a[0] * iT2 + a[1] * iT + a[2] + a[3] * T + a[4] * T2 + a[5] * T3 + a[6] * T4;
+  if (hRT) hRT[0] = -a[0] * iT2 + a[1] * lnT * iT + a[2] + a[3] * T / 2.0 + a[4] * T2 / 3.0 + a[5] * T3 / 4.0
+                    + a[6] * T4 / 5.0 + a[7] * iT;
+  if (sR) sR[0] = -a[0] * iT2 / 2.0 - a[1] * iT + a[2] * lnT + a[3] * T + a[4] * T2 / 2.0 + a[5] * T3 / 3.0
+                  + a[6] * T4 / 4.0 + a[8];
+  if (dcpR) dcpR[0] = -2.0 * a[0] * iT2 * iT - a[1] * iT2 + a[3] + 2.0 * a[4] * T + 3.0 * a[5] * T2 + 4.0 * a[6] * T3;
+}
+
 void orc_species_thermo(const flint_mech_desc* m, double T, double* cpR, double* hRT,
                         double* sR, double* dcpR) {
   double lnT = log(T);
+  if (m->nasa9) {
+    for (int k = 0; k < m->ns; ++k)
+      nasa9_thermo(m->nasa9 + 32 * k, T, lnT, cpR ? cpR + k : NULL, hRT ? hRT + k : NULL, sR ? sR + k : NULL,
+                   dcpR ? dcpR + k : NULL);
+    return;
+  }
   for (int k = 0; k < m->ns; ++k) {
     const double* c = m->nasa7 + 17 * k;
     const double* a = (T <= c[1]) ? c + 3 : c + 10;

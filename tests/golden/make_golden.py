@@ -13,8 +13,9 @@ except unit conversion of YAML rate parameters into the IR):
 * tests/golden/pelucchi_thermo.json sampled rows of test/Pelucchi/INPUT/thermo.dat
 * tests/golden/mech_pelucchi.json  the Pelucchi YAML as a mechanism IR
 * tests/golden/wd_info.json        WD chemistry-info.txt stoichiometry + phase.txt
-* tests/golden/mech_<name>.json    the other in-tree NASA-7 mechanisms (Ecker, Smooke,
-                                   TSR-CDF-13, TSR-GP-24, TSR-Rich-31, Troyes, ZK) as IR
+* tests/golden/mech_<name>.json    the other in-tree mechanisms (Ecker, Smooke, TSR-CDF-13,
+                                   TSR-GP-24, TSR-Rich-31, Troyes, ZK, CORIA; WD and Cross
+                                   with NASA-9 thermo) as IR
 * flint_gb300/data/mech_c1.json    the 2-step CH4/air mechanism: WD reactions 1-2
                                    (test/WD/INPUT/WD.yaml) with NASA-7 data of CH4, O2,
                                    CO, CO2, H2O (TSR-Rich-31.yaml) and N2 (troyes.yaml),
@@ -65,11 +66,10 @@ def sample_rows(rows, temps):
     return out
 
 
-# the reference's in-tree mechanisms whose YAML uses NASA-7 thermo (WD and Cross
-# use NASA-9, CORIA a rate form outside the IR)
+# the reference's in-tree mechanisms (WD and Cross with NASA-9 thermo)
 INTREE = [("Ecker", "ecker.yaml"), ("Smooke", "smooke.yaml"), ("TSR-CDF-13", "TSR-CDF-13.yaml"),
           ("TSR-GP-24", "TSR-GP-24.yaml"), ("TSR-Rich-31", "TSR-Rich-31.yaml"), ("Troyes", "troyes.yaml"),
-          ("ZK", "ZK.yaml")]
+          ("ZK", "ZK.yaml"), ("CORIA", "coria.yaml"), ("WD", "WD.yaml"), ("Cross", "cross.yaml")]
 
 
 def main(ref):

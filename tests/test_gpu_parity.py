@@ -282,13 +282,14 @@ def test_reactor_c5_54_species():
     assert abs(nst.cpu().numpy().sum() / ns_o.sum() - 1.0) < 0.05
 
 
-INTREE = ["ecker", "smooke", "troyes", "tsr_cdf_13", "tsr_gp_24", "tsr_rich_31", "zk"]
+INTREE = ["ecker", "smooke", "troyes", "tsr_cdf_13", "tsr_gp_24", "tsr_rich_31", "zk", "coria", "wd", "cross"]
 
 
 @pytest.mark.parametrize("name", INTREE)
 def test_intree_mechanisms_wdot_jacobian_generated(name):
-    """The reference's own NASA-7 mechanisms (test/*/INPUT/*.yaml, as IR):
-    data-driven wdot and Jacobian, and the generated per-mechanism kernel."""
+    """The reference's own mechanisms (test/*/INPUT/*.yaml, as IR; WD and Cross
+    with NASA-9 thermo): data-driven wdot, cp, h and Jacobian, and the generated
+    per-mechanism kernel."""
     import os
     from flint_gb300.ytf_cuda import GeneratedMechanism
     mech = Mechanism.load(os.path.join(os.path.dirname(__file__), "golden", f"mech_{name}.json"))
@@ -299,11 +300,15 @@ def test_intree_mechanisms_wdot_jacobian_generated(name):
     _, J_o, Js_o = orc.wdot_jac_batch(T, p, Y)
     chem = Chemistry(mech)
     Tt, pt, Yt = cuda(T, p, Y)
-    w, _, _ = chem.wdot(Tt, pt, Yt)
+    cp, h = torch.empty_like(Tt), torch.empty_like(Tt)
+    w, _, _ = chem.wdot(Tt, pt, Yt, cp=cp, h=h)
     _, J = chem.wdot_jac(Tt, pt, Yt)
     wg, cpg, hg = GeneratedMechanism(mech).wdot(Tt, pt, Yt)
     torch.cuda.synchronize()
     assert wdot_err(w.cpu().numpy().ravel(), w_o, ws_o) < RTOL_WDOT
+    np.testing.assert_allclose(cp.cpu().numpy(), cp_o, rtol=1e-13)
+    hs = np.abs(h_o) + cp_o * T
+    assert np.max(np.abs(h.cpu().numpy() - h_o) / hs) < 1e-13
     assert wdot_err(wg.cpu().numpy().ravel(), w_o, ws_o) < RTOL_WDOT
     np.testing.assert_allclose(cpg.cpu().numpy(), cp_o, rtol=1e-13)
     err = np.abs(J.cpu().numpy().ravel() - J_o) / (Js_o + 1e-300)
