@@ -22,6 +22,7 @@ module FLINT_GPU
     type(c_ptr) :: mw, nasa7, rtype, reversible, arrh, arrh0, troe
     type(c_ptr) :: rsp, rnu, rord, psp, pnu, eff
     real(c_double) :: r_eos, r_thermo, p_ref
+    type(c_ptr) :: nasa9 = c_null_ptr   ! optional NASA-9 rows (ns, 32)
   end type flint_mech_desc
 
   type, bind(C) :: flint_reactor_opts
