@@ -12,6 +12,7 @@
 //
 // All kernels are grid-stride loops over cells sized to whole waves of the 152
 // SMs, so any N (including 0 and ragged tails) is handled without a tail kernel.
+#include <atomic>
 #include "flint_dev.cuh"
 #include "flint_host.h"
 
@@ -291,27 +292,30 @@ cudaError_t probe_fp64(double* tflops) {
 }
 
 // ---------------------------------------------------------------- launchers
-static int g_sms = 0;
+// Device properties, cached per device (the current device of the calling
+// thread); the cache entries are atomics, so concurrent first calls are safe.
+constexpr int MAX_DEV_CACHE = 64;
+static std::atomic<int> g_sms[MAX_DEV_CACHE];
+static std::atomic<int> g_optin[MAX_DEV_CACHE];
 
-int device_sms() {
-  if (g_sms == 0) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&g_sms, cudaDevAttrMultiProcessorCount, dev);
-    if (g_sms <= 0) g_sms = 1;
+static int cached_attr(std::atomic<int>* cache, cudaDeviceAttr attr, int fallback) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= MAX_DEV_CACHE) dev = 0;
+  int v = cache[dev].load(std::memory_order_relaxed);
+  if (v <= 0) {
+    if (cudaDeviceGetAttribute(&v, attr, dev) != cudaSuccess || v <= 0) {
+      (void)cudaGetLastError();
+      v = fallback;
+    }
+    cache[dev].store(v, std::memory_order_relaxed);
   }
-  return g_sms;
+  return v;
 }
 
-static int g_optin = 0;
+int device_sms() { return cached_attr(g_sms, cudaDevAttrMultiProcessorCount, 1); }
+
 size_t device_smem_optin() {
-  if (g_optin == 0) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&g_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-    if (g_optin <= 0) g_optin = 48 * 1024;
-  }
-  return (size_t)g_optin;
+  return (size_t)cached_attr(g_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, 48 * 1024);
 }
 
 static int64_t grid_for(const void* fn, int threads, size_t smem, int64_t work_items) {

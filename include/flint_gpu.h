@@ -17,6 +17,12 @@
  *   rhs_native(nz, time, Z, F)            src/lib/Lib_Chemistry_rhs.f90:15-52
  *   setup_odesolver / run_odesolver       OSlo, call sites src/test/Fortran/test-batchF.f90:81,105
  *   free_chemistry_data()                 src/lib/Lib_Chemistry_data.f90:168
+ *   cons2prim(cons, T)                    src/lib/Lib_ThermoTransport.f90:129-165
+ *   co_k_mi_lam_Wilke(rhoi, rho, T, ...)  src/lib/Lib_ThermoTransport.f90:407-462
+ *
+ * Threads: a handle (mechanism or surrogate) serves one thread at a time;
+ * different handles may be used concurrently.  The allocation-free reactor
+ * entry's static scratch is shared by every handle of a device.
  *
  * Device-pointer entry points take device (or managed) memory and are
  * asynchronous on `stream`; the *_host variants take host memory, stage it
