@@ -312,6 +312,46 @@ int flint_mech_destroy(flint_mech_t h) {
   return FLINT_OK;
 }
 
+int flint_tables_read(const char* folder, const char* prefix, flint_table_set_t* out) {
+  if (!folder || !out) return fail(FLINT_ERR_ARG, "NULL argument");
+  *out = nullptr;
+  auto* t = new flint_table_set_s();
+  std::string err;
+  int rc = tables_read(folder, prefix, t, err);
+  if (rc != FLINT_OK) { delete t; return fail(rc, "flint_tables_read(%s): %s", folder, err.c_str()); }
+  *out = t;
+  return FLINT_OK;
+}
+
+int flint_tables_desc(flint_table_set_t t, flint_table_desc* desc) {
+  if (!t || !desc) return fail(FLINT_ERR_ARG, "NULL argument");
+  tables_desc(t, desc);
+  return FLINT_OK;
+}
+
+const char* flint_tables_species_name(flint_table_set_t t, int k) {
+  if (!t || k < 0 || k >= t->ns) return nullptr;
+  return t->names[k].c_str();
+}
+
+int flint_tables_free(flint_table_set_t t) {
+  delete t;
+  return FLINT_OK;
+}
+
+int flint_mech_create_from_files(const char* folder, const char* prefix, flint_mech_t* out) {
+  if (!out) return fail(FLINT_ERR_ARG, "NULL argument");
+  *out = nullptr;
+  flint_table_set_t t = nullptr;
+  int rc = flint_tables_read(folder, prefix, &t);
+  if (rc != FLINT_OK) return rc;
+  flint_table_desc d;
+  tables_desc(t, &d);
+  rc = flint_mech_create_tables(&d, out);
+  delete t;
+  return rc;
+}
+
 int flint_mech_sizes(flint_mech_t h, int* ns, int* nr) {
   // (tabulated handles report their species and total reaction counts too)
   if (!h) return fail(FLINT_ERR_ARG, "NULL handle");

@@ -2,9 +2,21 @@
 #pragma once
 #include <cstdint>
 #include <string>
+#include <vector>
 #include <cuda_runtime.h>
 #include "flint_dev.cuh"
 #include "../../include/flint_gpu.h"
+
+// FLINT input files parsed on the host (flint_files.cu): the arrays of
+// flint_table_desc, owned here, in its Fortran layout.
+struct flint_table_set_s {
+  int ns = 0, tmin = 0, tmax = 0, ti1 = 0, ti2 = 0;
+  int nr[3] = {0, 0, 0};   // Arrhenius, Troe, Lindemann
+  std::vector<std::string> names;
+  std::vector<double> wm, cp, h, mu, kt;
+  std::vector<double> ni1[3], ni2[3], eps[3];
+  std::vector<double> kf, kb, ktroe[4], klind[3];
+};
 
 namespace flint {
 
@@ -88,5 +100,9 @@ cudaError_t table_transport(void* p, int64_t n, const double* rhoi, const double
                             cudaStream_t st);
 cudaError_t table_cons2prim(void* p, int64_t n, int np, const double* cons, const double* T, double* prim,
                             double* Tout, cudaStream_t st);
+
+// FLINT's tabulated input files -> arrays (flint_files.cu)
+int tables_read(const char* folder, const char* prefix, flint_table_set_s* t, std::string& err);
+void tables_desc(const flint_table_set_s* t, flint_table_desc* d);
 
 }  // namespace flint

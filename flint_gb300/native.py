@@ -114,6 +114,12 @@ def lib():
     L.flint_probe_fp64_peak.argtypes = [C.POINTER(C.c_double)]
     L.flint_selftest_exp.argtypes = [vp, i64, vp, vp, vp]
     L.flint_mech_create_tables.argtypes = [C.POINTER(TableDesc), C.POINTER(vp)]
+    L.flint_tables_read.argtypes = [C.c_char_p, C.c_char_p, C.POINTER(vp)]
+    L.flint_tables_desc.argtypes = [vp, C.POINTER(TableDesc)]
+    L.flint_tables_species_name.argtypes = [vp, C.c_int]
+    L.flint_tables_species_name.restype = C.c_char_p
+    L.flint_tables_free.argtypes = [vp]
+    L.flint_mech_create_from_files.argtypes = [C.c_char_p, C.c_char_p, C.POINTER(vp)]
     L.flint_rhs_native_batch.argtypes = [vp, i64, vp, vp, vp]
     L.flint_cons2prim_batch.argtypes = [vp, i64, C.c_int, vp, vp, vp, vp, vp]
     L.flint_transport_batch.argtypes = [vp, i64, vp, vp, vp, vp, vp]

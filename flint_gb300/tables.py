@@ -229,6 +229,10 @@ def write_folder(t, folder):
                      ["Temperature", "k_inf", "k_0", "k_c"],
                      [(f"Reaction {j + 1}", [t[n_][j] for n_ in ("kinf_lind", "k0_lind", "kc_lind")])
                       for j in range(t["nr_lind"])], T)
+    if t.get("mi_tab") is not None:
+        _write_zones(os.path.join(folder, "transport.dat"), "Transport Properties",
+                     ["Temperature", "Viscosity", "Conductivity"],
+                     [(names[k], [t["mi_tab"][k], t["k_tab"][k]]) for k in range(ns)], T)
 
 
 def read_tecplot_points(path):
@@ -307,6 +311,36 @@ def read_folder(folder, prefix=""):
     return t
 
 
+def read_folder_native(folder, prefix=""):
+    """The same files through the library's own reader (flint_tables_read):
+    a table dict of copies of its arrays, for callers and tests that want the
+    parse a Fortran-free host would do."""
+    L = native.lib()
+    h = C.c_void_p()
+    native.check(L.flint_tables_read(os.fsencode(folder), prefix.encode(), C.byref(h)), "flint_tables_read")
+    try:
+        d = native.TableDesc()
+        native.check(L.flint_tables_desc(h, C.byref(d)), "flint_tables_desc")
+        ns, nrow, nti = d.ns, d.tmax - d.tmin + 1, d.ti2 - d.ti1 + 1
+        t = {"ns": ns, "tmin": d.tmin, "tmax": d.tmax, "ti1": d.ti1, "ti2": d.ti2, "runiv": d.runiv,
+             "nr_arrh": d.nr_arrh, "nr_troe": d.nr_troe, "nr_lind": d.nr_lind,
+             "names": [L.flint_tables_species_name(h, k).decode() for k in range(ns)]}
+        nr = {"arrh": d.nr_arrh, "troe": d.nr_troe, "lind": d.nr_lind}
+        shape = {"wm": (ns,), "cp_tab": (ns, nrow), "h_tab": (ns, nrow), "mi_tab": (ns, nrow), "k_tab": (ns, nrow)}
+        for name in ARRAYS:
+            key = name.rsplit("_", 1)[-1]
+            shp = shape.get(name) or ((nr[key], ns + 1) if name[:3] in ("ni1", "ni2", "eps")
+                                      else (nr["arrh" if name in ("kf_tab", "kb_tab") else key], nti))
+            ptr = getattr(d, name)
+            t[name] = (np.ctypeslib.as_array(ptr, shape=shp).copy() if ptr and all(shp)
+                       else np.zeros(shp) if name not in ("mi_tab", "k_tab") else None)
+        if t["mi_tab"] is None:
+            del t["mi_tab"], t["k_tab"]
+        return t
+    finally:
+        L.flint_tables_free(h)
+
+
 # ----------------------------------------------------------------- handle
 class Tables:
     """A tabulated mechanism on the GPU: FLINT's general loop and rhs_native."""
@@ -319,6 +353,20 @@ class Tables:
         native.check(self.L.flint_mech_create_tables(C.byref(desc), C.byref(h)), "flint_mech_create_tables")
         self.h = h
         self.ns = t["ns"]
+
+    @classmethod
+    def from_files(cls, folder, prefix=""):
+        """A handle straight from FLINT's input files (flint_mech_create_from_files)."""
+        obj = cls.__new__(cls)
+        obj.L = native.lib()
+        h = C.c_void_p()
+        native.check(obj.L.flint_mech_create_from_files(os.fsencode(folder), prefix.encode(), C.byref(h)),
+                     "flint_mech_create_from_files")
+        obj.h, obj.t, obj._keep = h, None, {}
+        ns = C.c_int()
+        native.check(obj.L.flint_mech_sizes(h, C.byref(ns), None), "flint_mech_sizes")
+        obj.ns = ns.value
+        return obj
 
     def close(self):
         if self.h:

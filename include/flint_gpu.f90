@@ -2,6 +2,7 @@
 !>
 !> A FLINT caller replaces
 !>   read_idealgas_thermo / read_chemistry / Assign_Mechanism  -> flint_mech_create
+!>   the same readers on a folder of tabulated input files     -> flint_mech_create_from_files
 !>   loop over cells of chemistry_source(roi, T, omegadot)    -> flint_chemistry_source_batch
 !>   loop over cells of run_odesolver(neq, tin, tout, Z, rhs_native, err)
 !>                                                            -> flint_reactor_advance_host
@@ -35,6 +36,14 @@ module FLINT_GPU
     integer(c_int) function flint_mech_create(desc, mech) bind(C, name='flint_mech_create')
       import :: c_int, c_ptr, flint_mech_desc
       type(flint_mech_desc), intent(in) :: desc
+      type(c_ptr), intent(out) :: mech
+    end function
+
+    ! folder and prefix: NUL-terminated, e.g. trim(dir)//c_null_char
+    integer(c_int) function flint_mech_create_from_files(folder, prefix, mech) &
+        bind(C, name='flint_mech_create_from_files')
+      import :: c_int, c_char, c_ptr
+      character(kind=c_char), dimension(*), intent(in) :: folder, prefix
       type(c_ptr), intent(out) :: mech
     end function
 

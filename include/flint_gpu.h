@@ -79,6 +79,8 @@ enum {
 #define FLINT_MAXSP_PER_SIDE 3
 
 typedef struct flint_mech_s* flint_mech_t;
+/* FLINT input files parsed on the host (flint_tables_read). */
+typedef struct flint_table_set_s* flint_table_set_t;
 
 /* Analytic mechanism description: NASA-7 thermo + Arrhenius / third-body /
  * falloff kinetics with reverse rates from Kc (Gibbs).  All arrays are host
@@ -168,6 +170,24 @@ int flint_mech_create(const flint_mech_desc* desc, flint_mech_t* out);
  * copies the tables to device memory owned by *out.  Handles made this way
  * serve flint_chemistry_source_batch and flint_rhs_native_batch. */
 int flint_mech_create_tables(const flint_table_desc* desc, flint_mech_t* out);
+/* Replaces read_idealgas_thermo, read_idealgas_transport and read_chemistry
+ * (Load_ThermoTransport.f90:7-95, :129-174, Load_Chemistry.f90:7-164) for
+ * callers without FLINT's Fortran loaders: parses <folder>/<prefix>phase.txt,
+ * thermo.dat, chemistry-info.txt, chemistry-Arrhenius.dat and, when the
+ * mechanism has such reactions, chemistry-Troe.dat / chemistry-Lindemann.dat,
+ * plus transport.dat when present (Tecplot ASCII POINT zones, 1-K rows; a
+ * thermo table starting at 1 K gains the cloned row 0 with h = 0, as the
+ * reference builds it).  Host only, no GPU needed.  A missing or malformed
+ * file returns FLINT_ERR_IO with the reason in flint_last_error(), where the
+ * reference prints [ERROR] and returns or stops.  prefix may be NULL. */
+int flint_tables_read(const char* folder, const char* prefix, flint_table_set_t* out);
+/* Fill *desc with pointers into the set (valid until flint_tables_free). */
+int flint_tables_desc(flint_table_set_t set, flint_table_desc* desc);
+/* Name of species k (0-based) as phase.txt gives it. */
+const char* flint_tables_species_name(flint_table_set_t set, int k);
+int flint_tables_free(flint_table_set_t set);
+/* flint_tables_read + flint_mech_create_tables + flint_tables_free. */
+int flint_mech_create_from_files(const char* folder, const char* prefix, flint_mech_t* out);
 /* Replaces free_chemistry_data (Lib_Chemistry_data.f90:168). */
 int flint_mech_destroy(flint_mech_t mech);
 /* Text of the last error on the calling thread ("" if none). */

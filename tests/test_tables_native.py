@@ -1,0 +1,116 @@
+"""The library's own reader of FLINT's input files (flint_tables_read, the C
+counterpart of read_idealgas_thermo / read_idealgas_transport / read_chemistry,
+Load_ThermoTransport.f90:7-174, Load_Chemistry.f90:7-164) against the Python
+reader on the same folders, and its error returns.  Host only: no GPU."""
+import copy
+import json
+import os
+
+import numpy as np
+import pytest
+
+from flint_gb300 import mechgen, native, tables
+from flint_gb300.mech import Mechanism
+
+GOLD = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def _same(a, b):
+    assert a["ns"] == b["ns"] and a["names"] == b["names"]
+    for k in ("tmin", "tmax", "ti1", "ti2", "nr_arrh", "nr_troe", "nr_lind"):
+        assert a[k] == b[k], k
+    for k in tables.ARRAYS:
+        if b.get(k) is None or np.asarray(b[k]).size == 0:
+            assert a.get(k) is None or np.asarray(a[k]).size == 0, k
+            continue
+        np.testing.assert_array_equal(a[k], np.asarray(b[k]).reshape(a[k].shape), err_msg=k)
+
+
+@pytest.fixture(scope="module")
+def pel_folder(tmp_path_factory):
+    m = Mechanism.load(os.path.join(GOLD, "mech_pelucchi.json"))
+    t = tables.generate(m, 1, 3000)
+    d = tmp_path_factory.mktemp("pel")
+    tables.write_folder(t, str(d))
+    return t, str(d)
+
+
+def test_native_reader_matches_python_reader(pel_folder):
+    t, d = pel_folder
+    a, b = tables.read_folder_native(d), tables.read_folder(d)
+    _same(a, b)
+    assert a["tmin"] == 0 and np.all(a["h_tab"][:, 0] == 0.0)   # row 0 cloned, h(0) = 0
+    assert a["nr_troe"] == 2 and a["nr_lind"] == 4
+    assert a["runiv"] == 8314.51
+
+
+def test_native_reader_transport_and_prefix(tmp_path):
+    m = copy.deepcopy(mechgen.load("c1"))
+    t = tables.generate(m, 200, 4000)
+    T = np.arange(t["tmin"], t["tmax"] + 1, dtype=np.float64)
+    t["mi_tab"] = np.array([(1.0 + 0.1 * k) * 1.8e-5 * (T / 300.0) ** 0.7 for k in range(m.ns)])
+    t["k_tab"] = np.array([(1.0 + 0.1 * k) * 0.025 * (T / 300.0) ** 0.8 for k in range(m.ns)])
+    tables.write_folder(t, str(tmp_path))
+    for f in os.listdir(tmp_path):                      # same files under a prefix
+        os.link(tmp_path / f, tmp_path / ("case_" + f))
+    a, b = tables.read_folder_native(str(tmp_path), "case_"), tables.read_folder(str(tmp_path), "case_")
+    _same(a, b)
+    assert a["tmin"] == 200 and a["mi_tab"].shape == (m.ns, 3801)
+
+
+def test_native_reader_reference_chemistry_info(tmp_path):
+    """The reference's WD chemistry-info.txt and phase.txt, as in the Python reader's test."""
+    g = json.load(open(os.path.join(GOLD, "wd_info.json")))
+    (tmp_path / "chemistry-info.txt").write_text("\n".join(g["info_lines"]) + "\n")
+    (tmp_path / "phase.txt").write_text("ideal-gas phase\n" + "".join(f"{k} {v}\n" for k, v in g["phase"].items()))
+    T = np.arange(1.0, 11.0)
+    names = list(g["phase"])
+    tables._write_zones(str(tmp_path / "thermo.dat"), "t", ["Temperature", "Cp", "Enthalpy", "Entropy", "dCp"],
+                        [(n, [np.full(10, 1000.0 + i), np.arange(10.0) * (i + 1), np.ones(10), np.zeros(10)])
+                         for i, n in enumerate(names)], T)
+    tables._write_zones(str(tmp_path / "chemistry-Arrhenius.dat"), "a", ["Temperature", "kf", "kb"],
+                        [(f"Reaction {j + 1}", [np.arange(10.0) + j, np.zeros(10)]) for j in range(3)], T)
+    a, b = tables.read_folder_native(str(tmp_path)), tables.read_folder(str(tmp_path))
+    _same(a, b)
+    assert a["ni1_arrh"][0, names.index("O2")] == 1.5 and a["ni2_arrh"][0, names.index("H2O")] == 2.0
+
+
+def test_native_reader_fortran_exponents(tmp_path):
+    """Tecplot rows written with Fortran D exponents parse like E exponents."""
+    m = copy.deepcopy(mechgen.load("c1"))
+    t = tables.generate(m, 300, 400)
+    tables.write_folder(t, str(tmp_path))
+    for f in ("thermo.dat", "chemistry-Arrhenius.dat"):
+        p = tmp_path / f
+        p.write_text(p.read_text().replace("E+", "D+").replace("E-", "D-"))
+    _same(tables.read_folder_native(str(tmp_path)), tables.read_folder(str(tmp_path)))
+
+
+@pytest.mark.parametrize("missing", ["phase.txt", "thermo.dat", "chemistry-info.txt", "chemistry-Arrhenius.dat",
+                                     "chemistry-Troe.dat"])
+def test_native_reader_missing_file_is_an_io_error(pel_folder, tmp_path, missing):
+    _, d = pel_folder
+    for f in os.listdir(d):
+        if f != missing:
+            os.link(os.path.join(d, f), tmp_path / f)
+    with pytest.raises(RuntimeError, match=r"status 4\).*" + missing.split(".")[0]):
+        tables.read_folder_native(str(tmp_path))
+
+
+def test_native_reader_ragged_zone_is_an_io_error(pel_folder, tmp_path):
+    _, d = pel_folder
+    for f in os.listdir(d):
+        os.link(os.path.join(d, f), tmp_path / f)
+    p = tmp_path / "chemistry-Arrhenius.dat"
+    lines = open(os.path.join(d, "chemistry-Arrhenius.dat")).read().splitlines()
+    del lines[10]                                          # one row short in zone 1
+    os.unlink(p)
+    p.write_text("\n".join(lines) + "\n")
+    with pytest.raises(RuntimeError, match="ragged"):
+        tables.read_folder_native(str(tmp_path))
+
+
+def test_from_files_null_arguments():
+    L = native.lib()
+    assert L.flint_tables_read(None, None, None) == 1
+    assert L.flint_mech_create_from_files(b"/nonexistent-folder", None, None) == 1
