@@ -120,6 +120,27 @@ static int pack(const flint_mech_desc* d, ImageLayout& L, std::vector<uint8_t>& 
   int nlist = 0;
   for (auto& l : lists) nlist += (int)l.size();
   L.nlist = nlist;
+  // third-body rows in sparse form (ImageLayout::o_tbd): the row's most
+  // common efficiency times the total concentration plus the exceptions
+  std::vector<double> tbd, tbv;
+  std::vector<int> tbp{0}, tbs;
+  for (int rr = 0; rr < nr; ++rr) {
+    const int r = order[rr];
+    if (d->rtype[r] == 0) continue;
+    const double* e = d->eff + (size_t)r * ns;
+    double mode = e[0];
+    int best = 0;
+    for (int a = 0; a < ns; ++a) {
+      int c = 0;
+      for (int b = 0; b < ns; ++b) c += e[b] == e[a];
+      if (c > best) { best = c; mode = e[a]; }
+    }
+    tbd.push_back(mode);
+    for (int k = 0; k < ns; ++k)
+      if (e[k] != mode) { tbs.push_back(k); tbv.push_back(e[k] - mode); }
+    tbp.push_back((int)tbs.size());
+  }
+  const int ntbl = std::max((int)tbs.size(), 1);
   const int S = L.nsp, P = L.nrpad;
   int off = 0;
   auto sec = [&](int bytes) { int o = off; off = rup(off + bytes, 16); return o; };
@@ -129,7 +150,7 @@ static int pack(const flint_mech_desc* d, ImageLayout& L, std::vector<uint8_t>& 
   L.o_rnu = sec(8 * 3 * P); L.o_rord = sec(8 * 3 * P); L.o_pnu = sec(8 * 3 * P);
   L.o_rsp = sec(4 * 3 * P); L.o_psp = sec(4 * 3 * P); L.o_code = sec(4 * P); L.o_dnu = sec(8 * P);
   L.o_pcode = sec(4 * P);
-  L.o_eff = sec(8 * L.ntb * S);
+  L.o_tbd = sec(8 * L.ntb); L.o_tbp = sec(4 * (L.ntb + 1)); L.o_tbs = sec(4 * ntbl); L.o_tbv = sec(8 * ntbl);
   L.o_cstart = sec(4 * (S + 1)); L.o_lr = sec(4 * std::max(nlist, 1)); L.o_lnu = sec(8 * std::max(nlist, 1));
   L.o_exptab = sec(8 * 64);
   L.o_nasa9 = d->nasa9 ? sec(8 * 32 * S) : -1;
@@ -151,6 +172,10 @@ static int pack(const flint_mech_desc* d, ImageLayout& L, std::vector<uint8_t>& 
       for (int j = 0; j < 32; ++j) D(L.o_nasa9)[j * S + k] = d->nasa9[32 * k + j];
   }
   for (int i = 0; i < 3 * P; ++i) { I(L.o_rsp)[i] = -1; I(L.o_psp)[i] = -1; }
+  std::copy(tbd.begin(), tbd.end(), D(L.o_tbd));
+  std::copy(tbp.begin(), tbp.end(), I(L.o_tbp));
+  std::copy(tbs.begin(), tbs.end(), I(L.o_tbs));
+  std::copy(tbv.begin(), tbv.end(), D(L.o_tbv));
   int tb = 0;
   for (int rr = 0; rr < nr; ++rr) {
     int r = order[rr];
@@ -191,7 +216,6 @@ static int pack(const flint_mech_desc* d, ImageLayout& L, std::vector<uint8_t>& 
     }
     if (t != 0) {
       w |= (uint32_t)tb << 8;
-      for (int k = 0; k < ns; ++k) D(L.o_eff)[tb * S + k] = d->eff[(size_t)r * ns + k];
       ++tb;
     }
     reinterpret_cast<uint32_t*>(img.data() + L.o_code)[rr] = w;

@@ -52,7 +52,13 @@ struct ImageLayout {
   int o_code;                    // uint32 [nrpad]
   int o_pcode;                   // uint32 [nrpad]: product order codes, 4 bits per slot
   int o_dnu;                     // double [nrpad]
-  int o_eff;                     // [ntb][nsp]
+  // third-body rows, sparse: M_t = tbd[t] * sum_k c_k + sum over e in
+  // [tbp[t], tbp[t+1]) of tbv[e] * c[tbs[e]], tbd[t] the row's most common
+  // efficiency and tbv the others minus tbd[t]
+  int o_tbd;                     // double [ntb]
+  int o_tbp;                     // int32 [ntb+1]
+  int o_tbs;                     // int32 [ntbl]
+  int o_tbv;                     // double [ntbl]
   int o_cstart;                  // int32 [nsp+1]
   int o_lr;                      // int32 [nlist]
   int o_lnu;                     // double [nlist]
@@ -70,7 +76,8 @@ struct MechView {
   const int *rsp, *psp, *cstart, *lr;
   const uint32_t* code;
   const uint32_t* pcode;
-  const double *eff, *lnu, *exptab;
+  const double *tbd, *tbv, *lnu, *exptab;
+  const int *tbp, *tbs;
   const double* nasa9;   // null: NASA-7 (nasa)
   int nfall;
 
@@ -88,12 +95,21 @@ struct MechView {
     rsp = (const int*)(base + L.o_rsp); psp = (const int*)(base + L.o_psp);
     code = (const uint32_t*)(base + L.o_code);
     pcode = (const uint32_t*)(base + L.o_pcode);
-    eff = (const double*)(base + L.o_eff);
+    tbd = (const double*)(base + L.o_tbd); tbv = (const double*)(base + L.o_tbv);
+    tbp = (const int*)(base + L.o_tbp); tbs = (const int*)(base + L.o_tbs);
     cstart = (const int*)(base + L.o_cstart); lr = (const int*)(base + L.o_lr);
     lnu = (const double*)(base + L.o_lnu);
     nasa9 = L.o_nasa9 >= 0 ? (const double*)(base + L.o_nasa9) : nullptr;
   }
 };
+
+// Third-body concentration of efficiency row t (sparse form, see o_tbd):
+// M = sum_k eff_k c_k with ctot = sum_k c_k.
+__device__ __forceinline__ double tb_conc(const MechView& m, int t, double ctot, const double* c) {
+  double M = m.tbd[t] * ctot;
+  for (int e = m.tbp[t]; e < m.tbp[t + 1]; ++e) M = fma(m.tbv[e], c[m.tbs[e]], M);
+  return M;
+}
 
 // Copy the image (global) into shared memory; whole block participates.
 __device__ inline void stage_image(uint8_t* smem, const uint8_t* __restrict__ g, int bytes) {
@@ -328,6 +344,7 @@ __device__ void warp_kinetics(const MechView& m, const WarpScratch& s, int lane,
   double wbar = rr * T * p;
   const double invp = rr * T * sumYW;
   double rho = p * m.inv_r_eos * invT * wbar;   // p / (R T sum Y/W)
+  const double ctot = rho * sumYW;                 // sum_k c_k
   // species-parallel: concentrations and thermo, species k = lane + 32 j
   double my_cpR[SPL], my_hRT[SPL], my_dcpR[SPL], my_c[SPL];
 #pragma unroll
@@ -379,9 +396,7 @@ __device__ void warp_kinetics(const MechView& m, const WarpScratch& s, int lane,
       const int r = f0 + lane, P = m.nrpad;
       const uint32_t w = m.code[r];
       troe = rx_type(w) == 3;
-      const double* effrow = m.eff + rx_tbrow(w) * nsp;
-      double M = 0.0;
-      for (int k = 0; k < ns; ++k) M += effrow[k] * s.c[k];
+      const double M = tb_conc(m, rx_tbrow(w), ctot, s.c);
       kinf = fo[lane];
       kratio = fo[WARP + lane];
       Pr = kratio * M;
@@ -489,10 +504,7 @@ __device__ void warp_kinetics(const MechView& m, const WarpScratch& s, int lane,
       }
       double Mfac = 1.0, keff = kf, dlnkeff = dlnkf, dkdM = 0.0;
       if (type == 1) {
-        const double* effrow = m.eff + rx_tbrow(w) * nsp;
-        double M = 0.0;
-        for (int k = 0; k < ns; ++k) M += effrow[k] * s.c[k];
-        Mfac = M;
+        Mfac = tb_conc(m, rx_tbrow(w), ctot, s.c);
       } else if (type >= 2) {
         const int i = r - f0;
         keff = fo[5 * WARP + i]; dlnkeff = fo[6 * WARP + i]; dkdM = fo[7 * WARP + i];
@@ -572,6 +584,7 @@ __device__ void warp_kinetics(const MechView& m, const WarpScratch& s, int lane,
     if (k < ns) {
       double* Jrow = s.Jr + k * ld;
       for (int jj = 0; jj < ns; ++jj) Jrow[jj] = 0.0;
+      double tball = 0.0;   // third-body terms common to every column
       for (int e = m.cstart[k]; e < m.cstart[k + 1]; ++e) {
         const int r = m.lr[e];
         const double nu = m.lnu[e];
@@ -585,11 +598,14 @@ __device__ void warp_kinetics(const MechView& m, const WarpScratch& s, int lane,
         const uint32_t w = m.code[r];
         if (rx_type(w) != 0) {
           const double t = nu * s.dq[6 * nrpad + r];
-          const double* effrow = m.eff + rx_tbrow(w) * nsp;
-          for (int jj = 0; jj < ns; ++jj) Jrow[jj] += t * effrow[jj];
+          const int row = rx_tbrow(w);
+          tball = fma(t, m.tbd[row], tball);
+          for (int q = m.tbp[row]; q < m.tbp[row + 1]; ++q) Jrow[m.tbs[q]] += t * m.tbv[q];
         }
         JT[j] += nu * s.dq[7 * nrpad + r];
       }
+      if (tball != 0.0)
+        for (int jj = 0; jj < ns; ++jj) Jrow[jj] += tball;
     }
   }
   __syncwarp();

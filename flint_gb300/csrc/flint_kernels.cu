@@ -44,7 +44,7 @@ k_wdot_small(const uint8_t* __restrict__ img, ImageLayout L, int64_t n, int layo
     const double T = Tg[i];
     const double lnT = log(T), invT = 1.0 / T;
     double rho;
-    double cpm = 0.0, hm = 0.0;
+    double cpm = 0.0, hm = 0.0, ctot = 0.0;
     if (roi_mode) {
       // chemistry_source(roi, T, omegadot): c = max(roi,0)/W (WD.f90:18-21)
       rho = 0.0;
@@ -53,6 +53,7 @@ k_wdot_small(const uint8_t* __restrict__ img, ImageLayout L, int64_t n, int layo
         r = r > 0.0 ? r : 0.0;
         roi_io[i * ns + k] = r;
         CS(k) = r * m.invmw[k];
+        ctot += CS(k);
       }
     } else {
       double sumYW = 0.0;
@@ -68,6 +69,7 @@ k_wdot_small(const uint8_t* __restrict__ img, ImageLayout L, int64_t n, int layo
         cpm += y * th.cpR * m.invmw[k];
         hm += y * th.hRT * m.invmw[k];
         CS(k) = rho * y * m.invmw[k];
+        ctot += CS(k);
         GS(k) = th.hRT - th.sR;
       }
     }
@@ -107,9 +109,9 @@ k_wdot_small(const uint8_t* __restrict__ img, ImageLayout L, int64_t n, int layo
       }
       double keff = kf, Mfac = 1.0;
       if (type != 0) {
-        const double* effrow = m.eff + rx_tbrow(w) * m.nsp;
-        double M = 0.0;
-        for (int k = 0; k < ns; ++k) M += effrow[k] * CS(k);
+        const int row = rx_tbrow(w);
+        double M = m.tbd[row] * ctot;
+        for (int e = m.tbp[row]; e < m.tbp[row + 1]; ++e) M = fma(m.tbv[e], CS(m.tbs[e]), M);
         if (type == 1) Mfac = M;
         else keff = falloff_eval(m, r, type, kf, 0.0, M, T, lnT, invT).keff;
       }
