@@ -42,22 +42,18 @@ from flint_gb300 import dist as fdist  # noqa: E402
 
 CELLS = 262144
 METRIC = "cell-steps/s on 1 GB300: surrogate+fallback vs plain FP64 at stated T/Y error"
-# FP64 pipe ops (DADD + DMUL + 2*DFMA, thread level) per event of the reactor
-# kernel on the 31-species mechanism, from ncu counts of the standalone
-# source-term / Jacobian kernels (profiles/fp64_ops_per_event.md) plus the
-# dense LU counts of a 32x32 system.
 # FP64 FLOPs per kinetics evaluation (2 x DFMA + DADD + DMUL thread instructions,
 # predicated on) of the warp kernels, per state: k_wdot_warp<0> for one RHS and
 # k_wdot_warp<1> for one Jacobian, from ncu on the c2-wdot / c2-wdotjac and
 # c5-wdot / c5-wdotjac workloads (profiles/fp64_ops_per_state.md).
-KINETICS_FLOPS = {"synthetic-31sp-160r": {"rhs": 20645.0, "jac": 47315.0},
-                  "synthetic-54sp-320r": {"rhs": 36305.0, "jac": 97972.0}}
+KINETICS_FLOPS = {"synthetic-31sp-160r": {"rhs": 18800.0, "jac": 40686.0},
+                  "synthetic-54sp-320r": {"rhs": 31720.0, "jac": 82537.0}}
 
 
 # DRAM bytes (read + write) per cell of one k_reactor launch, from ncu
-# (profiles/k_reactor_c3_8192cells.md: 3.01 MB for 8,192 cells of the
+# (profiles/k_reactor_c3_8192cells.md: 2.70 MB for 8,192 cells of the
 # 31-species workload); the traffic field scales it by the launch's cells.
-REACTOR_DRAM_BYTES_PER_CELL = {"synthetic-31sp-160r": 3.012608e6 / 8192}
+REACTOR_DRAM_BYTES_PER_CELL = {"synthetic-31sp-160r": 2.699264e6 / 8192}
 
 
 def fp64_ops(ev, ns, mech_name="synthetic-31sp-160r"):
