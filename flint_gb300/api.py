@@ -66,6 +66,20 @@ class Chemistry:
         self.ns, self.nr = mech.ns, mech.nr
 
     @classmethod
+    def from_ir(cls, blob, mech: Mechanism = None):
+        """A handle from an IR blob (flint_mech_create_from_ir); `mech` only
+        labels the object (its .mech), the kernels see the blob's data."""
+        obj = cls.__new__(cls)
+        obj.mech, obj.L = mech, native.lib()
+        h = C.c_void_p()
+        native.check(obj.L.flint_mech_create_from_ir(bytes(blob), len(blob), C.byref(h)), "flint_mech_create_from_ir")
+        obj.h = h
+        ns, nr = C.c_int(), C.c_int()
+        native.check(obj.L.flint_mech_sizes(h, C.byref(ns), C.byref(nr)), "flint_mech_sizes")
+        obj.ns, obj.nr = ns.value, nr.value
+        return obj
+
+    @classmethod
     def from_config(cls, name):
         from . import mechgen
         return cls(mechgen.load(name))

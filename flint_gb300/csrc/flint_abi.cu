@@ -363,6 +363,46 @@ int flint_tables_free(flint_table_set_t t) {
   return FLINT_OK;
 }
 
+int flint_ir_parse(const void* blob, int64_t bytes, flint_ir_t* out) {
+  if (!blob || !out) return fail(FLINT_ERR_ARG, "NULL argument");
+  *out = nullptr;
+  auto* ir = new flint_ir_s();
+  std::string err;
+  int rc = ir_parse(blob, bytes, ir, err);
+  if (rc != FLINT_OK) { delete ir; return fail(rc, "flint_ir_parse: %s", err.c_str()); }
+  *out = ir;
+  return FLINT_OK;
+}
+
+int flint_ir_desc(flint_ir_t ir, flint_mech_desc* desc) {
+  if (!ir || !desc) return fail(FLINT_ERR_ARG, "NULL argument");
+  ir_desc(ir, desc);
+  return FLINT_OK;
+}
+
+int flint_ir_free(flint_ir_t ir) {
+  delete ir;
+  return FLINT_OK;
+}
+
+int64_t flint_ir_bytes(int ns, int nr, int nasa9) {
+  if (ns < 1 || nr < 0) return -1;
+  return ir_bytes(ns, nr, nasa9 != 0);
+}
+
+int flint_mech_create_from_ir(const void* blob, int64_t bytes, flint_mech_t* out) {
+  if (!out) return fail(FLINT_ERR_ARG, "NULL argument");
+  *out = nullptr;
+  flint_ir_t ir = nullptr;
+  int rc = flint_ir_parse(blob, bytes, &ir);
+  if (rc != FLINT_OK) return rc;
+  flint_mech_desc d;
+  ir_desc(ir, &d);
+  rc = flint_mech_create(&d, out);
+  delete ir;
+  return rc;
+}
+
 int flint_mech_create_from_files(const char* folder, const char* prefix, flint_mech_t* out) {
   if (!out) return fail(FLINT_ERR_ARG, "NULL argument");
   *out = nullptr;

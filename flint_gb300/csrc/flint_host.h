@@ -18,6 +18,14 @@ struct flint_table_set_s {
   std::vector<double> kf, kb, ktroe[4], klind[3];
 };
 
+// A parsed mechanism IR blob (flint_ir.cu): the arrays of flint_mech_desc.
+struct flint_ir_s {
+  int ns = 0, nr = 0, flags = 0;
+  double consts[3] = {0.0, 0.0, 0.0};   // r_eos, r_thermo, p_ref
+  std::vector<double> mw, nasa7, arrh, arrh0, troe, rnu, rord, pnu, eff, nasa9;
+  std::vector<int> rtype, reversible, rsp, psp;
+};
+
 namespace flint {
 
 void count_launch();
@@ -104,5 +112,10 @@ cudaError_t table_cons2prim(void* p, int64_t n, int np, const double* cons, cons
 // FLINT's tabulated input files -> arrays (flint_files.cu)
 int tables_read(const char* folder, const char* prefix, flint_table_set_s* t, std::string& err);
 void tables_desc(const flint_table_set_s* t, flint_table_desc* d);
+
+// mechanism IR blob -> arrays (flint_ir.cu)
+int64_t ir_bytes(int ns, int nr, bool nasa9);
+int ir_parse(const void* blob, int64_t bytes, flint_ir_s* ir, std::string& err);
+void ir_desc(const flint_ir_s* ir, flint_mech_desc* d);
 
 }  // namespace flint

@@ -163,6 +163,24 @@ class Mechanism:
             a["nasa9"] = self.nasa9_array()
         return a
 
+    # Field order of the IR blob after its header (flint_mech_create_from_ir)
+    IR_FIELDS = (("mw", "<f8"), ("nasa7", "<f8"), ("rtype", "<i4"), ("reversible", "<i4"), ("arrh", "<f8"),
+                 ("arrh0", "<f8"), ("troe", "<f8"), ("rsp", "<i4"), ("rnu", "<f8"), ("rord", "<f8"),
+                 ("psp", "<i4"), ("pnu", "<f8"), ("eff", "<f8"))
+
+    def to_ir(self):
+        """The mechanism as one IR blob (bytes): the 48-byte header "FLIR",
+        version 1, ns, nr, flags (bit 0: NASA-9), 0, r_eos, r_thermo, p_ref, then
+        the arrays of to_arrays() little-endian in IR_FIELDS order (+ nasa9)."""
+        a = self.to_arrays()
+        n9 = "nasa9" in a
+        head = (np.array([0x52494C46, 1, self.ns, self.nr, 1 if n9 else 0, 0], dtype="<u4").tobytes()
+                + np.asarray(a["consts"], dtype="<f8").tobytes())
+        body = [np.ascontiguousarray(a[k], dtype=t).tobytes() for k, t in self.IR_FIELDS]
+        if n9:
+            body.append(np.ascontiguousarray(a["nasa9"], dtype="<f8").tobytes())
+        return head + b"".join(body)
+
     def nasa9_array(self):
         """(ns, 32) NASA-9 rows: [nranges, T0, T1, T2, T3, 3 x (a1..a7, b1, b2)];
         NASA-7 species in their exact NASA-9 form (a1 = a2 = 0)."""

@@ -120,6 +120,12 @@ def lib():
     L.flint_tables_species_name.restype = C.c_char_p
     L.flint_tables_free.argtypes = [vp]
     L.flint_mech_create_from_files.argtypes = [C.c_char_p, C.c_char_p, C.POINTER(vp)]
+    L.flint_ir_parse.argtypes = [C.c_char_p, i64, C.POINTER(vp)]
+    L.flint_ir_desc.argtypes = [vp, C.POINTER(MechDesc)]
+    L.flint_ir_free.argtypes = [vp]
+    L.flint_ir_bytes.argtypes = [C.c_int, C.c_int, C.c_int]
+    L.flint_ir_bytes.restype = i64
+    L.flint_mech_create_from_ir.argtypes = [C.c_char_p, i64, C.POINTER(vp)]
     L.flint_rhs_native_batch.argtypes = [vp, i64, vp, vp, vp]
     L.flint_cons2prim_batch.argtypes = [vp, i64, C.c_int, vp, vp, vp, vp, vp]
     L.flint_transport_batch.argtypes = [vp, i64, vp, vp, vp, vp, vp]

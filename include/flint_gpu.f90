@@ -3,6 +3,7 @@
 !> A FLINT caller replaces
 !>   read_idealgas_thermo / read_chemistry / Assign_Mechanism  -> flint_mech_create
 !>   the same readers on a folder of tabulated input files     -> flint_mech_create_from_files
+!>   a mechanism held as one IR byte string                    -> flint_mech_create_from_ir
 !>   loop over cells of chemistry_source(roi, T, omegadot)    -> flint_chemistry_source_batch
 !>   loop over cells of run_odesolver(neq, tin, tout, Z, rhs_native, err)
 !>                                                            -> flint_reactor_advance_host
@@ -44,6 +45,15 @@ module FLINT_GPU
         bind(C, name='flint_mech_create_from_files')
       import :: c_int, c_char, c_ptr
       character(kind=c_char), dimension(*), intent(in) :: folder, prefix
+      type(c_ptr), intent(out) :: mech
+    end function
+
+    ! blob: the mechanism IR bytes (layout in flint_gpu.h), nbytes its length
+    integer(c_int) function flint_mech_create_from_ir(blob, nbytes, mech) &
+        bind(C, name='flint_mech_create_from_ir')
+      import :: c_int, c_int8_t, c_int64_t, c_ptr
+      integer(c_int8_t), dimension(*), intent(in) :: blob
+      integer(c_int64_t), value :: nbytes
       type(c_ptr), intent(out) :: mech
     end function
 

@@ -81,6 +81,8 @@ enum {
 typedef struct flint_mech_s* flint_mech_t;
 /* FLINT input files parsed on the host (flint_tables_read). */
 typedef struct flint_table_set_s* flint_table_set_t;
+/* A parsed mechanism IR blob (flint_ir_parse). */
+typedef struct flint_ir_s* flint_ir_t;
 
 /* Analytic mechanism description: NASA-7 thermo + Arrhenius / third-body /
  * falloff kinetics with reverse rates from Kc (Gibbs).  All arrays are host
@@ -188,6 +190,29 @@ const char* flint_tables_species_name(flint_table_set_t set, int k);
 int flint_tables_free(flint_table_set_t set);
 /* flint_tables_read + flint_mech_create_tables + flint_tables_free. */
 int flint_mech_create_from_files(const char* folder, const char* prefix, flint_mech_t* out);
+
+/* Mechanism IR blob: flint_mech_desc serialized as one byte string, the
+ * form a caller stores or sends an analytic mechanism in (flint_gb300.mech
+ * writes it: Mechanism.to_ir()).  Little-endian, packed, no padding:
+ *   header (48 bytes): "FLIR", uint32 version = 1, int32 ns, int32 nr,
+ *     uint32 flags (bit 0: NASA-9 section present), uint32 0,
+ *     double r_eos, r_thermo, p_ref;
+ *   then, in this order: double mw[ns], nasa7[ns][17]; int32 rtype[nr],
+ *     reversible[nr]; double arrh[nr][3], arrh0[nr][3], troe[nr][4];
+ *     int32 rsp[nr][3]; double rnu[nr][3], rord[nr][3]; int32 psp[nr][3];
+ *     double pnu[nr][3], eff[nr][ns]; [double nasa9[ns][32] if flags bit 0].
+ * The meaning of each array is that of the flint_mech_desc field of the same
+ * name.  The blob's length must equal flint_ir_bytes(ns, nr, nasa9); a bad
+ * magic, version, count, flag or length returns FLINT_ERR_ARG before any
+ * array is read.  Host only, no GPU needed. */
+int flint_ir_parse(const void* blob, int64_t bytes, flint_ir_t* out);
+/* Fill *desc with pointers into the parsed IR (valid until flint_ir_free). */
+int flint_ir_desc(flint_ir_t ir, flint_mech_desc* desc);
+int flint_ir_free(flint_ir_t ir);
+/* Exact blob length for ns species, nr reactions (nasa9: 0 or 1); -1 if invalid. */
+int64_t flint_ir_bytes(int ns, int nr, int nasa9);
+/* flint_ir_parse + flint_mech_create + flint_ir_free. */
+int flint_mech_create_from_ir(const void* blob, int64_t bytes, flint_mech_t* out);
 /* Replaces free_chemistry_data (Lib_Chemistry_data.f90:168). */
 int flint_mech_destroy(flint_mech_t mech);
 /* Text of the last error on the calling thread ("" if none). */
