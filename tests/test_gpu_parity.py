@@ -6,6 +6,8 @@ accumulates); mixture cp and h to 1e-13 relative.  The reactor is compared by
 its own tolerance: both the GPU and the oracle run against a
 tighter-tolerance oracle solution.
 """
+import os
+
 import numpy as np
 import pytest
 
