@@ -158,7 +158,8 @@ typedef struct {
   double atol;            /* absolute tolerance (all components)            */
   int max_steps;          /* internal step limit per cell (bounded loop)    */
   int max_order;          /* BDF order limit, 1..5                           */
-  int constant_volume;    /* 0 = constant pressure (default), 1 = constant volume */
+  int constant_volume;    /* must be 0 (constant pressure); 1 (constant volume) is
+                             rejected with FLINT_ERR_ARG in this build         */
   int reserved;
   double tmin, tmax;      /* valid temperature range; outside -> T_OUT_OF_RANGE */
 } flint_reactor_opts;
