@@ -146,6 +146,28 @@ class Chemistry:
                                                       _hptr(J)), "flint_wdot_jac_batch_host")
         return w, J
 
+    def wdot_jac_constv(self, T, rho, Y, layout=CELL_MAJOR, wdot=None, jac=None):
+        """wdot and the constant-volume reactor Jacobian at density rho (device
+        tensors), jac[cell, col, row]."""
+        import torch
+        n, nv = T.shape[0], self.ns + 1
+        if jac is None:
+            jac = torch.empty((n, nv, nv), dtype=torch.float64, device=T.device)
+        native.check(self.L.flint_wdot_jac_constv_batch(self.h, n, layout, _dptr(T), _dptr(rho), _dptr(Y),
+                                                        _dptr(wdot), _dptr(jac), _stream()),
+                     "flint_wdot_jac_constv_batch")
+        return wdot, jac
+
+    def rhs_constv(self, T, rho, Y, f=None):
+        """Constant-volume reactor RHS (dY/dt, dT/dt) at density rho (device tensors), f (n, ns+1)."""
+        import torch
+        n = T.shape[0]
+        if f is None:
+            f = torch.empty((n, self.ns + 1), dtype=torch.float64, device=T.device)
+        native.check(self.L.flint_rhs_constv_batch(self.h, n, _dptr(T), _dptr(rho), _dptr(Y), _dptr(f), _stream()),
+                     "flint_rhs_constv_batch")
+        return f
+
     def rhs(self, T, p, Y, f=None):
         """Constant-pressure RHS (dY/dt, dT/dt), (N, ns+1)."""
         import torch
@@ -167,9 +189,10 @@ class Chemistry:
         return lay.value
 
     def reactor_advance(self, T, p, Y, dt, rtol=1e-8, atol=1e-14, max_steps=20000, max_order=5,
-                        tmin=200.0, tmax=6000.0, status=None, nsteps=None):
-        """Advance every cell over its own dt (T, Y updated in place); returns (status, nsteps)."""
-        opts = native.reactor_opts(rtol, atol, max_steps, max_order, tmin, tmax)
+                        tmin=200.0, tmax=6000.0, status=None, nsteps=None, constant_volume=False):
+        """Advance every cell over its own dt (T, Y updated in place); returns (status, nsteps).
+        constant_volume: hold each cell's initial density instead of its pressure."""
+        opts = native.reactor_opts(rtol, atol, max_steps, max_order, tmin, tmax, constant_volume)
         n = T.shape[0]
         if _is_torch(T):
             import torch

@@ -495,6 +495,32 @@ int flint_rhs_constp_batch(flint_mech_t h, int64_t n, const double* T, const dou
   return e == cudaSuccess ? FLINT_OK : cuda_fail(e, "flint_rhs_constp_batch");
 }
 
+int flint_wdot_jac_constv_batch(flint_mech_t h, int64_t n, int layout, const double* T, const double* rho,
+                                const double* Y, double* wdot, double* jac, void* stream) {
+  int rc = check_common(h, n, layout);
+  if (rc) return rc;
+  if (n == 0) return FLINT_OK;
+  if (!T || !rho || !Y || !jac) return fail(FLINT_ERR_ARG, "NULL array");
+  const int64_t need = warp_jac_scratch_doubles(h->L);
+  if (need > 0 && !h->dwscratch) {
+    cudaError_t ea = cudaMalloc(&h->dwscratch, (size_t)need * sizeof(double));
+    if (ea != cudaSuccess) { h->dwscratch = nullptr; return fail(FLINT_ERR_NOMEM, "Jacobian work area: %s", cudaGetErrorString(ea)); }
+  }
+  cudaError_t e = launch_wdot_jac(h->dimg, h->L, n, layout, T, rho, Y, wdot, jac, h->dwscratch,
+                                  (cudaStream_t)stream, 1);
+  return e == cudaSuccess ? FLINT_OK : cuda_fail(e, "flint_wdot_jac_constv_batch");
+}
+
+int flint_rhs_constv_batch(flint_mech_t h, int64_t n, const double* T, const double* rho, const double* Y, double* f,
+                           void* stream) {
+  int rc = check_common(h, n, FLINT_CELL_MAJOR);
+  if (rc) return rc;
+  if (n == 0) return FLINT_OK;
+  if (!T || !rho || !Y || !f) return fail(FLINT_ERR_ARG, "NULL array");
+  cudaError_t e = launch_rhs(h->dimg, h->L, n, T, rho, Y, f, (cudaStream_t)stream, 1);
+  return e == cudaSuccess ? FLINT_OK : cuda_fail(e, "flint_rhs_constv_batch");
+}
+
 void flint_reactor_default_opts(flint_reactor_opts* o) {
   if (!o) return;
   o->rtol = 1e-8; o->atol = 1e-14; o->max_steps = 20000; o->max_order = 5;
@@ -511,7 +537,6 @@ int flint_reactor_advance(flint_mech_t h, int64_t n, double* T, const double* p,
   if (opts) o = *opts; else flint_reactor_default_opts(&o);
   if (!(o.rtol > 0.0) || !(o.atol > 0.0) || o.max_steps < 1 || o.max_order < 1 || o.max_order > 5)
     return fail(FLINT_ERR_ARG, "reactor options out of range");
-  if (o.constant_volume) return fail(FLINT_ERR_ARG, "constant-volume reactor is not in this build");
   rc = ensure_jsave(h);
   if (rc) return rc;
   cudaError_t e = launch_reactor(h->dimg, h->L, n, T, p, Y, dt, o, status, nsteps, h->dcounter, h->djsave,
@@ -586,7 +611,6 @@ int flint_reactor_advance_noalloc(flint_mech_t h, int64_t n, double* T, const do
   if (opts) o = *opts; else flint_reactor_default_opts(&o);
   if (!(o.rtol > 0.0) || !(o.atol > 0.0) || o.max_steps < 1 || o.max_order < 1 || o.max_order > 5)
     return fail(FLINT_ERR_ARG, "reactor options out of range");
-  if (o.constant_volume) return fail(FLINT_ERR_ARG, "constant-volume reactor is not in this build");
   cudaError_t e = launch_reactor_noalloc(h->dimg, h->L, n, T, p, Y, dt, o, status, nsteps, (cudaStream_t)stream);
   return e == cudaSuccess ? FLINT_OK : cuda_fail(e, "flint_reactor_advance_noalloc");
 }
@@ -673,6 +697,8 @@ int flint_surrogate_advance(flint_surrogate_t s, int64_t n, double* T, const dou
   if (opts) o = *opts; else flint_reactor_default_opts(&o);
   if (!(o.rtol > 0.0) || !(o.atol > 0.0) || o.max_steps < 1 || o.max_order < 1 || o.max_order > 5)
     return fail(FLINT_ERR_ARG, "reactor options out of range");
+  if (o.constant_volume)
+    return fail(FLINT_ERR_ARG, "the surrogate advances at constant pressure (its projection and gate conserve enthalpy)");
   rc = ensure_jsave(s->mech);
   if (rc) return rc;
   rc = surrogate_advance(s->s, n, T, p, Y, dt, o, gate, status, nsteps, s->mech->djsave, s->mech->jslots,

@@ -320,12 +320,18 @@ __device__ inline Falloff falloff_eval(const MechView& m, int r, int type, doubl
 
 // Warp-cooperative kinetics of one cell.  Component k = lane + 32 j (slot j
 // of SPL) supplies Y_k (0 beyond ns).  Computes c, thermo, rates of progress,
-// molar production, the RHS of the constant-pressure reactor and (JAC) the
-// Jacobian rows in s.Jr:
+// molar production, the reactor RHS and (JAC) the Jacobian rows in s.Jr:
 //   s.Jr[i*ldj + j] = d f_i / d x_j,  x = (Y_0..Y_{ns-1}, T), f = (dY/dt, dT/dt).
+// cv = false: constant pressure, pr = p (rho follows from p, T, Y);
+//   dT/dt = -sum_k h_k wdot_k / (rho cp).
+// cv = true: constant volume, pr = rho (fixed); the energy equation of
+//   rhs_native (Lib_Chemistry_rhs.f90:43-50), dT/dt = -sum_k u_k wdot_k /
+//   (rho cv) with u_k = h_k - R T and cv = cp - R per mole, and c depends on Y
+//   only (dc_k/dY_k = rho/W_k, dc/dT = 0).  The flag is warp-uniform.
 template <bool JAC, int SPL>
 __device__ void warp_kinetics(const MechView& m, const WarpScratch& s, int lane, const double (&Yk)[SPL],
-                              double T, double p, CellOutT<SPL>& out) {
+                              double T, double pr, CellOutT<SPL>& out, bool cv = false) {
+  const double p = pr;
   const int ns = m.ns, nsp = m.nsp, nrpad = m.nrpad;
   const double lnT = log(T);
   const double lnC0 = m.lnpref_rth - lnT;        // ln(p_ref / (R T))
@@ -342,8 +348,8 @@ __device__ void warp_kinetics(const MechView& m, const WarpScratch& s, int lane,
   const double rr = 1.0 / (T * sumYW * p);
   const double invT = rr * sumYW * p;
   double wbar = rr * T * p;
-  const double invp = rr * T * sumYW;
-  double rho = p * m.inv_r_eos * invT * wbar;   // p / (R T sum Y/W)
+  const double invp = rr * T * sumYW;           // cv: 1 / rho
+  double rho = cv ? pr : p * m.inv_r_eos * invT * wbar;   // p / (R T sum Y/W)
   const double ctot = rho * sumYW;                 // sum_k c_k
   // species-parallel: concentrations and thermo, species k = lane + 32 j
   double my_cpR[SPL], my_hRT[SPL], my_dcpR[SPL], my_c[SPL];
@@ -541,6 +547,7 @@ __device__ void warp_kinetics(const MechView& m, const WarpScratch& s, int lane,
   }
   __syncwarp();
   // species-parallel: production rates (each lane sums its species' reaction lists)
+  const double cvone = cv ? 1.0 : 0.0;
   double wm[SPL];
   double Ql = 0.0, Dl = 0.0, cpl = 0.0, hl = 0.0;
 #pragma unroll
@@ -549,8 +556,8 @@ __device__ void warp_kinetics(const MechView& m, const WarpScratch& s, int lane,
     wm[j] = 0.0;
     if (k < ns) {
       for (int e = m.cstart[k]; e < m.cstart[k + 1]; ++e) wm[j] += m.lnu[e] * s.q[m.lr[e]];
-      Ql += my_hRT[j] * wm[j];
-      Dl += my_c[j] * my_cpR[j];
+      Ql += (my_hRT[j] - cvone) * wm[j];     // cv: u_k / RT = h_k / RT - 1
+      Dl += my_c[j] * (my_cpR[j] - cvone);   // cv: cv_k / R = cp_k / R - 1
       cpl += Yk[j] * my_cpR[j] * m.invmw[k];
       hl += Yk[j] * my_hRT[j] * m.invmw[k];
     }
@@ -559,7 +566,7 @@ __device__ void warp_kinetics(const MechView& m, const WarpScratch& s, int lane,
   const double D = warp_sum(Dl);
   const double invD = 1.0 / D;
   const double fT = -T * Q * invD;
-  const double irho = m.r_eos * T * sumYW * invp;   // 1 / rho
+  const double irho = cv ? invp : m.r_eos * T * sumYW * invp;   // 1 / rho
   out.rho = rho;
   out.fT = fT;
 #pragma unroll
@@ -618,16 +625,23 @@ __device__ void warp_kinetics(const MechView& m, const WarpScratch& s, int lane,
     Sk[j] = 0.0; HJ[j] = 0.0;
     if (k < ns) {
       const double* Jrow = s.Jr + k * ld;
-      for (int jj = 0; jj < ns; ++jj) Sk[j] += s.c[jj] * Jrow[jj];
-      for (int kk = 0; kk < ns; ++kk) HJ[j] += s.hRT[kk] * s.Jr[kk * ld + k];
-      HSl += my_hRT[j] * Sk[j];
-      dQTl += (my_cpR[j] - my_hRT[j]) * invT * wm[j] + my_hRT[j] * (JT[j] - Sk[j] * invT);
-      dDTl += my_c[j] * (my_dcpR[j] - my_cpR[j] * invT);
+      if (cv) {
+        // rho fixed: no dependence of c on T or through rho on Y (Sk = 0)
+        for (int kk = 0; kk < ns; ++kk) HJ[j] += (s.hRT[kk] - 1.0) * s.Jr[kk * ld + k];
+        dQTl += (my_cpR[j] - my_hRT[j]) * invT * wm[j] + (my_hRT[j] - 1.0) * JT[j];
+        dDTl += my_c[j] * my_dcpR[j];
+      } else {
+        for (int jj = 0; jj < ns; ++jj) Sk[j] += s.c[jj] * Jrow[jj];
+        for (int kk = 0; kk < ns; ++kk) HJ[j] += s.hRT[kk] * s.Jr[kk * ld + k];
+        HSl += my_hRT[j] * Sk[j];
+        dQTl += (my_cpR[j] - my_hRT[j]) * invT * wm[j] + my_hRT[j] * (JT[j] - Sk[j] * invT);
+        dDTl += my_c[j] * (my_dcpR[j] - my_cpR[j] * invT);
+      }
     }
   }
   const double HS = warp_sum(HSl);
   __syncwarp();
-  const double wr = wbar * irho;
+  const double wr = cv ? 0.0 : wbar * irho;
   const double dQT = warp_sum(dQTl), dDT = warp_sum(dDTl);
   const double QD = Q * invD, TD = T * invD;
   const double JTT = -QD - TD * (dQT - QD * dDT);
@@ -637,16 +651,16 @@ __device__ void warp_kinetics(const MechView& m, const WarpScratch& s, int lane,
     const int k = lane + 32 * j;
     JTm[j] = 0.0;
     if (k < ns) {
-      const double rw = rho * m.invmw[k], ww = wbar * m.invmw[k];
+      const double rw = rho * m.invmw[k], ww = cv ? 0.0 : wbar * m.invmw[k];
       const double dQ = rw * HJ[j] - ww * HS;
-      const double dD = rw * my_cpR[j] - ww * D;
+      const double dD = rw * (my_cpR[j] - cvone) - ww * D;
       JTm[j] = -TD * (dQ - QD * dD);
       // species row k in (Y, T) variables
       const double tk = Sk[j] - wm[j];
       const double Wk = m.mw[k];
       double* Jrow = s.Jr + k * ld;
       for (int jj = 0; jj < ns; ++jj) Jrow[jj] = Wk * m.invmw[jj] * (Jrow[jj] - wr * tk);
-      Jrow[ns] = (Wk * irho) * (JT[j] - tk * invT);
+      Jrow[ns] = (Wk * irho) * (cv ? JT[j] : JT[j] - tk * invT);
     }
   }
   __syncwarp();

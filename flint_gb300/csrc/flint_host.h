@@ -51,10 +51,10 @@ cudaError_t launch_chemistry_source(const uint8_t* img, const ImageLayout& L, in
                                     const double* T, double* omegadot, cudaStream_t st);
 cudaError_t launch_wdot_jac(const uint8_t* img, const ImageLayout& L, int64_t n, int layout, const double* T,
                             const double* p, const double* Y, double* wdot, double* jac, double* gscratch,
-                            cudaStream_t st);
+                            cudaStream_t st, int cv = 0);   // cv: constant volume, p holds rho
 int64_t warp_jac_scratch_doubles(const ImageLayout& L);
 cudaError_t launch_rhs(const uint8_t* img, const ImageLayout& L, int64_t n, const double* T, const double* p,
-                       const double* Y, double* f, cudaStream_t st);
+                       const double* Y, double* f, cudaStream_t st, int cv = 0);
 int reactor_slots(const ImageLayout& L);
 size_t reactor_slot_bytes(const ImageLayout& L);
 // Reactor layouts: the Newton matrix in shared memory (8 warps per block) or in

@@ -150,7 +150,7 @@ k_wdot_warp(const uint8_t* __restrict__ img, ImageLayout L, int64_t n, int layou
             const double* __restrict__ Tg, const double* __restrict__ pg,
             const double* __restrict__ Yg, double* __restrict__ wdot, double* __restrict__ cpo,
             double* __restrict__ ho, double* __restrict__ jac, double* __restrict__ rhs_out,
-            double* __restrict__ gscratch) {
+            double* __restrict__ gscratch, int cv) {
   extern __shared__ __align__(16) uint8_t smem[];
   stage_image(smem, img, L.bytes);
   MechView m;
@@ -178,7 +178,7 @@ k_wdot_warp(const uint8_t* __restrict__ img, ImageLayout L, int64_t n, int layou
       if (k < ns) Yk[j] = (layout == 1) ? Yg[(int64_t)k * n + cell] : Yg[cell * ns + k];
     }
     CellOutT<SPL> o;
-    warp_kinetics<JAC, SPL>(m, s, lane, Yk, T, p, o);
+    warp_kinetics<JAC, SPL>(m, s, lane, Yk, T, p, o, cv != 0);
 #pragma unroll
     for (int j = 0; j < SPL; ++j) {
       const int k = lane + 32 * j;
@@ -366,7 +366,7 @@ int64_t warp_jac_scratch_doubles(const ImageLayout& L) {
 template <bool JAC>
 static cudaError_t launch_warp(const uint8_t* img, const ImageLayout& L, int64_t n, int layout, const double* T,
                                const double* p, const double* Y, double* wdot, double* cp, double* h, double* jac,
-                               double* rhs, double* gscratch, cudaStream_t st) {
+                               double* rhs, double* gscratch, cudaStream_t st, int cv = 0) {
   size_t sm = warp_smem(L, JAC);
   const void* fn = warp_fn<JAC>(L);
   cudaError_t e = set_smem(fn, sm);
@@ -376,13 +376,13 @@ static cudaError_t launch_warp(const uint8_t* img, const ImageLayout& L, int64_t
   int64_t g = grid_for(fn, WARP_THREADS, sm, n * 32);
   if (L.nsp > 32)
     k_wdot_warp<JAC, 2, true><<<(unsigned)g, WARP_THREADS, sm, st>>>(img, L, n, layout, T, p, Y, wdot, cp, h, jac,
-                                                                      rhs, gscratch);
+                                                                      rhs, gscratch, cv);
   else if (gj)
     k_wdot_warp<JAC, 1, true><<<(unsigned)g, WARP_THREADS, sm, st>>>(img, L, n, layout, T, p, Y, wdot, cp, h, jac,
-                                                                      rhs, gscratch);
+                                                                      rhs, gscratch, cv);
   else
     k_wdot_warp<JAC, 1, false><<<(unsigned)g, WARP_THREADS, sm, st>>>(img, L, n, layout, T, p, Y, wdot, cp, h, jac,
-                                                                       rhs, nullptr);
+                                                                       rhs, nullptr, cv);
   count_launch();
   return cudaGetLastError();
 }
@@ -429,15 +429,15 @@ cudaError_t launch_chemistry_source(const uint8_t* img, const ImageLayout& L, in
 
 cudaError_t launch_wdot_jac(const uint8_t* img, const ImageLayout& L, int64_t n, int layout, const double* T,
                             const double* p, const double* Y, double* wdot, double* jac, double* gscratch,
-                            cudaStream_t st) {
+                            cudaStream_t st, int cv) {
   if (n <= 0) return cudaSuccess;
-  return launch_warp<true>(img, L, n, layout, T, p, Y, wdot, nullptr, nullptr, jac, nullptr, gscratch, st);
+  return launch_warp<true>(img, L, n, layout, T, p, Y, wdot, nullptr, nullptr, jac, nullptr, gscratch, st, cv);
 }
 
 cudaError_t launch_rhs(const uint8_t* img, const ImageLayout& L, int64_t n, const double* T, const double* p,
-                       const double* Y, double* f, cudaStream_t st) {
+                       const double* Y, double* f, cudaStream_t st, int cv) {
   if (n <= 0) return cudaSuccess;
-  return launch_warp<false>(img, L, n, 0, T, p, Y, nullptr, nullptr, nullptr, nullptr, f, nullptr, st);
+  return launch_warp<false>(img, L, n, 0, T, p, Y, nullptr, nullptr, nullptr, nullptr, f, nullptr, st, cv);
 }
 
 }  // namespace flint

@@ -180,8 +180,9 @@ __device__ inline void warp_lu_solve(const double* A, int ld, int nv, int lane, 
 // the Newton loop's code compact) measured 3 % slower on the 31-species
 // workload and equal on the 54-species one.
 template <int SPL>
-__device__ __forceinline__ void refresh_newton_matrix(MechView m, WarpScratch s, int lane, double p, double gamma,
-                                                   int eval_J, double ya, double yb, double* Jg, int* pivs) {
+__device__ __forceinline__ void refresh_newton_matrix(MechView m, WarpScratch s, int lane, double p, bool cv,
+                                                   double gamma, int eval_J, double ya, double yb, double* Jg,
+                                                   int* pivs) {
   constexpr int JW = 32 * SPL;
   const int ns = m.ns, nv = ns + 1, ld = s.ldj;
   const int Tslot = ns >> 5, Tlane = ns & 31;
@@ -191,7 +192,7 @@ __device__ __forceinline__ void refresh_newton_matrix(MechView m, WarpScratch s,
     yk[0] = (lane < ns) ? ya : 0.0;
     if (SPL > 1) yk[SPL - 1] = (lane + 32 < ns) ? yb : 0.0;
     CellOutT<SPL> co;
-    warp_kinetics<true, SPL>(m, s, lane, yk, Tv, p, co);
+    warp_kinetics<true, SPL>(m, s, lane, yk, Tv, p, co, cv);
 #pragma unroll
     for (int j = 0; j < SPL; ++j) {
       const int r = lane + 32 * j;
@@ -306,6 +307,17 @@ k_reactor(const uint8_t* __restrict__ img, ImageLayout L, int64_t n, double* __r
     const double T0 = Tg[cell];
     bad |= !(isfinite(T0) && isfinite(p) && p > 0.0 && isfinite(tout) && tout >= 0.0);
     bad = __any_sync(FULL, bad);
+    // constant volume: the kinetics take the density, fixed at its initial
+    // value p / (R T sum Y/W)
+    const bool cv = o.constant_volume != 0;
+    double pr = p;
+    if (cv) {
+      double yw = 0.0;
+#pragma unroll
+      for (int j = 0; j < SPL; ++j)
+        if (lane + 32 * j < ns) yw += y[j] * m.invmw[lane + 32 * j];
+      pr = p / (m.r_eos * T0 * warp_sum(yw));
+    }
     int status = FLINT_CELL_OK, nst = 0;
     if (bad) status = FLINT_CELL_NAN_INPUT;
     else if (T0 < o.tmin || T0 > o.tmax) status = FLINT_CELL_T_OUT_OF_RANGE;
@@ -336,7 +348,7 @@ k_reactor(const uint8_t* __restrict__ img, ImageLayout L, int64_t n, double* __r
         double yk[SPL];
 #pragma unroll
         for (int j = 0; j < SPL; ++j) yk[j] = (lane + 32 * j < ns) ? yv[j] : 0.0;
-        warp_kinetics<false, SPL>(m, s, lane, yk, Tv, p, co);
+        warp_kinetics<false, SPL>(m, s, lane, yk, Tv, pr, co, cv);
         __syncwarp();
 #pragma unroll
         for (int j = 0; j < SPL; ++j) fo[j] = co.f[j];
@@ -401,7 +413,7 @@ k_reactor(const uint8_t* __restrict__ img, ImageLayout L, int64_t n, double* __r
               ++n_jac;
               have_J = 1; jfresh = 1; nstJ = nst; need_J = 0;
             }
-            refresh_newton_matrix<SPL>(m, s, lane, p, gamma, eval_J, ypred[0], ypred[SPL - 1], Jg, pivs);
+            refresh_newton_matrix<SPL>(m, s, lane, pr, cv, gamma, eval_J, ypred[0], ypred[SPL - 1], Jg, pivs);
 #pragma unroll
             for (int j = 0; j < SPL; ++j) mystep[j] = pivs[32 * SPL + lane + 32 * j];
             ++n_lu;

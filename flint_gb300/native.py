@@ -53,8 +53,9 @@ class ReactorOpts(C.Structure):
                 ("tmin", C.c_double), ("tmax", C.c_double)]
 
 
-def reactor_opts(rtol=1e-8, atol=1e-14, max_steps=20000, max_order=5, tmin=200.0, tmax=6000.0):
-    return ReactorOpts(rtol, atol, max_steps, max_order, 0, 0, tmin, tmax)
+def reactor_opts(rtol=1e-8, atol=1e-14, max_steps=20000, max_order=5, tmin=200.0, tmax=6000.0,
+                 constant_volume=False):
+    return ReactorOpts(rtol, atol, max_steps, max_order, 1 if constant_volume else 0, 0, tmin, tmax)
 
 
 def ptr(a):
@@ -106,6 +107,8 @@ def lib():
     L.flint_chemistry_source_batch.argtypes = [vp, i64, vp, vp, vp, vp]
     L.flint_wdot_jac_batch.argtypes = [vp, i64, C.c_int, vp, vp, vp, vp, vp, vp]
     L.flint_rhs_constp_batch.argtypes = [vp, i64, vp, vp, vp, vp, vp]
+    L.flint_rhs_constv_batch.argtypes = [vp, i64, vp, vp, vp, vp, vp]
+    L.flint_wdot_jac_constv_batch.argtypes = [vp, i64, C.c_int, vp, vp, vp, vp, vp, vp]
     L.flint_reactor_advance.argtypes = [vp, i64, vp, vp, vp, vp, C.POINTER(ReactorOpts), vp, vp, vp]
     L.flint_reactor_autotune.argtypes = [vp, i64, vp, vp, vp, vp, C.POINTER(ReactorOpts), C.POINTER(C.c_int), vp]
     L.flint_reactor_default_opts.argtypes = [C.POINTER(ReactorOpts)]

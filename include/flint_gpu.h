@@ -158,8 +158,10 @@ typedef struct {
   double atol;            /* absolute tolerance (all components)            */
   int max_steps;          /* internal step limit per cell (bounded loop)    */
   int max_order;          /* BDF order limit, 1..5                           */
-  int constant_volume;    /* must be 0 (constant pressure); 1 (constant volume) is
-                             rejected with FLINT_ERR_ARG in this build         */
+  int constant_volume;    /* 0: constant pressure (default); 1: constant volume,
+                             the density fixed at p/(R T sum Y/W) of the input
+                             state and the energy equation of rhs_native
+                             (Lib_Chemistry_rhs.f90:43-50); p is not updated */
   int reserved;
   double tmin, tmax;      /* valid temperature range; outside -> T_OUT_OF_RANGE */
 } flint_reactor_opts;
@@ -276,6 +278,17 @@ int flint_wdot_jac_batch(flint_mech_t mech, int64_t n, int layout, const double*
                          const double* p, const double* Y, double* wdot, double* jac,
                          void* stream);
 
+/* Constant-volume forms of the two calls below and above (the system of
+ * rhs_native, Lib_Chemistry_rhs.f90:15-52, from the analytic mechanism):
+ * rho [kg/m^3] per cell replaces p, dT/dt = -sum_k u_k wdot_k / (rho cv), and
+ * J = d(dY/dt, dT/dt)/d(Y, T) at fixed rho (same storage as
+ * flint_wdot_jac_batch). */
+int flint_wdot_jac_constv_batch(flint_mech_t mech, int64_t n, int layout, const double* T,
+                                const double* rho, const double* Y, double* wdot, double* jac,
+                                void* stream);
+int flint_rhs_constv_batch(flint_mech_t mech, int64_t n, const double* T, const double* rho,
+                           const double* Y, double* f, void* stream);
+
 /* Constant-pressure reactor right-hand side f = (dY/dt, dT/dt), cell-major
  * (ns+1) per cell. */
 int flint_rhs_constp_batch(flint_mech_t mech, int64_t n, const double* T, const double* p,
@@ -286,7 +299,9 @@ int flint_rhs_constp_batch(flint_mech_t mech, int64_t n, const double* T, const 
  * run_odesolver of OSlo as called at test-batchF.f90:81,105) with a batched
  * variable-order BDF / Newton integrator and dense LU of the (ns+1) system.
  * T and Y (cell-major) are updated in place; status[cell] gets FLINT_CELL_*,
- * nsteps[cell] the internal steps taken (either may be NULL). */
+ * nsteps[cell] the internal steps taken (either may be NULL).  Constant
+ * pressure by default; opts->constant_volume = 1 integrates at the cell's
+ * initial density, as run_odesolver does with rhs_native. */
 int flint_reactor_advance(flint_mech_t mech, int64_t n, double* T, const double* p,
                           double* Y, const double* dt, const flint_reactor_opts* opts,
                           int* status, int* nsteps, void* stream);

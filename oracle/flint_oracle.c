@@ -431,6 +431,96 @@ void orc_jac_cell(const flint_mech_desc* m, double T, double p, const double* Y,
   free(Jc);
 }
 
+/* Constant volume: the system rhs_native integrates (Lib_Chemistry_rhs.f90:
+ * 15-52: rho fixed, energy equation :43-50) with the analytic mechanism.
+ * c_k = rho Y_k / W_k, dY_k/dt = W_k wdot_k / rho and, per mole,
+ * dT/dt = -sum_k (h_k - R T) wdot_k / (sum_k c_k (cp_k - R)). */
+void orc_rhs_constv_cell(const flint_mech_desc* m, double T, double rho, const double* Y, double* f) {
+  int ns = m->ns;
+  double c[MAXNS], cpR[MAXNS], hRT[MAXNS], sR[MAXNS], gRT[MAXNS], wm[MAXNS], wabs[MAXNS];
+  for (int k = 0; k < ns; ++k) c[k] = rho * Y[k] / m->mw[k];
+  orc_species_thermo(m, T, cpR, hRT, sR, NULL);
+  for (int k = 0; k < ns; ++k) gRT[k] = hRT[k] - sR[k];
+  kinetics(m, T, c, hRT, gRT, wm, wabs, NULL, NULL, NULL, NULL);
+  double Q = 0.0, D = 0.0;
+  for (int k = 0; k < ns; ++k) {
+    f[k] = m->mw[k] * wm[k] / rho;
+    Q += (hRT[k] - 1.0) * wm[k];
+    D += c[k] * (cpR[k] - 1.0);
+  }
+  f[ns] = -T * Q / D;
+}
+
+/* d(dY/dt, dT/dt)/d(Y, T) at fixed rho (column-major per cell like
+ * orc_jac_cell; Js the same chain rule on term magnitudes). */
+void orc_jac_constv_cell(const flint_mech_desc* m, double T, double rho, const double* Y,
+                         double* f, double* J, double* Js) {
+  int ns = m->ns, n = ns + 1;
+  double c[MAXNS], cpR[MAXNS], hRT[MAXNS], sR[MAXNS], gRT[MAXNS], dcpR[MAXNS];
+  double wm[MAXNS], wabs[MAXNS], JT[MAXNS], JTa[MAXNS];
+  double* Jc = (double*)malloc(sizeof(double) * ns * ns * 2);
+  double* Jca = Jc + ns * ns;
+  for (int k = 0; k < ns; ++k) c[k] = rho * Y[k] / m->mw[k];
+  orc_species_thermo(m, T, cpR, hRT, sR, dcpR);
+  for (int k = 0; k < ns; ++k) gRT[k] = hRT[k] - sR[k];
+  kinetics(m, T, c, hRT, gRT, wm, wabs, Jc, Jca, JT, JTa);
+  double Q = 0.0, Qa = 0.0, D = 0.0;
+  for (int k = 0; k < ns; ++k) {
+    Q += (hRT[k] - 1.0) * wm[k];
+    Qa += fabs(hRT[k] - 1.0) * wabs[k];
+    D += c[k] * (cpR[k] - 1.0);
+  }
+  for (int k = 0; k < ns; ++k) f[k] = m->mw[k] * wm[k] / rho;
+  f[ns] = -T * Q / D;
+  /* species rows: dc_j/dY_mm = rho/W_mm delta_j,mm, dc/dT = 0 */
+  for (int k = 0; k < ns; ++k) {
+    for (int mm = 0; mm < ns; ++mm) {
+      double ratio = m->mw[k] / m->mw[mm];
+      J[mm * n + k] = ratio * Jc[mm * ns + k];
+      if (Js) Js[mm * n + k] = ratio * Jca[mm * ns + k];
+    }
+    J[ns * n + k] = (m->mw[k] / rho) * JT[k];
+    if (Js) Js[ns * n + k] = (m->mw[k] / rho) * JTa[k];
+  }
+  /* temperature row */
+  for (int mm = 0; mm < ns; ++mm) {
+    double HJ = 0.0, HJa = 0.0;
+    for (int k = 0; k < ns; ++k) {
+      HJ += (hRT[k] - 1.0) * Jc[mm * ns + k];
+      HJa += fabs(hRT[k] - 1.0) * Jca[mm * ns + k];
+    }
+    double rw = rho / m->mw[mm];
+    double dQ = rw * HJ, dQa = rw * HJa;
+    double dD = rw * (cpR[mm] - 1.0), dDa = rw * fabs(cpR[mm] - 1.0);
+    J[mm * n + ns] = -(T / D) * (dQ - (Q / D) * dD);
+    if (Js) Js[mm * n + ns] = (T / fabs(D)) * (dQa + (Qa / fabs(D)) * dDa);
+  }
+  {
+    double dQT = 0.0, dQTa = 0.0, dDT = 0.0, dDTa = 0.0;
+    for (int k = 0; k < ns; ++k) {
+      dQT += (cpR[k] - hRT[k]) / T * wm[k] + (hRT[k] - 1.0) * JT[k];
+      dQTa += fabs((cpR[k] - hRT[k]) / T) * wabs[k] + fabs(hRT[k] - 1.0) * JTa[k];
+      dDT += c[k] * dcpR[k];
+      dDTa += fabs(c[k]) * fabs(dcpR[k]);
+    }
+    J[ns * n + ns] = -Q / D - (T / D) * (dQT - (Q / D) * dDT);
+    if (Js) Js[ns * n + ns] = Qa / fabs(D) + (T / fabs(D)) * (dQTa + (Qa / fabs(D)) * dDTa);
+  }
+  free(Jc);
+}
+
+void orc_jac_constv_batch(const flint_mech_desc* m, int64_t n, const double* T, const double* rho,
+                          const double* Y, double* f, double* jac, double* jscale, int nthreads) {
+  int ns = m->ns, nv = ns + 1, nn = nv * nv;
+  set_threads(nthreads);
+#pragma omp parallel for schedule(static)
+  for (int64_t i = 0; i < n; ++i) {
+    double fl[MAXNS + 1];
+    orc_jac_constv_cell(m, T[i], rho[i], Y + i * ns, fl, jac + i * nn, jscale ? jscale + i * nn : NULL);
+    if (f) for (int k = 0; k < nv; ++k) f[i * nv + k] = fl[k];
+  }
+}
+
 /* ------------------------------------------------------------------ batches */
 static void gather_Y(int64_t i, int64_t n, int ns, int layout, const double* Y, double* y) {
   for (int k = 0; k < ns; ++k) y[k] = (layout == FLINT_SPECIES_MAJOR) ? Y[(int64_t)k * n + i] : Y[i * ns + k];
@@ -528,17 +618,20 @@ static void lu_solve(int n, const double* a, const int* piv, double* b) {
   }
 }
 
+/* p: pressure (constant pressure) or density (constv: constant volume) */
 typedef struct { const flint_mech_desc* m; double p; int constv; } rhs_ctx;
 
 static void rhs_y(const rhs_ctx* cx, const double* y, double* f) {
   int ns = cx->m->ns;
-  orc_rhs_constp_cell(cx->m, y[ns], cx->p, y, f);
+  if (cx->constv) orc_rhs_constv_cell(cx->m, y[ns], cx->p, y, f);
+  else orc_rhs_constp_cell(cx->m, y[ns], cx->p, y, f);
 }
 
 static void jac_y(const rhs_ctx* cx, const double* y, double* J) {
   int ns = cx->m->ns;
   double f[MAXNS + 1];
-  orc_jac_cell(cx->m, y[ns], cx->p, y, f, J, NULL);
+  if (cx->constv) orc_jac_constv_cell(cx->m, y[ns], cx->p, y, f, J, NULL);
+  else orc_jac_cell(cx->m, y[ns], cx->p, y, f, J, NULL);
 }
 
 /* One cell of the reactor.  Returns the FLINT_CELL_* status.  The step-size
@@ -768,7 +861,13 @@ void orc_reactor_advance(const flint_mech_desc* m, int64_t n, double* T, const d
     else if (T[i] < o->tmin || T[i] > o->tmax) st = FLINT_CELL_T_OUT_OF_RANGE;
     else if (dt[i] == 0.0) st = FLINT_CELL_OK;
     else {
-      rhs_ctx cx = {m, p[i], o->constant_volume};
+      double pr = p[i];
+      if (o->constant_volume) {   /* density fixed at its initial value */
+        double sumYW = 0.0;
+        for (int k = 0; k < ns; ++k) sumYW += y[k] / m->mw[k];
+        pr = p[i] / (m->r_eos * T[i] * sumYW);
+      }
+      rhs_ctx cx = {m, pr, o->constant_volume};
       st = reactor_cell(&cx, ns + 1, y, dt[i], o, &nst);
       for (int k = 0; k < ns; ++k) Y[i * ns + k] = y[k];
       T[i] = y[ns];

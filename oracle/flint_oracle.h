@@ -56,6 +56,12 @@ void orc_wdot_jac_batch(const flint_mech_desc* m, int64_t n, int layout, const d
 /* Batched constant-pressure reactor advance: the same variable-order
  * fixed-leading-coefficient BDF / Newton algorithm the GPU runs, with a dense
  * partial-pivoting LU.  T, Y (cell-major) updated in place. */
+/* Constant-volume RHS and Jacobian (rho fixed; rhs_native's system). */
+void orc_rhs_constv_cell(const flint_mech_desc* m, double T, double rho, const double* Y, double* f);
+void orc_jac_constv_cell(const flint_mech_desc* m, double T, double rho, const double* Y,
+                         double* f, double* J, double* Js);
+void orc_jac_constv_batch(const flint_mech_desc* m, int64_t n, const double* T, const double* rho,
+                          const double* Y, double* f, double* jac, double* jscale, int nthreads);
 void orc_reactor_advance(const flint_mech_desc* m, int64_t n, double* T, const double* p,
                          double* Y, const double* dt, const flint_reactor_opts* o,
                          int* status, int* nsteps, int nthreads);

@@ -36,6 +36,9 @@ def lib():
         L.orc_wdot_cell.argtypes = [md, C.c_double, C.c_double, vp, vp, vp, vp, vp]
         L.orc_rhs_constp_cell.argtypes = [md, C.c_double, C.c_double, vp, vp]
         L.orc_jac_cell.argtypes = [md, C.c_double, C.c_double, vp, vp, vp, vp]
+        L.orc_rhs_constv_cell.argtypes = [md, C.c_double, C.c_double, vp, vp]
+        L.orc_jac_constv_cell.argtypes = [md, C.c_double, C.c_double, vp, vp, vp, vp]
+        L.orc_jac_constv_batch.argtypes = [md, i64, vp, vp, vp, vp, vp, vp, C.c_int]
         L.orc_wdot_batch.argtypes = [md, i64, C.c_int, vp, vp, vp, vp, vp, vp, vp, C.c_int]
         L.orc_wdot_jac_batch.argtypes = [md, i64, C.c_int, vp, vp, vp, vp, vp, vp, C.c_int]
         L.orc_reactor_advance.argtypes = [md, i64, vp, vp, vp, vp, C.POINTER(ReactorOpts), vp, vp, C.c_int]
@@ -86,6 +89,30 @@ class Oracle:
         Y = np.ascontiguousarray(Y, dtype=np.float64)
         self.L.orc_jac_cell(C.byref(self.desc), float(T), float(p), _vp(Y), _vp(f), _vp(J), _vp(Js))
         return f, J.reshape(n, n).T.copy(), Js.reshape(n, n).T.copy()  # J[row, col]
+
+    def rhs_constv(self, T, rho, Y):
+        """Constant-volume RHS (dY/dt, dT/dt) of one cell at density rho."""
+        f = np.zeros(self.ns + 1)
+        Y = np.ascontiguousarray(Y, dtype=np.float64)
+        self.L.orc_rhs_constv_cell(C.byref(self.desc), float(T), float(rho), _vp(Y), _vp(f))
+        return f
+
+    def jac_constv(self, T, rho, Y):
+        n = self.ns + 1
+        f = np.zeros(n); J = np.zeros(n * n); Js = np.zeros(n * n)
+        Y = np.ascontiguousarray(Y, dtype=np.float64)
+        self.L.orc_jac_constv_cell(C.byref(self.desc), float(T), float(rho), _vp(Y), _vp(f), _vp(J), _vp(Js))
+        return f, J.reshape(n, n).T.copy(), Js.reshape(n, n).T.copy()  # J[row, col]
+
+    def jac_constv_batch(self, T, rho, Y, nthreads=0):
+        """(f (n, ns+1), J, Js) at constant volume; J, Js flat, per cell column-major."""
+        T = np.ascontiguousarray(T, dtype=np.float64); rho = np.ascontiguousarray(rho, dtype=np.float64)
+        Y = np.ascontiguousarray(Y, dtype=np.float64)
+        n, nv = T.shape[0], self.ns + 1
+        f = np.zeros(n * nv); J = np.zeros(n * nv * nv); Js = np.zeros(n * nv * nv)
+        self.L.orc_jac_constv_batch(C.byref(self.desc), n, _vp(T), _vp(rho), _vp(Y), _vp(f), _vp(J), _vp(Js),
+                                    nthreads)
+        return f.reshape(n, nv), J, Js
 
     def wdot_batch(self, T, p, Y, layout=0, nthreads=0):
         T = np.ascontiguousarray(T, dtype=np.float64); p = np.ascontiguousarray(p, dtype=np.float64)

@@ -399,3 +399,82 @@ def test_handle_from_ir_blob_matches_descriptor(name):
     torch.cuda.synchronize()
     for x, y in zip(*outs):
         assert torch.equal(x, y)
+
+
+@pytest.mark.parametrize("cfg", ["pelucchi", "c5"])
+def test_constv_rhs_and_jacobian(cfg):
+    """Constant volume (rhs_native's system with the analytic mechanism): the
+    RHS and the fixed-density Jacobian against the oracle, to 1e-12 of the
+    oracle's term scale, on one (Pelucchi: Troe, Lindemann) and two (54
+    species) species per lane."""
+    if cfg == "c5":
+        mech = mechgen.load("c5")
+    else:
+        mech = Mechanism.load(os.path.join(os.path.dirname(__file__), "golden", "mech_pelucchi.json"))
+    T, p, Y = mechgen.c2_states(1100, mech, seed=17)
+    W = np.array([s.mw for s in mech.species])
+    rho = p / (mech.r_eos * T * (Y / W).sum(1))
+    orc = Oracle(mech)
+    f_o, J_o, Js_o = orc.jac_constv_batch(T, rho, Y)
+    chem = Chemistry(mech)
+    Tt, rt, Yt = cuda(T, rho, Y)
+    f = chem.rhs_constv(Tt, rt, Yt)
+    _, J = chem.wdot_jac_constv(Tt, rt, Yt)
+    torch.cuda.synchronize()
+    nv = mech.ns + 1
+    Jg = J.cpu().numpy().ravel()
+    assert (np.abs(Jg - J_o) / (Js_o + 1e-300)).max() < RTOL_WDOT
+    # f's term scales: wscale / rho for dY/dt, T x the scale of d(dT/dt)/dT
+    # (which bounds sum |u_k wdot_k| / (rho cv)) for dT/dt
+    _, ws_o, _, _ = orc.wdot_batch(T, p, Y)
+    fsT = T * Js_o.reshape(len(T), nv, nv)[:, mech.ns, mech.ns]
+    fs = np.concatenate([ws_o.reshape(-1, mech.ns) / rho[:, None], fsT[:, None]], axis=1)
+    assert (np.abs(f.cpu().numpy() - f_o) / (fs + 1e-300)).max() < RTOL_WDOT
+    # at the density the pressure implies, dY/dt equals the constant-pressure one
+    fp = torch.empty((len(T), nv), dtype=torch.float64, device="cuda")
+    pt = cuda(p)[0]
+    assert chem.L.flint_rhs_constp_batch(chem.h, len(T), Tt.data_ptr(), pt.data_ptr(), Yt.data_ptr(),
+                                         fp.data_ptr(), None) == 0
+    torch.cuda.synchronize()
+    np.testing.assert_allclose(f.cpu().numpy()[:, :-1], fp.cpu().numpy()[:, :-1], rtol=1e-11,
+                               atol=1e-12 * fs[:, :-1].max())
+
+
+def test_constv_reactor_vs_oracle():
+    """opts.constant_volume = 1: the GPU reactor and the oracle's, both against
+    a tight-tolerance oracle solution, and the mixture internal energy held."""
+    mech, T, p, Y, dt = _reactor_case(256, seed=8)
+    chem = Chemistry(mech)
+    orc = Oracle(mech)
+    T_o, Y_o, st_o, ns_o = orc.reactor_advance(T, p, Y, dt, reactor_opts(constant_volume=True))
+    T_x, Y_x, st_x, _ = orc.reactor_advance(T, p, Y, dt, reactor_opts(rtol=1e-12, atol=1e-18, max_steps=400000,
+                                                                       constant_volume=True))
+    Tt, pt, Yt, dtt = cuda(T, p, Y, dt)
+    st, nst = chem.reactor_advance(Tt, pt, Yt, dtt, constant_volume=True)
+    torch.cuda.synchronize()
+    st, nst = st.cpu().numpy(), nst.cpu().numpy()
+    Tg, Yg = Tt.cpu().numpy(), Yt.cpu().numpy()
+    assert (st == 0).all() and (st_o == 0).all() and (st_x == 0).all()
+    assert abs(nst.sum() / ns_o.sum() - 1.0) < 0.05
+    for Tv, Yv in ((Tg, Yg), (T_o, Y_o)):
+        assert np.max(np.abs(Tv - T_x) / T_x) < 1e-5 and np.abs(Yv - Y_x).max() < 1e-6
+    assert np.max(np.abs(Tg - T_o) / T_o) < 1e-6 and np.max(np.abs(Yg - Y_o)) < 1e-6
+    # internal energy per kg, sum_k Y_k/W_k R T (h_k/RT - 1), before and after
+    W = np.array([s.mw for s in mech.species])
+
+    def u_mass(Tc, Yc):
+        hRT = np.zeros((len(Tc), mech.ns))
+        for k, sp in enumerate(mech.species):
+            lo = Tc < sp.tmid
+            for sel, a in ((lo, sp.low), (~lo, sp.high)):
+                t = Tc[sel]
+                hRT[sel, k] = a[0] + a[1] * t / 2 + a[2] * t ** 2 / 3 + a[3] * t ** 3 / 4 + a[4] * t ** 4 / 5 + a[5] / t
+        return (Yc / W * (hRT - 1.0)).sum(1) * mech.r_thermo * Tc
+    u0, u1 = u_mass(T, Y), u_mass(Tg, Yg)
+    scale = np.abs(u0) + mech.r_thermo * T * (Y / W).sum(1)
+    assert np.max(np.abs(u1 - u0) / scale) < 1e-6
+    # constant pressure on the same cells ends elsewhere (the option takes effect)
+    Tt2, Yt2 = cuda(T, Y)
+    chem.reactor_advance(Tt2, pt, Yt2, dtt)
+    torch.cuda.synchronize()
+    assert np.abs(Tt2.cpu().numpy() - Tg).max() > 1.0
