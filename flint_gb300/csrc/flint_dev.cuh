@@ -556,8 +556,13 @@ __device__ void warp_kinetics(const MechView& m, const WarpScratch& s, int lane,
     wm[j] = 0.0;
     if (k < ns) {
       for (int e = m.cstart[k]; e < m.cstart[k + 1]; ++e) wm[j] += m.lnu[e] * s.q[m.lr[e]];
-      Ql += (my_hRT[j] - cvone) * wm[j];     // cv: u_k / RT = h_k / RT - 1
-      Dl += my_c[j] * (my_cpR[j] - cvone);   // cv: cv_k / R = cp_k / R - 1
+      if (cv) {
+        Ql += (my_hRT[j] - 1.0) * wm[j];     // u_k / RT = h_k / RT - 1
+        Dl += my_c[j] * (my_cpR[j] - 1.0);   // cv_k / R = cp_k / R - 1
+      } else {
+        Ql += my_hRT[j] * wm[j];
+        Dl += my_c[j] * my_cpR[j];
+      }
       cpl += Yk[j] * my_cpR[j] * m.invmw[k];
       hl += Yk[j] * my_hRT[j] * m.invmw[k];
     }
