@@ -146,6 +146,16 @@ class Chemistry:
                                                       _hptr(J)), "flint_wdot_jac_batch_host")
         return w, J
 
+    def species_thermo(self, T):
+        """Species cp, h, s (at p_ref) and g = h - T s, mass units, (n, ns) each
+        (device tensors)."""
+        import torch
+        n = T.shape[0]
+        out = [torch.empty((n, self.ns), dtype=torch.float64, device=T.device) for _ in range(4)]
+        native.check(self.L.flint_species_thermo_batch(self.h, n, _dptr(T), *[_dptr(o) for o in out], _stream()),
+                     "flint_species_thermo_batch")
+        return tuple(out)
+
     def wdot_jac_constv(self, T, rho, Y, layout=CELL_MAJOR, wdot=None, jac=None):
         """wdot and the constant-volume reactor Jacobian at density rho (device
         tensors), jac[cell, col, row]."""

@@ -452,6 +452,16 @@ int flint_thermo_batch(flint_mech_t h, int64_t n, int layout, const double* T, c
   return e == cudaSuccess ? FLINT_OK : cuda_fail(e, "flint_thermo_batch");
 }
 
+int flint_species_thermo_batch(flint_mech_t h, int64_t n, const double* T, double* cp, double* hs, double* s,
+                               double* g, void* stream) {
+  int rc = check_common(h, n, FLINT_CELL_MAJOR);
+  if (rc) return rc;
+  if (n == 0 || (!cp && !hs && !s && !g)) return FLINT_OK;
+  if (!T) return fail(FLINT_ERR_ARG, "NULL array");
+  cudaError_t e = launch_species_thermo(h->dimg, h->L, n, T, cp, hs, s, g, (cudaStream_t)stream);
+  return e == cudaSuccess ? FLINT_OK : cuda_fail(e, "flint_species_thermo_batch");
+}
+
 int flint_chemistry_source_batch(flint_mech_t h, int64_t n, double* roi, const double* T, double* omegadot,
                                  void* stream) {
   if (h && h->table) {

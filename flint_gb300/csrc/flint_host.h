@@ -45,6 +45,8 @@ inline cudaError_t set_smem(const void* fn, size_t bytes) {
 
 cudaError_t launch_wdot(const uint8_t* img, const ImageLayout& L, int64_t n, int layout, const double* T,
                         const double* p, const double* Y, double* wdot, double* cp, double* h, cudaStream_t st);
+cudaError_t launch_species_thermo(const uint8_t* img, const ImageLayout& L, int64_t n, const double* T, double* cp,
+                                  double* h, double* s, double* g, cudaStream_t st);
 cudaError_t launch_thermo(const uint8_t* img, const ImageLayout& L, int64_t n, int layout, const double* T,
                           const double* Y, double* cp, double* h, cudaStream_t st);
 cudaError_t launch_chemistry_source(const uint8_t* img, const ImageLayout& L, int64_t n, double* roi,

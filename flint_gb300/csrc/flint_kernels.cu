@@ -231,6 +231,32 @@ k_thermo(const uint8_t* __restrict__ img, ImageLayout L, int64_t n, int layout, 
   }
 }
 
+// ---------------------------------------------------------------- species thermo
+// Species cp, h, s (at p_ref) and g = h - T s in mass units for N
+// temperatures (cpi, H0i, S0i of Lib_ThermoTransport.f90:40-97, :233-248, from
+// the polynomials): one thread per (cell, species), outputs cell-major (N, ns).
+__global__ void k_species_thermo(const uint8_t* __restrict__ img, ImageLayout L, int64_t n,
+                                 const double* __restrict__ Tg, double* __restrict__ cpo,
+                                 double* __restrict__ ho, double* __restrict__ so, double* __restrict__ go) {
+  extern __shared__ __align__(16) uint8_t smem[];
+  stage_image(smem, img, L.bytes);
+  MechView m;
+  m.bind(L, smem);
+  const int ns = m.ns;
+  const int64_t total = n * ns;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t cell = i / ns;
+    const int k = (int)(i - cell * ns);
+    const double T = Tg[cell], lnT = log(T), invT = 1.0 / T;
+    const SpThermo th = nasa7(m, k, T, lnT, invT);
+    const double rw = m.r_thermo * m.invmw[k];
+    if (cpo) cpo[i] = th.cpR * rw;
+    if (ho) ho[i] = th.hRT * rw * T;
+    if (so) so[i] = th.sR * rw;
+    if (go) go[i] = (th.hRT - th.sR) * rw * T;
+  }
+}
+
 // ---------------------------------------------------------------- exp self-test
 __global__ void k_exp_selftest(const uint8_t* __restrict__ img, ImageLayout L, int64_t n,
                                const double* __restrict__ x, double* __restrict__ y) {
@@ -411,6 +437,17 @@ cudaError_t launch_thermo(const uint8_t* img, const ImageLayout& L, int64_t n, i
   set_smem((const void*)k_thermo, sm);
   int64_t g = grid_for((const void*)k_thermo, SMALL_THREADS, sm, n);
   k_thermo<<<(unsigned)g, SMALL_THREADS, sm, st>>>(img, L, n, layout, T, Y, cp, h);
+  count_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t launch_species_thermo(const uint8_t* img, const ImageLayout& L, int64_t n, const double* T, double* cp,
+                                  double* h, double* s, double* g, cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  size_t sm = L.bytes;
+  set_smem((const void*)k_species_thermo, sm);
+  const int64_t blocks = grid_for((const void*)k_species_thermo, SMALL_THREADS, sm, n * L.ns);
+  k_species_thermo<<<(unsigned)blocks, SMALL_THREADS, sm, st>>>(img, L, n, T, cp, h, s, g);
   count_launch();
   return cudaGetLastError();
 }

@@ -103,6 +103,7 @@ def lib():
     L.flint_mech_destroy.argtypes = [vp]
     L.flint_mech_sizes.argtypes = [vp, _ip, _ip]
     L.flint_thermo_batch.argtypes = [vp, i64, C.c_int, vp, vp, vp, vp, vp]
+    L.flint_species_thermo_batch.argtypes = [vp, i64, vp, vp, vp, vp, vp, vp]
     L.flint_wdot_batch.argtypes = [vp, i64, C.c_int, vp, vp, vp, vp, vp, vp, vp]
     L.flint_chemistry_source_batch.argtypes = [vp, i64, vp, vp, vp, vp]
     L.flint_wdot_jac_batch.argtypes = [vp, i64, C.c_int, vp, vp, vp, vp, vp, vp]

@@ -230,6 +230,12 @@ int flint_mech_sizes(flint_mech_t mech, int* ns, int* nr);
  * Lib_ThermoTransport.f90:251-271, :40-52).  Either output may be NULL. */
 int flint_thermo_batch(flint_mech_t mech, int64_t n, int layout, const double* T,
                        const double* Y, double* cp, double* h, void* stream);
+/* Species cp [J/kg/K], h [J/kg], s at p_ref [J/kg/K] and g = h - T s [J/kg]
+ * for N temperatures (cpi, H0i, S0i of Lib_ThermoTransport.f90:40-97,
+ * :233-248, from the NASA-7 / NASA-9 polynomials), cell-major (N, ns) outputs;
+ * any output may be NULL.  Analytic handles. */
+int flint_species_thermo_batch(flint_mech_t mech, int64_t n, const double* T, double* cp,
+                               double* h, double* s, double* g, void* stream);
 
 /* ----------------------------------------------------------- source term */
 /* Net mass production rates wdot [kg/m^3/s] of N cells at (T, p, Y), plus the
