@@ -27,6 +27,17 @@ module FLINT_GPU
     type(c_ptr) :: nasa9 = c_null_ptr   ! optional NASA-9 rows (ns, 32)
   end type flint_mech_desc
 
+  ! mirror of flint_table_desc: FLINT's module arrays by c_loc, in their own layout
+  type, bind(C) :: flint_table_desc
+    integer(c_int) :: ns, nr_arrh, nr_troe, nr_lind, tmin, tmax, ti1, ti2
+    type(c_ptr) :: wm, cp_tab, h_tab, kf_tab, kb_tab
+    type(c_ptr) :: kinf_troe, k0_troe, kc_troe, fcent_troe, kinf_lind, k0_lind, kc_lind
+    type(c_ptr) :: ni1_arrh, ni2_arrh, eps_arrh, ni1_troe, ni2_troe, eps_troe
+    type(c_ptr) :: ni1_lind, ni2_lind, eps_lind
+    real(c_double) :: runiv
+    type(c_ptr) :: mi_tab = c_null_ptr, k_tab = c_null_ptr   ! optional transport tables
+  end type flint_table_desc
+
   type, bind(C) :: flint_reactor_opts
     real(c_double) :: rtol, atol
     integer(c_int) :: max_steps, max_order, constant_volume, reserved
@@ -37,6 +48,12 @@ module FLINT_GPU
     integer(c_int) function flint_mech_create(desc, mech) bind(C, name='flint_mech_create')
       import :: c_int, c_ptr, flint_mech_desc
       type(flint_mech_desc), intent(in) :: desc
+      type(c_ptr), intent(out) :: mech
+    end function
+
+    integer(c_int) function flint_mech_create_tables(desc, mech) bind(C, name='flint_mech_create_tables')
+      import :: c_int, c_ptr, flint_table_desc
+      type(flint_table_desc), intent(in) :: desc
       type(c_ptr), intent(out) :: mech
     end function
 
@@ -74,6 +91,53 @@ module FLINT_GPU
     end function
 
     ! Wilke viscosity and conductivity over ncells on device arrays (rhoi: (ns, ncells))
+    ! device arrays below (c_ptr by value); stream: a cudaStream_t or c_null_ptr
+    integer(c_int) function flint_rhs_native_batch(mech, n, Z, F, stream) &
+        bind(C, name='flint_rhs_native_batch')
+      import :: c_int, c_int64_t, c_ptr
+      type(c_ptr), value :: mech, Z, F, stream
+      integer(c_int64_t), value :: n
+    end function
+
+    integer(c_int) function flint_thermo_batch(mech, n, layout, temp, Y, cp, h, stream) &
+        bind(C, name='flint_thermo_batch')
+      import :: c_int, c_int64_t, c_ptr
+      type(c_ptr), value :: mech, temp, Y, cp, h, stream
+      integer(c_int64_t), value :: n
+      integer(c_int), value :: layout
+    end function
+
+    integer(c_int) function flint_species_thermo_batch(mech, n, temp, cp, h, s, g, stream) &
+        bind(C, name='flint_species_thermo_batch')
+      import :: c_int, c_int64_t, c_ptr
+      type(c_ptr), value :: mech, temp, cp, h, s, g, stream
+      integer(c_int64_t), value :: n
+    end function
+
+    integer(c_int) function flint_wdot_batch(mech, n, layout, temp, p, Y, wdot, cp, h, stream) &
+        bind(C, name='flint_wdot_batch')
+      import :: c_int, c_int64_t, c_ptr
+      type(c_ptr), value :: mech, temp, p, Y, wdot, cp, h, stream
+      integer(c_int64_t), value :: n
+      integer(c_int), value :: layout
+    end function
+
+    integer(c_int) function flint_wdot_jac_batch(mech, n, layout, temp, p, Y, wdot, jac, stream) &
+        bind(C, name='flint_wdot_jac_batch')
+      import :: c_int, c_int64_t, c_ptr
+      type(c_ptr), value :: mech, temp, p, Y, wdot, jac, stream
+      integer(c_int64_t), value :: n
+      integer(c_int), value :: layout
+    end function
+
+    integer(c_int) function flint_reactor_advance(mech, n, temp, p, Y, dt, opts, status, nsteps, stream) &
+        bind(C, name='flint_reactor_advance')
+      import :: c_int, c_int64_t, c_ptr, flint_reactor_opts
+      type(c_ptr), value :: mech, temp, p, Y, dt, status, nsteps, stream
+      integer(c_int64_t), value :: n
+      type(flint_reactor_opts), intent(in) :: opts
+    end function
+
     integer(c_int) function flint_transport_batch(mech, n, rhoi, temp, mu, lambda, stream) &
         bind(C, name='flint_transport_batch')
       import :: c_int, c_int64_t, c_ptr
