@@ -46,3 +46,40 @@ def test_error_reporting_without_gpu():
     rc = L.flint_mech_create(None, None)
     assert rc == 1
     assert b"NULL" in L.flint_last_error()
+
+
+def _c_struct_fields(name):
+    txt = open(os.path.join(REPO, "include", "flint_gpu.h")).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    body = re.search(r"typedef struct \{([^}]*)\}\s*" + name + r";", txt, flags=re.S).group(1)
+    names = []
+    for decl in body.split(";"):
+        decl = decl.strip()
+        if not decl:
+            continue
+        kind = "ptr" if "*" in decl else ("double" if "double" in decl else "int")
+        first, *rest = decl.split(",")
+        names.append((re.findall(r"[A-Za-z_]\w*", first)[-1], kind))
+        names += [(r.strip(), kind) for r in rest]
+    return names
+
+
+def _f90_type_fields(name):
+    f90 = open(os.path.join(REPO, "include", "flint_gpu.f90")).read()
+    body = re.search(r"type, bind\(C\) :: " + name + r"\n(.*?)end type " + name, f90, flags=re.S).group(1)
+    names = []
+    for ln in body.splitlines():
+        ln = ln.split("!")[0]
+        if "::" in ln:
+            decl, vars_ = ln.split("::")
+            kind = "ptr" if "c_ptr" in decl else ("double" if "c_double" in decl else "int")
+            names += [(re.sub(r"=.*", "", v).strip(), kind) for v in vars_.split(",")]
+    return [n for n in names if n[0]]
+
+
+def test_fortran_mirrors_match_c_structs():
+    """The bind(C) derived types list the C structs' fields in the same order
+    and with the same kinds (int, double, pointer): no Fortran compiler exists
+    here to check the layout."""
+    for name in ("flint_mech_desc", "flint_table_desc", "flint_reactor_opts"):
+        assert _f90_type_fields(name) == _c_struct_fields(name), name
