@@ -67,8 +67,10 @@ class Chemistry:
 
     @classmethod
     def from_ir(cls, blob, mech: Mechanism = None):
-        """A handle from an IR blob (flint_mech_create_from_ir); `mech` only
-        labels the object (its .mech), the kernels see the blob's data."""
+        """A handle from an IR blob (flint_mech_create_from_ir).  The kernels
+        see only the blob's data; `mech` becomes .mech, which the kinetics,
+        thermo and reactor calls do not need but the surrogate's host code does
+        (species names and the element matrix are not in the blob)."""
         obj = cls.__new__(cls)
         obj.mech, obj.L = mech, native.lib()
         h = C.c_void_p()
