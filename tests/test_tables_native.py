@@ -114,3 +114,35 @@ def test_from_files_null_arguments():
     L = native.lib()
     assert L.flint_tables_read(None, None, None) == 1
     assert L.flint_mech_create_from_files(b"/nonexistent-folder", None, None) == 1
+
+
+def test_native_reader_on_reference_wd_files(tmp_path):
+    """FLINT's own WD input, rebuilt in the reference's exact text formats from
+    the committed fixtures (phase.txt and chemistry-info.txt verbatim; the rows
+    T = 999-1001 K of each chemistry-Arrhenius.dat zone as the file prints
+    them): the library's reader returns the reference's rate constants, kf at
+    1000 K = 1.798555407738E+01 and 2.851560446681E+03 for reactions 1 and 2.
+    thermo.dat is missing from the reference tree, so a flat one stands in."""
+    info = json.load(open(os.path.join(GOLD, "wd_info.json")))
+    arr = json.load(open(os.path.join(GOLD, "wd_arrhenius.json")))
+    (tmp_path / "phase.txt").write_text(
+        "ideal-gas phase\n" + "".join(f"{k} {v:.6f}\n" for k, v in info["phase"].items()))
+    (tmp_path / "chemistry-info.txt").write_text("\n".join(info["info_lines"]) + "\n")
+    lines = ['TITLE = "Arrhenius data"', 'VARIABLES = "Temperature", "kf", "kb"']
+    for z in arr["zones"]:
+        rows = [r for r in z["rows"] if 999.0 <= r[0] <= 1001.0]
+        assert [r[0] for r in rows] == [999.0, 1000.0, 1001.0]
+        lines += [f'ZONE T="{z["zone"]}"', f"I={len(rows)}, F=POINT"]
+        lines += [f"{r[0]:12.3f}   {r[1]:.12E}   {r[2]:.12E}" for r in rows]
+    (tmp_path / "chemistry-Arrhenius.dat").write_text("\n".join(lines) + "\n")
+    names = list(info["phase"])
+    T = np.array([999.0, 1000.0, 1001.0])
+    tables._write_zones(str(tmp_path / "thermo.dat"), "t", ["Temperature", "Cp", "Enthalpy", "Entropy", "dCp"],
+                        [(n, [np.full(3, 1000.0), np.zeros(3), np.ones(3), np.zeros(3)]) for n in names], T)
+    t = tables.read_folder_native(str(tmp_path))
+    assert t["ns"] == 5 and t["names"] == names and t["nr_arrh"] == 3
+    np.testing.assert_array_equal(t["wm"], list(info["phase"].values()))
+    assert (t["ti1"], t["ti2"]) == (999, 1001)
+    assert t["kf_tab"][0, 1] == 1.798555407738E+01 and t["kf_tab"][1, 1] == 2.851560446681E+03
+    assert t["ni1_arrh"][0, names.index("CH4")] == 1.0 and t["ni1_arrh"][0, names.index("O2")] == 1.5
+    _same(t, tables.read_folder(str(tmp_path)))
