@@ -146,3 +146,47 @@ def test_native_reader_on_reference_wd_files(tmp_path):
     assert t["kf_tab"][0, 1] == 1.798555407738E+01 and t["kf_tab"][1, 1] == 2.851560446681E+03
     assert t["ni1_arrh"][0, names.index("CH4")] == 1.0 and t["ni1_arrh"][0, names.index("O2")] == 1.5
     _same(t, tables.read_folder(str(tmp_path)))
+
+
+def test_native_reader_on_reference_pelucchi_files(tmp_path):
+    """The reference's Pelucchi falloff and thermo files in their exact text
+    formats (rows T = 999-1001 K of chemistry-Troe.dat, chemistry-Lindemann.dat
+    and thermo.dat from the committed fixtures, headers as the files print
+    them; phase.txt, chemistry-info.txt and the Arrhenius table written by this
+    package for the same mechanism): the library's reader returns the
+    reference's numbers, digit for digit."""
+    m = Mechanism.load(os.path.join(GOLD, "mech_pelucchi.json"))
+    tables.write_folder(tables.generate(m, 999, 1001), str(tmp_path))
+
+    def zones(fname):
+        return [(z["zone"], [r for r in z["rows"] if 999.0 <= r[0] <= 1001.0])
+                for z in json.load(open(os.path.join(GOLD, fname)))["zones"]]
+
+    def rate_file(path, title, cols, zs):
+        out = [f'TITLE = "{title}"', "VARIABLES = " + ", ".join(f'"{c}"' for c in cols)]
+        for name, rows in zs:
+            out += [f'ZONE T="{name}"', f"I={len(rows)}, F=POINT"]
+            out += [f"{r[0]:12.3f}" + "".join(f"{v:21.12E}" for v in r[1:]) for r in rows]
+        path.write_text("\n".join(out) + "\n")
+    troe, lind, thermo = zones("pelucchi_troe.json"), zones("pelucchi_lind.json"), zones("pelucchi_thermo.json")
+    rate_file(tmp_path / "chemistry-Troe.dat", "Fall-off Troe data",
+              ["Temperature", "k_inf", "k_0", "k_c", "F_cent"], troe)
+    rate_file(tmp_path / "chemistry-Lindemann.dat", "Fall-off Lindemann data",
+              ["Temperature", "k_inf", "k_0", "k_c"], lind)
+    out = ['TITLE = "Mass Thermodynamic Properties"',
+           'VARIABLES = "Temperature", "Cp", "Enthalpy", "Entropy", "dCp"']
+    for name, rows in thermo:
+        out += [f'ZONE T="{name}"', f"I={len(rows)}, F=POINT"]
+        out += [f"{r[0]:.1f} " + " ".join(f"{v:.6f}" for v in r[1:]) for r in rows]
+    (tmp_path / "thermo.dat").write_text("\n".join(out) + "\n")
+    t = tables.read_folder_native(str(tmp_path))
+    assert (t["nr_troe"], t["nr_lind"], t["tmin"], t["tmax"]) == (2, 4, 999, 1001)
+    for j, (_, rows) in enumerate(troe):
+        for c, key in enumerate(("kinf_troe", "k0_troe", "kc_troe", "fcent_troe")):
+            assert list(t[key][j]) == [r[1 + c] for r in rows], key
+    for j, (_, rows) in enumerate(lind):
+        for c, key in enumerate(("kinf_lind", "k0_lind", "kc_lind")):
+            assert list(t[key][j]) == [r[1 + c] for r in rows], key
+    for k, (_, rows) in enumerate(thermo):
+        assert list(t["cp_tab"][k]) == [r[1] for r in rows] and list(t["h_tab"][k]) == [r[2] for r in rows]
+    _same(t, tables.read_folder(str(tmp_path)))
