@@ -84,7 +84,7 @@ typedef struct flint_table_set_s* flint_table_set_t;
 /* A parsed mechanism IR blob (flint_ir_parse). */
 typedef struct flint_ir_s* flint_ir_t;
 
-/* Analytic mechanism description: NASA-7 thermo + Arrhenius / third-body /
+/* Analytic mechanism description: NASA-7 (or NASA-9) thermo + Arrhenius / third-body /
  * falloff kinetics with reverse rates from Kc (Gibbs).  All arrays are host
  * memory, row-major, read once by flint_mech_create. */
 typedef struct {
@@ -104,7 +104,7 @@ typedef struct {
   const double* pnu;      /* [nr][3] product stoichiometric coefficients     */
   const double* eff;      /* [nr][ns] third-body efficiencies (types 1-3)    */
   double r_eos;           /* gas constant of the EOS and energy equation (FLINT Runiv 8314.51) */
-  double r_thermo;        /* gas constant of NASA-7 -> cp,h,s and Kc (8314.46261815324) */
+  double r_thermo;        /* gas constant of the polynomials -> cp,h,s and Kc (8314.46261815324) */
   double p_ref;           /* standard pressure of Kc, Pa (101325)            */
   /* optional NASA-9 thermo (NULL: nasa7 serves): [ns][32] = nranges (1-3),
    * T0..T3 (range i is [T_i, T_i+1]; unused +inf), 3 x (a1..a7, b1, b2);
@@ -226,7 +226,7 @@ const char* flint_version(void);
 int flint_mech_sizes(flint_mech_t mech, int* ns, int* nr);
 
 /* -------------------------------------------------------------- thermo */
-/* Mixture cp [J/kg/K] and h [J/kg] for N cells (NASA-7, f_cp / H of
+/* Mixture cp [J/kg/K] and h [J/kg] for N cells (NASA-7 / NASA-9, f_cp / H of
  * Lib_ThermoTransport.f90:251-271, :40-52).  Either output may be NULL. */
 int flint_thermo_batch(flint_mech_t mech, int64_t n, int layout, const double* T,
                        const double* Y, double* cp, double* h, void* stream);
