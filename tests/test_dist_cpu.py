@@ -135,3 +135,36 @@ def test_rebalance_three_gloo_ranks(tmp_path):
     for r, (a, b) in enumerate(new):
         np.testing.assert_array_equal(np.load(tmp_path / f"T{r}.npy"), Tg[a:b])
         np.testing.assert_array_equal(np.load(tmp_path / f"Y{r}.npy"), Yg[a:b])
+
+
+def _rebalance_empty_main(rank, world, port, out_dir):
+    import torch
+    import torch.distributed as dist
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), RANK=str(rank), WORLD_SIZE=str(world))
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    from flint_gb300 import dist as fd
+    lens = [0, 30]                           # rank 0 starts with no cells
+    start = sum(lens[:rank])
+    cost = np.ones(30)
+    cost[0] = 1000.0                         # one cell outweighs the rest together
+    x = torch.arange(60, dtype=torch.float64).reshape(30, 2)[start:start + lens[rank]]
+    old, new = fd.rebalance_plan(cost[start:start + lens[rank]])
+    y = fd.redistribute(x, old, new)
+    np.save(os.path.join(out_dir, f"plan{rank}.npy"), np.array([old, new]))
+    np.save(os.path.join(out_dir, f"x{rank}.npy"), y.numpy())
+    dist.destroy_process_group()
+
+
+def test_rebalance_with_an_empty_rank(tmp_path):
+    """A rank that holds no cells takes part in the plan and the exchange; the
+    one expensive cell ends up alone on a rank."""
+    import torch.multiprocessing as mp
+    world = 2
+    mp.start_processes(_rebalance_empty_main, args=(world, _free_port(), str(tmp_path)), nprocs=world,
+                       start_method="spawn")
+    old, new = np.load(tmp_path / "plan0.npy")
+    assert np.array_equal(old, np.load(tmp_path / "plan1.npy")[0])
+    assert [tuple(r) for r in old] == [(0, 0), (0, 30)] and [tuple(r) for r in new] == [(0, 1), (1, 30)]
+    xg = np.arange(60, dtype=np.float64).reshape(30, 2)
+    for r, (a, b) in enumerate(new):
+        np.testing.assert_array_equal(np.load(tmp_path / f"x{r}.npy"), xg[a:b])
