@@ -15,20 +15,29 @@ from flint_gb300.native import MechDesc, ReactorOpts, TableDesc, mech_desc, ptr
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 SO = os.path.join(HERE, "_build", "liboracle.so")
+SO_NATIVE = os.path.join(HERE, "_build", "liboracle_native.so")
 
-_lib = None
+_libs = {}
 
 
 def build():
     subprocess.run(["make", "-s", "-C", HERE], check=True)
 
 
-def lib():
-    global _lib
-    if _lib is None:
-        if not os.path.exists(SO) or os.path.getmtime(SO) < os.path.getmtime(os.path.join(HERE, "flint_oracle.c")):
+def native_flags():
+    """The CPU-tuning flag of the timed baseline build (-mcpu=native / -march=native)."""
+    r = subprocess.run(["make", "-s", "-C", HERE, "native-flags"], capture_output=True, text=True)
+    return r.stdout.strip()
+
+
+def lib(native=False):
+    """The portable oracle (the checker), or with native=True the same source
+    built for the host CPU (the timed CPU baseline)."""
+    if native not in _libs:
+        so = SO_NATIVE if native else SO
+        if not os.path.exists(so) or os.path.getmtime(so) < os.path.getmtime(os.path.join(HERE, "flint_oracle.c")):
             build()
-        L = C.CDLL(SO)
+        L = C.CDLL(so)
         dp, vp, i64 = C.POINTER(C.c_double), C.c_void_p, C.c_int64
         md = C.POINTER(MechDesc)
         L.orc_species_thermo.argtypes = [md, C.c_double, vp, vp, vp, vp]
@@ -48,8 +57,8 @@ def lib():
         L.orc_rhs_native_batch.argtypes = [td, i64, vp, vp, C.c_int]
         L.orc_cons2prim_batch.argtypes = [td, i64, C.c_int, vp, vp, vp, vp, C.c_int]
         L.orc_transport_batch.argtypes = [td, i64, vp, vp, vp, vp, C.c_int]
-        _lib = L
-    return _lib
+        _libs[native] = L
+    return _libs[native]
 
 
 def _vp(a):
@@ -59,11 +68,11 @@ def _vp(a):
 class Oracle:
     """Oracle bound to one mechanism."""
 
-    def __init__(self, mech):
+    def __init__(self, mech, native=False):
         self.mech = mech
         self.desc, self._keep = mech_desc(mech)
         self.ns, self.nr = mech.ns, mech.nr
-        self.L = lib()
+        self.L = lib(native)
 
     def species_thermo(self, T):
         ns = self.ns
@@ -150,12 +159,12 @@ class Oracle:
 class TableOracle:
     """Oracle of FLINT's general loop and rhs_native on a table dict."""
 
-    def __init__(self, t):
+    def __init__(self, t, native=False):
         from flint_gb300.tables import table_desc
         self.t = t
         self.desc, self._keep = table_desc(t)
         self.ns = t["ns"]
-        self.L = lib()
+        self.L = lib(native)
 
     def general(self, roi, T, nthreads=0):
         roi = np.ascontiguousarray(roi, dtype=np.float64); T = np.ascontiguousarray(T, dtype=np.float64)

@@ -2,7 +2,7 @@
 
 Run once in a container where the reference tree is mounted:
 
-    python tests/golden/make_golden.py /root/reference
+    python tests/golden/make_golden.py <path of the FLINT source tree>
 
 It writes, from the reference's own input files only (nothing is computed here
 except unit conversion of YAML rate parameters into the IR):
@@ -169,4 +169,6 @@ def main(ref):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_golden.py <path of the FLINT source tree>")
+    main(sys.argv[1])

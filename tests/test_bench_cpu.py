@@ -35,6 +35,12 @@ def test_reference_arm_json_line():
     e = d["e2e"]
     assert e["value"] == d["value"] and e["unit"] == d["unit"]
     assert e["h2d_bytes_per_step"] == 0 and e["d2h_bytes_per_step"] == 0
+    # the line reports what was timed: the sample's cells and its own time per
+    # step; the whole workload's figure is a separate, labelled projection
+    n = d["config"]["cells"]
+    assert n <= d["config"]["cells_in_workload"]
+    assert abs(d["ms_per_step"] - 1e3 * n / d["value"]) <= 1e-6 * d["ms_per_step"]
+    assert d["projected_ms_for_all_cells"] >= d["ms_per_step"]
 
 
 def test_reference_arm_nonzero_rank_is_silent():
