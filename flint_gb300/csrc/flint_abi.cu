@@ -609,8 +609,9 @@ int flint_reactor_advance_noalloc(flint_mech_t h, int64_t n, double* T, const do
                                   const flint_reactor_opts* opts, int* status, int* nsteps, void* stream) {
   int rc = check_common(h, n, FLINT_CELL_MAJOR);
   if (rc) return rc;
-  if (n == 0) return FLINT_OK;
-  if (!T || !p || !Y || !dt) return fail(FLINT_ERR_ARG, "NULL array");
+  // n == 0 is the warm-up: it advances nothing (the arrays may be NULL) and
+  // does the one-time set-up on the current device
+  if (n > 0 && (!T || !p || !Y || !dt)) return fail(FLINT_ERR_ARG, "NULL array");
   if ((int64_t)(h->L.ns + 1) * (h->L.ns + 1) > 32 * 32)
     return fail(FLINT_ERR_MECH, "flint_reactor_advance_noalloc: %d unknowns exceed the 32 x 32 Jacobian slots of its "
                                 "static scratch (%zu bytes)", h->L.ns + 1, reactor_noalloc_bytes());

@@ -623,6 +623,26 @@ int reactor_layout_candidates(const ImageLayout& L, int* out) {
   return k;
 }
 
+// The BDF coefficient table lives in __constant__ memory, one copy per device,
+// uploaded by the first launch on that device (with it current).
+static cudaError_t ensure_bdf_table() {
+  static std::mutex bdf_mu;
+  static bool bdf_ready[MAX_DEVICES] = {false};
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= MAX_DEVICES) return cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> lk(bdf_mu);
+  if (!bdf_ready[dev]) {
+    BdfL B;
+    bdf_coeffs(B);
+    e = cudaMemcpyToSymbol(c_bdf, &B, sizeof(B));
+    if (e != cudaSuccess) return e;
+    bdf_ready[dev] = true;
+  }
+  return cudaSuccess;
+}
+
 cudaError_t launch_reactor(const uint8_t* img, const ImageLayout& L, int64_t n, double* T, const double* p,
                            double* Y, const double* dt, const flint_reactor_opts& o, int* status, int* nsteps,
                            unsigned int* work_counter, double* jsave, int slots, cudaStream_t st,
@@ -643,23 +663,8 @@ cudaError_t launch_reactor(const uint8_t* img, const ImageLayout& L, int64_t n, 
   if (blocks > full) blocks = full;
   if (blocks * wpb > slots) blocks = slots / wpb;
   if (blocks < 1) return cudaErrorInvalidValue;
-  // the BDF coefficient table lives in __constant__ memory, one copy per device
-  static std::mutex bdf_mu;
-  static bool bdf_ready[MAX_DEVICES] = {false};
-  int dev = 0;
-  e = cudaGetDevice(&dev);
+  e = ensure_bdf_table();
   if (e != cudaSuccess) return e;
-  if (dev < 0 || dev >= MAX_DEVICES) return cudaErrorInvalidDevice;
-  {
-    std::lock_guard<std::mutex> lk(bdf_mu);
-    if (!bdf_ready[dev]) {
-      BdfL B;
-      bdf_coeffs(B);
-      e = cudaMemcpyToSymbol(c_bdf, &B, sizeof(B));
-      if (e != cudaSuccess) return e;
-      bdf_ready[dev] = true;
-    }
-  }
   e = cudaMemsetAsync(work_counter, 0, NCOUNTERS * sizeof(unsigned long long), st);
   if (e != cudaSuccess) return e;
   const int64_t sd = reactor_slot_doubles_of(L, layout);
@@ -687,7 +692,11 @@ cudaError_t launch_reactor(const uint8_t* img, const ImageLayout& L, int64_t n, 
 // scratch (its work-stealing and statistics counters and one saved-Jacobian
 // slot per resident warp) lives in this file-scope device array instead of
 // memory allocated by the handle.  Every GPU that loads the library holds it
-// until the process exits.
+// until the process exits.  With CUDA's lazy module loading (the default) the
+// driver gives the array device memory only when this file's module is first
+// used on a device; the n = 0 call (launch_reactor_noalloc_prepare) does that
+// and every other one-time step, so a caller makes it before its own pool
+// takes the device memory and before any stream capture.
 constexpr int NOALLOC_SLOTS = 1280;                  // saved-Jacobian slots of 32 x 32 FP64
 constexpr size_t NOALLOC_COUNTER_BYTES = 256;        // counters, zeroed by every call
 constexpr size_t NOALLOC_BYTES = NOALLOC_COUNTER_BYTES + (size_t)NOALLOC_SLOTS * JSLOT * sizeof(double);
@@ -716,13 +725,30 @@ static cudaError_t noalloc_scratch_address(void** out) {
 }
 
 size_t reactor_noalloc_bytes() { return NOALLOC_BYTES; }
+// Only the shared-memory layout keeps a warp's scratch within one 32 x 32
+// slot; the entry point always runs it (a layout chosen by
+// flint_reactor_autotune applies to flint_reactor_advance only).
 bool reactor_noalloc_fits(const ImageLayout& L) { return reactor_slot_doubles_of(L) <= JSLOT; }
 int reactor_noalloc_slots() { return NOALLOC_SLOTS; }
+
+// One-time set-up on the current device, without a launch: module load (and
+// with it the static array's device memory), the array's address, the BDF
+// table and the kernel's shared-memory attribute.
+cudaError_t launch_reactor_noalloc_prepare(const ImageLayout& L) {
+  if (!reactor_noalloc_fits(L)) return cudaErrorInvalidValue;
+  void* base = nullptr;
+  cudaError_t e = noalloc_scratch_address(&base);
+  if (e != cudaSuccess) return e;
+  e = ensure_bdf_table();
+  if (e != cudaSuccess) return e;
+  return set_smem(reactor_fn(L), reactor_smem(L));
+}
 
 cudaError_t launch_reactor_noalloc(const uint8_t* img, const ImageLayout& L, int64_t n, double* T, const double* p,
                                    double* Y, const double* dt, const flint_reactor_opts& o, int* status,
                                    int* nsteps, cudaStream_t st) {
   if (!reactor_noalloc_fits(L)) return cudaErrorInvalidValue;
+  if (n <= 0) return launch_reactor_noalloc_prepare(L);
   void* base = nullptr;
   cudaError_t e = noalloc_scratch_address(&base);
   if (e != cudaSuccess) return e;

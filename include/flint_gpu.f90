@@ -138,6 +138,18 @@ module FLINT_GPU
       type(flint_reactor_opts), intent(in) :: opts
     end function
 
+    ! flint_reactor_advance without any device allocation (scratch in a static
+    ! 10 MiB + 256 B device array, up to 31 species, one call at a time on the
+    ! GPU).  Call it once with n = 0 before the solver's pool reserves its
+    ! device memory and before any stream capture: that call does the set-up.
+    integer(c_int) function flint_reactor_advance_noalloc(mech, n, temp, p, Y, dt, opts, status, nsteps, &
+        stream) bind(C, name='flint_reactor_advance_noalloc')
+      import :: c_int, c_int64_t, c_ptr, flint_reactor_opts
+      type(c_ptr), value :: mech, temp, p, Y, dt, status, nsteps, stream
+      integer(c_int64_t), value :: n
+      type(flint_reactor_opts), intent(in) :: opts
+    end function
+
     integer(c_int) function flint_transport_batch(mech, n, rhoi, temp, mu, lambda, stream) &
         bind(C, name='flint_transport_batch')
       import :: c_int, c_int64_t, c_ptr

@@ -330,12 +330,21 @@ int flint_reactor_autotune(flint_mech_t mech, int64_t n, const double* T, const 
  * counters and one saved Jacobian per resident warp) is a static device array
  * of 1280 slots of 32 x 32 doubles plus 256 bytes of counters (10 MiB + 256 B),
  * which every GPU that loads the library holds until exit.  Mechanisms of up to
- * 31 species fit; larger ones are rejected with FLINT_ERR_MECH.  The first call
- * on a device looks the array's address up (cudaGetSymbolAddress) and uploads
- * the BDF table, so make that first call before any stream capture.  Every
- * call shares the one array and zeroes its counters: calls that overlap on the
- * GPU (two streams, two threads) race and must be serialised by the caller.
- * flint_reactor_stats does not report these calls. */
+ * 31 species fit; larger ones are rejected with FLINT_ERR_MECH.
+ * Warm-up: a call with n = 0 (the arrays may then be NULL) advances nothing
+ * and does the one-time set-up on the current device: under CUDA's default
+ * lazy module loading the array gets its device memory only then (or on the
+ * first real call); the call also looks the array's address up
+ * (cudaGetSymbolAddress), uploads the BDF table and sets the kernel's
+ * shared-memory attribute.  Make that call, with the device current, before
+ * the caller's pool reserves its device memory and before any stream capture
+ * (CUDA_MODULE_LOADING=EAGER instead makes the array resident when the library
+ * loads).  The kernel always runs the shared-memory layout, the only one whose
+ * per-warp scratch fits a slot; a layout chosen by flint_reactor_autotune
+ * applies to flint_reactor_advance only.  Every call shares the one array and
+ * zeroes its counters: calls that overlap on the GPU (two streams, two
+ * threads) race and must be serialised by the caller.  flint_reactor_stats
+ * does not report these calls. */
 int flint_reactor_advance_noalloc(flint_mech_t mech, int64_t n, double* T, const double* p,
                                   double* Y, const double* dt, const flint_reactor_opts* opts,
                                   int* status, int* nsteps, void* stream);

@@ -37,6 +37,11 @@ def test_fortran_interface_binds_declared_symbols():
     bound = set(re.findall(r"bind\(C,\s*name='(flint_[a-z0-9_]+)'\)", f90))
     assert bound, "no bind(C) interfaces"
     assert bound <= set(declared_symbols())
+    # the entry points a CFD caller's time loop needs, including the one for
+    # solvers whose memory pool forbids library allocations
+    for s in ("flint_reactor_advance", "flint_reactor_advance_noalloc", "flint_chemistry_source_batch",
+              "flint_wdot_batch", "flint_mech_destroy"):
+        assert s in bound, s
 
 
 def test_error_reporting_without_gpu():
