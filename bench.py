@@ -370,7 +370,6 @@ def run_ours(args):
 SURROGATE_CKPT = os.path.join(REPO, "flint_gb300", "data", "surrogate_c3.bin")
 SURROGATE_CKPT_C5 = os.path.join(REPO, "flint_gb300", "data", "surrogate_c5.bin")
 SUR_CELLS = 1048576
-PLAIN_SAMPLE = None   # the plain leg re-solves every cell: errors are measured over the whole workload
 
 
 def run_surrogate(args):
@@ -467,7 +466,7 @@ def run_surrogate(args):
     acc, rej = counts["c"]
     Ts, Ys, sts, nsts = Td.clone(), Yd.clone(), st.clone(), nst.clone()
     # ---- plain FP64 integrator on a sample of the same cells (timed) + errors
-    m = n if PLAIN_SAMPLE is None else min(PLAIN_SAMPLE, n)
+    m = n if args.plain_sample is None else min(args.plain_sample, n)
     Tp, Yp = Td0[:m].clone(), Yd0[:m].clone()
     stp = torch.empty(m, dtype=torch.int32, device=dev); nsp = torch.empty(m, dtype=torch.int32, device=dev)
     flush.zero_()
@@ -536,6 +535,7 @@ def run_surrogate(args):
                           "max_abs_dT_K": float(dT.max()), "max_abs_dY": float(dY.max()),
                           "max_abs_dT_accepted_K": float(dT[accm].max()) if accm.any() else 0.0,
                           "max_abs_dY_accepted": float(dY[accm].max()) if accm.any() else 0.0,
+                          "miss": miss_report(dT, dY, accm, sur),
                           "target": {"dT_K": 1.0, "dY": 1e-4}, "gate": sur.gate},
             "e2e": {"value": n * ws / t_e2e, "unit": "cell-steps/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
@@ -567,6 +567,27 @@ def run_surrogate(args):
         print(json.dumps(line))
     if ws > 1:
         torch.distributed.destroy_process_group()
+
+
+def miss_report(dT, dY, accm, sur, target_dT=1.0, target_dY=1e-4):
+    """Accepted cells of this run (unseen in training and calibration) whose
+    error against the FP64 integrator exceeds the target, or the calibration
+    margin x target, as fractions of the accepted cells; and the calibration's
+    conformal bound: with all n accepted held-out cells inside margin x target,
+    an unseen accepted cell (exchangeable with them) lies beyond the largest of
+    their errors with probability at most 1/(n + 1)."""
+    acc = int(accm.sum())
+    cal = (getattr(sur, "header", {}) or {}).get("extra", {}).get("calibration") or {}
+    margin = cal.get("margin", 0.5)
+    beyond = ((dT > target_dT) | (dY > target_dY)) & accm
+    beyond_m = ((dT > margin * target_dT) | (dY > margin * target_dY)) & accm
+    n_val_acc = int(round(cal.get("accept_frac", 0.0) * cal.get("val_cells", 0)))
+    return {"accepted_cells": acc, "beyond_target": int(beyond.sum()),
+            "miss_rate": int(beyond.sum()) / max(acc, 1),
+            "calibration_margin": margin, "beyond_margin": int(beyond_m.sum()),
+            "miss_rate_margin": int(beyond_m.sum()) / max(acc, 1),
+            "calibration_accepted_cells": n_val_acc,
+            "conformal_bound_margin": 1.0 / (n_val_acc + 1) if n_val_acc else None}
 
 
 def run_kernel_workload(args):
@@ -632,6 +653,8 @@ def run_kernel_workload(args):
         e0.record(stream); step(); e1.record(stream); e1.synchronize()
         times.append(e0.elapsed_time(e1) / 1e3)
     t = statistics.mean(times)
+    parity = None if args.no_parity else parity_sample(chem, T, p, Y, w, jac, tab,
+                                                       (roi_d, Tc_d) if tab is not None else None)
     nv = chem.ns + 1
     bytes_per_state = 8 * (2 + 2 * chem.ns) + (8 * nv * nv if jac is not None else 16)
     roof = None
@@ -650,9 +673,48 @@ def run_kernel_workload(args):
                       "ms_per_step": t * 1e3, "states": n, "steps": args.steps, "warmup": args.warmup,
                       "gpu_launches": kernel_launches() - l0,
                       "hbm_gbs_algorithmic": n * bytes_per_state / t / 1e9,
-                      "bytes_per_state": bytes_per_state, "roofline": roof,
+                      "bytes_per_state": bytes_per_state, "roofline": roof, "parity": parity,
                       "cpu_baseline": None if args.no_cpu_baseline else
                       cpu_baseline_kernels(chem.mech, T, p, Y, jac is not None, tab)}))
+
+
+PARITY_SAMPLE = 4096
+PARITY_BAR = 1e-12
+
+
+def parity_sample(chem, T, p, Y, w, jac, tab=None, table_in=None, m=PARITY_SAMPLE):
+    """The last timed step's outputs against the FP64 oracle on m states spread
+    evenly over the whole timed batch: max |GPU - oracle| / (sum of |terms|)
+    per entry for wdot (and the Jacobian), the source-term tests' bar; for the
+    tabulated general loop, relative to the cell's largest rate."""
+    from oracle.oracle import Oracle, TableOracle
+    n = T.shape[0]
+    idx = np.unique(np.linspace(0, n - 1, min(m, n)).astype(np.int64))
+    it = None
+    try:
+        import torch
+        it = torch.from_numpy(idx).to(w.device)
+    except ImportError:
+        pass
+    wg = w.index_select(0, it).cpu().numpy()
+    res = {"states": int(idx.size), "of": int(n), "bar": PARITY_BAR, "sampled": "evenly spaced over the batch"}
+    if tab is not None:
+        roi_d, Tc_d = table_in
+        ref = TableOracle(tab.t).general(roi_d.index_select(0, it).cpu().numpy(), Tc_d.index_select(0, it).cpu().numpy())
+        sc = np.abs(ref).max(axis=1, keepdims=True)
+        res["wdot_max_err"] = float((np.abs(wg - ref) / (sc + 1e-300)).max())
+        res["scale"] = "the cell's largest rate"
+    else:
+        orc = Oracle(chem.mech)
+        w_o, ws_o, _, _ = orc.wdot_batch(T[idx], p[idx], Y[idx])
+        res["wdot_max_err"] = float((np.abs(wg.ravel() - w_o) / (ws_o + 1e-300)).max())
+        res["scale"] = "sum of |terms| per entry"
+        if jac is not None:
+            _, J_o, Js_o = orc.wdot_jac_batch(T[idx], p[idx], Y[idx])
+            Jg = jac.index_select(0, it).cpu().numpy().ravel()
+            res["jac_max_err"] = float((np.abs(Jg - J_o) / (Js_o + 1e-300)).max())
+    res["pass"] = bool(res["wdot_max_err"] < PARITY_BAR and res.get("jac_max_err", 0.0) < PARITY_BAR)
+    return res
 
 
 def cpu_baseline_kernels(mech, T, p, Y, with_jac, tab=None, target_s=5.0):
@@ -702,12 +764,17 @@ def main():
                     choices=["reactor", "reactor-c5", "c1-wdot", "c2-wdot", "c2-wdotjac", "c5-wdot", "c5-wdotjac",
                              "c2-general"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-parity", action="store_true",
+                    help="source-term workloads: skip the oracle check of the timed outputs")
     ap.add_argument("--generated", action="store_true",
                     help="source-term workloads: run the per-mechanism generated kernel (ytf_cuda)")
     ap.add_argument("--ref-seconds", type=float, default=10.0)
     ap.add_argument("--path", default="auto", choices=["auto", "surrogate", "plain"],
                     help="surrogate+fallback (headline, needs the trained checkpoint) or the plain integrator")
     ap.add_argument("--checkpoint", default=SURROGATE_CKPT)
+    ap.add_argument("--plain-sample", type=int, default=None,
+                    help="surrogate path: the plain integrator re-solves (and judges) only the first N cells "
+                         "(default: every cell)")
     ap.add_argument("--no-graph", action="store_true", help="surrogate path: direct calls instead of a CUDA graph")
     args = ap.parse_args()
     if args.workload == "reactor-c5":

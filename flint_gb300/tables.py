@@ -249,18 +249,157 @@ def read_tecplot_points(path):
     return [(z, np.array(r, dtype=np.float64)) for z, r in zones]
 
 
+# ------------------------------------------------------------ SZL binary
+# Tecplot's SZL binary (.szplt), the format FLINT's loaders fall back to when
+# the ASCII file is absent (Load_Chemistry.f90:95-96,
+# Load_ThermoTransport.f90:57-60), for the ordered one-dimensional zones FLINT's
+# tables are.  Layout, as the reference's own .szplt tables hold it:
+#   bytes 0-33   the text line "#!SZPLT 105BF $Revision: ... $\r\n"
+#   bytes 34-41  byte-order mark 08 07 06 05 04 03 02 01 (little-endian)
+#   bytes 42-49  uint64 offset of the file header
+#   file header  uint16 n, n uint16 tags, n uint64 values; a value is a count
+#                or the offset of a record:
+#                0x001 zones, 0x002 variables, 0x100 zone titles, 0x200
+#                variable names (uint64 byte length, then names each ended by
+#                '\r'), 0x101 zone type per zone ('o' ordered), 0x102 offset of
+#                each zone's header (uint64 per zone), 0x107/0x108/0x109 I, J, K
+#                per zone (uint64), 0x301 value location per zone and variable
+#                (1 nodal), 0x302 data type per zone and variable (1 float32,
+#                2 float64), 0x304 zone a variable is shared from (int32,
+#                -1 none)
+#   zone header  uint16 m, m tags, m values; tag 0x600 = offset of the
+#                variables' data offsets (uint64 per variable); each variable
+#                is then I*J*K contiguous values of its data type.
+SZL_MAGIC = b"#!SZPLT 105BF $Revision: 00000 $\r\n"
+SZL_BOM = bytes([8, 7, 6, 5, 4, 3, 2, 1])
+
+
+def read_szplt(path):
+    """SZL binary file -> list of (zone title, rows (n, nvar) float64), like read_tecplot_points."""
+    import struct
+    with open(path, "rb") as f:
+        d = f.read()
+    if d[:7] != b"#!SZPLT" or len(d) < 50 or d[34:42] != SZL_BOM:
+        raise ValueError(f"{path}: not a little-endian SZL file")
+
+    def u(fmt, o, n=1):
+        sz = struct.calcsize("<" + fmt) * n
+        if o < 0 or o + sz > len(d):
+            raise ValueError(f"{path}: record at {o} runs past the end of the file")
+        return struct.unpack_from(f"<{n}{fmt}", d, o)
+
+    def tags(o):
+        (n,) = u("H", o)
+        return dict(zip(u("H", o + 2, n), u("Q", o + 2 + 2 * n, n)))
+
+    H = tags(u("Q", 42)[0])
+    for t in (0x1, 0x2, 0x100, 0x101, 0x102, 0x107, 0x108, 0x109, 0x200, 0x301, 0x302, 0x304):
+        if t not in H:
+            raise ValueError(f"{path}: file header lacks tag {t:#x}")
+    nz, nv = H[0x1], H[0x2]
+
+    def names(o, count):
+        (ln,) = u("Q", o)
+        out = d[o + 8:o + 8 + ln].decode("latin-1").split("\r")[:count]
+        if len(out) != count:
+            raise ValueError(f"{path}: {len(out)} names where {count} are expected")
+        return out
+
+    ztitle, vname = names(H[0x100], nz), names(H[0x200], nv)
+    ztype = u("B", H[0x101], nz)
+    zhead = u("Q", H[0x102], nz)
+    I, J, K = u("Q", H[0x107], nz), u("Q", H[0x108], nz), u("Q", H[0x109], nz)
+    loc, dtyp, share = u("B", H[0x301], nz * nv), u("B", H[0x302], nz * nv), u("i", H[0x304], nz * nv)
+    zones = []
+    for z in range(nz):
+        if ztype[z] != ord("o"):
+            raise ValueError(f"{path}: zone {z + 1} is not an ordered zone")
+        Z = tags(zhead[z])
+        if 0x600 not in Z:
+            raise ValueError(f"{path}: zone {z + 1} header lacks its variable offsets")
+        voff = u("Q", Z[0x600], nv)
+        cnt = I[z] * J[z] * K[z]
+        cols = []
+        for v in range(nv):
+            k = z * nv + v
+            if loc[k] != 1 or share[k] != -1 or dtyp[k] not in (1, 2):
+                raise ValueError(f"{path}: zone {z + 1} variable {vname[v]}: only unshared nodal float32/float64 "
+                                 "data is supported")
+            dt = np.dtype("<f4" if dtyp[k] == 1 else "<f8")
+            if voff[v] + cnt * dt.itemsize > len(d):
+                raise ValueError(f"{path}: zone {z + 1} variable {vname[v]} runs past the end of the file")
+            cols.append(np.frombuffer(d, dtype=dt, count=cnt, offset=voff[v]).astype(np.float64))
+        zones.append((ztitle[z], np.stack(cols, axis=1)))
+    return zones
+
+
+def write_szplt(path, title, variables, zones, dtype=np.float32):
+    """Write ordered 1-D zones [(title, rows (n, nvar))] in the layout read_szplt reads.
+
+    In float32, values are first clipped to +-1e36, the cap of the reference's
+    float32 tables (their k_c at low T), so that nothing overflows."""
+    import struct
+    nz, nv = len(zones), len(variables)
+    code = 1 if np.dtype(dtype) == np.float32 else 2
+    body = bytearray(SZL_MAGIC + SZL_BOM + bytes(8) + bytes(24))
+    zhead = []
+    for _, rows in zones:
+        rows = np.asarray(rows)
+        offs = []
+        if np.dtype(dtype) == np.float32:
+            rows = np.clip(rows, -1e36, 1e36)
+        for v in range(nv):
+            offs.append(len(body))
+            body += np.ascontiguousarray(rows[:, v], dtype=np.dtype(dtype).newbyteorder("<")).tobytes()
+        zhead.append(len(body))
+        body += struct.pack("<H", 1) + struct.pack("<H", 0x600) + struct.pack("<Q", len(body) + 12)
+        body += struct.pack(f"<{nv}Q", *offs)
+
+    def names(lst):
+        s = "".join(x + "\r" for x in lst).encode("latin-1")
+        return struct.pack("<Q", len(s)) + s
+
+    recs = {0x100: names([z for z, _ in zones]), 0x101: b"o" * nz, 0x102: struct.pack(f"<{nz}Q", *zhead),
+            0x107: struct.pack(f"<{nz}Q", *[np.asarray(r).shape[0] for _, r in zones]),
+            0x108: struct.pack(f"<{nz}Q", *[1] * nz), 0x109: struct.pack(f"<{nz}Q", *[1] * nz),
+            0x200: names(list(variables)), 0x301: b"\x01" * (nz * nv), 0x302: bytes([code]) * (nz * nv),
+            0x304: struct.pack(f"<{nz * nv}i", *[-1] * (nz * nv))}
+    vals = {0x1: nz, 0x2: nv}
+    for t, r in recs.items():
+        vals[t] = len(body)
+        body += r
+    hdr = len(body)
+    keys = sorted(vals)
+    body += struct.pack("<H", len(keys)) + struct.pack(f"<{len(keys)}H", *keys)
+    body += struct.pack(f"<{len(keys)}Q", *[vals[k] for k in keys])
+    struct.pack_into("<Q", body, 42, hdr)
+    with open(path, "wb") as f:
+        f.write(bytes(body))
+
+
+def read_table_file(folder_prefix, base):
+    """The ASCII file base.dat, else the SZL binary base.szplt (the reference's order)."""
+    if os.path.exists(folder_prefix + base + ".dat"):
+        return read_tecplot_points(folder_prefix + base + ".dat")
+    if os.path.exists(folder_prefix + base + ".szplt"):
+        return read_szplt(folder_prefix + base + ".szplt")
+    raise FileNotFoundError(f"{folder_prefix}{base}.dat / .szplt")
+
+
 def read_folder(folder, prefix=""):
     """Parse FLINT's input files into a table dict (read_idealgas_thermo + read_chemistry).
 
-    Raises FileNotFoundError where the reference prints [ERROR] and returns or
-    stops (phase.txt, thermo.dat, chemistry-Arrhenius.dat)."""
+    Each table is read from its ASCII .dat file or, when that is absent, from
+    its SZL binary .szplt (the loaders' fallback).  Raises FileNotFoundError
+    where the reference prints [ERROR] and returns or stops (phase.txt, thermo,
+    chemistry-Arrhenius)."""
     P = lambda n: os.path.join(folder, prefix + n)  # noqa: E731
     with open(P("phase.txt")) as f:
         lines = [ln for ln in f.read().splitlines()[1:] if ln.strip()]
     names = [ln.split()[0] for ln in lines]
     wm = np.array([float(ln.split()[1]) for ln in lines])
     ns = len(names)
-    th = read_tecplot_points(P("thermo.dat"))
+    th = read_table_file(P(""), "thermo")
     T0 = int(round(th[0][1][0, 0]))
     rows = th[0][1].shape[0]
     tmin, tmax = T0, T0 + rows - 1
@@ -286,17 +425,17 @@ def read_folder(folder, prefix=""):
         a = np.array(st[key]).reshape(len(st[key]), ns + 1, 3)
         t[f"ni1_{key}"], t[f"ni2_{key}"], t[f"eps_{key}"] = (np.ascontiguousarray(a[:, :, i]) for i in range(3))
         t[f"nr_{key}"] = len(st[key])
-    arr = read_tecplot_points(P("chemistry-Arrhenius.dat"))
+    arr = read_table_file(P(""), "chemistry-Arrhenius")
     ti1 = int(round(arr[0][1][0, 0]))
     t["ti1"], t["ti2"] = ti1, ti1 + arr[0][1].shape[0] - 1
     t["kf_tab"] = np.array([z[1][:, 1] for z in arr[:t["nr_arrh"]]]).reshape(t["nr_arrh"], -1)
     t["kb_tab"] = np.array([z[1][:, 2] for z in arr[:t["nr_arrh"]]]).reshape(t["nr_arrh"], -1)
     if t["nr_troe"]:
-        z = read_tecplot_points(P("chemistry-Troe.dat"))
+        z = read_table_file(P(""), "chemistry-Troe")
         for i, nm in enumerate(("kinf_troe", "k0_troe", "kc_troe", "fcent_troe")):
             t[nm] = np.array([zz[1][:, 1 + i] for zz in z[:t["nr_troe"]]])
     if t["nr_lind"]:
-        z = read_tecplot_points(P("chemistry-Lindemann.dat"))
+        z = read_table_file(P(""), "chemistry-Lindemann")
         for i, nm in enumerate(("kinf_lind", "k0_lind", "kc_lind")):
             t[nm] = np.array([zz[1][:, 1 + i] for zz in z[:t["nr_lind"]]])
     # transport.dat (read_idealgas_transport, Load_ThermoTransport.f90:129-174):

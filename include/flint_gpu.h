@@ -178,11 +178,14 @@ int flint_mech_create_tables(const flint_table_desc* desc, flint_mech_t* out);
 /* Replaces read_idealgas_thermo, read_idealgas_transport and read_chemistry
  * (Load_ThermoTransport.f90:7-95, :129-174, Load_Chemistry.f90:7-164) for
  * callers without FLINT's Fortran loaders: parses <folder>/<prefix>phase.txt,
- * thermo.dat, chemistry-info.txt, chemistry-Arrhenius.dat and, when the
- * mechanism has such reactions, chemistry-Troe.dat / chemistry-Lindemann.dat,
- * plus transport.dat when present (Tecplot ASCII POINT zones, 1-K rows; a
- * thermo table starting at 1 K gains the cloned row 0 with h = 0, as the
- * reference builds it).  Host only, no GPU needed.  A missing or malformed
+ * thermo, chemistry-info.txt, chemistry-Arrhenius and, when the mechanism has
+ * such reactions, chemistry-Troe / chemistry-Lindemann, plus transport.dat
+ * when present (1-K rows; a thermo table starting at 1 K gains the cloned row
+ * 0 with h = 0, as the reference builds it).  Each table is read as Tecplot
+ * ASCII POINT zones (.dat) or, when that file is absent, as SZL binary
+ * (.szplt, ordered zones of float32 or float64 values), the loaders' own
+ * fallback (Load_Chemistry.f90:95-96, Load_ThermoTransport.f90:57-60).
+ * Host only, no GPU needed.  A missing or malformed
  * file returns FLINT_ERR_IO with the reason in flint_last_error(), where the
  * reference prints [ERROR] and returns or stops.  prefix may be NULL. */
 int flint_tables_read(const char* folder, const char* prefix, flint_table_set_t* out);

@@ -12,6 +12,13 @@ except unit conversion of YAML rate parameters into the IR):
 * tests/golden/pelucchi_lind.json  sampled rows of test/Pelucchi/INPUT/chemistry-Lindemann.dat
 * tests/golden/pelucchi_thermo.json sampled rows of test/Pelucchi/INPUT/thermo.dat
 * tests/golden/mech_pelucchi.json  the Pelucchi YAML as a mechanism IR
+* tests/golden/*_szl.json          sampled rows of the SZL binary tables (float32 values):
+                                   Troyes chemistry-Arrhenius.szplt (kf, kb) and thermo.szplt,
+                                   TSR-Rich-31 chemistry-Troe.szplt and thermo.szplt,
+                                   TSR-GP-24 chemistry-Troe.szplt
+* tests/golden/troyes_tables_szl.npz  the whole Troyes table set (phase.txt,
+                                   chemistry-info.txt and the two .szplt tables, read by
+                                   the library's reader), rows 280-3000 K
 * tests/golden/wd_info.json        WD chemistry-info.txt stoichiometry + phase.txt
 * tests/golden/mech_<name>.json    the other in-tree mechanisms (Ecker, Smooke, TSR-CDF-13,
                                    TSR-GP-24, TSR-Rich-31, Troyes, ZK, CORIA; WD and Cross
@@ -55,6 +62,40 @@ def read_tecplot_points(path):
             elif s and cur is not None and (s[0].isdigit() or s[0] in "+-."):
                 cur[1].append([float(x) for x in s.split()])
     return [(z, np.array(r)) for z, r in zones]
+
+
+def szl_zones(path):
+    """Ordered 1-D zones of an SZL binary (.szplt) -> list of (title, rows).
+
+    A decode of its own, independent of flint_gb300.tables.read_szplt: the file
+    header's tag table (offset at byte 42) gives the zone count (tag 1), the
+    variable count (2), zone titles (0x100), zone-header offsets (0x102), the
+    I extent per zone (0x107) and the data type per zone and variable (0x302,
+    1 = float32, 2 = float64); each zone header's tag 0x600 points at the
+    offsets of its variables' contiguous value arrays."""
+    import struct
+    d = open(path, "rb").read()
+    assert d[:7] == b"#!SZPLT" and d[34:42] == bytes([8, 7, 6, 5, 4, 3, 2, 1])
+
+    def table(o):
+        n = struct.unpack_from("<H", d, o)[0]
+        return dict(zip(struct.unpack_from(f"<{n}H", d, o + 2), struct.unpack_from(f"<{n}Q", d, o + 2 + 2 * n)))
+
+    H = table(struct.unpack_from("<Q", d, 42)[0])
+    nz, nv = H[1], H[2]
+    ln = struct.unpack_from("<Q", d, H[0x100])[0]
+    titles = d[H[0x100] + 8:H[0x100] + 8 + ln].decode().split("\r")[:nz]
+    out = []
+    for z in range(nz):
+        I = struct.unpack_from("<Q", d, H[0x107] + 8 * z)[0]
+        Z = table(struct.unpack_from("<Q", d, H[0x102] + 8 * z)[0])
+        cols = []
+        for v in range(nv):
+            off = struct.unpack_from("<Q", d, Z[0x600] + 8 * v)[0]
+            dt = {1: "<f4", 2: "<f8"}[d[H[0x302] + z * nv + v]]
+            cols.append(np.frombuffer(d, dtype=dt, count=I, offset=off).astype(np.float64))
+        out.append((titles[z], np.stack(cols, axis=1)))
+    return out
 
 
 def sample_rows(rows, temps):
@@ -110,6 +151,41 @@ def main(ref):
                "info_lines": info,
                "phase": M.read_phase_txt(os.path.join(test, "WD/INPUT/phase.txt"))},
               open(os.path.join(gold, "wd_info.json"), "w"), indent=0)
+
+    # ---- SZL binary tables (Troyes, TSR-Rich-31, TSR-GP-24) --------------------
+    # sampled rows for the oracle pins, checked against the library's reader
+    from flint_gb300 import tables as TB
+    temps_s = sorted(set([float(t) for t in range(300, 3501, 89)] + [500.0, 999.0, 1000.0, 1001.0, 2500.0]))
+    szl = [("Troyes/INPUT/chemistry-Arrhenius.szplt", "troyes_arrhenius_szl", ["T", "kf", "kb"]),
+           ("Troyes/INPUT/thermo.szplt", "troyes_thermo_szl", ["T", "Cp", "Enthalpy", "Entropy", "dCp"]),
+           ("TSR-Rich-31/INPUT/chemistry-Troe.szplt", "tsr_rich_31_troe_szl", ["T", "k_inf", "k_0", "k_c", "F_cent"]),
+           ("TSR-Rich-31/INPUT/thermo.szplt", "tsr_rich_31_thermo_szl", ["T", "Cp", "Enthalpy", "Entropy", "dCp"]),
+           ("TSR-GP-24/INPUT/chemistry-Troe.szplt", "tsr_gp_24_troe_szl", ["T", "k_inf", "k_0", "k_c", "F_cent"])]
+    for rel, key, cols in szl:
+        zs = szl_zones(os.path.join(test, rel))
+        mine = TB.read_szplt(os.path.join(test, rel))
+        assert [z for z, _ in zs] == [z for z, _ in mine]
+        assert all(np.array_equal(a, b) for (_, a), (_, b) in zip(zs, mine)), rel
+        json.dump({"source": "test/" + rel + " (float32 values)", "columns": cols, "rows_per_zone": int(zs[0][1].shape[0]),
+                   "first_T": zs[0][1][0, 0],
+                   "zones": [{"zone": z, "rows": sample_rows(r, [t for t in temps_s if r[0, 0] <= t <= r[-1, 0]])}
+                             for z, r in zs]},
+                  open(os.path.join(gold, key + ".json"), "w"), indent=0)
+    # the complete Troyes table set, read from the reference's own files
+    # (phase.txt, chemistry-info.txt, chemistry-Arrhenius.szplt, thermo.szplt)
+    # by the library's reader, rows 280-3000 K, for the GPU general-loop test
+    t = TB.read_folder(os.path.join(test, "Troyes/INPUT"))
+    lo, hi = 280, 3000
+    keep = {"ns": t["ns"], "names": np.array(t["names"]), "wm": t["wm"], "tmin": lo, "tmax": hi, "ti1": lo, "ti2": hi,
+            "cp_tab": t["cp_tab"][:, lo - t["tmin"]:hi - t["tmin"] + 1].astype(np.float32),
+            "h_tab": t["h_tab"][:, lo - t["tmin"]:hi - t["tmin"] + 1].astype(np.float32),
+            "kf_tab": t["kf_tab"][:, lo - t["ti1"]:hi - t["ti1"] + 1].astype(np.float32),
+            "kb_tab": t["kb_tab"][:, lo - t["ti1"]:hi - t["ti1"] + 1].astype(np.float32),
+            "ni1_arrh": t["ni1_arrh"], "ni2_arrh": t["ni2_arrh"], "eps_arrh": t["eps_arrh"]}
+    for k in ("cp_tab", "h_tab", "kf_tab", "kb_tab"):   # float32 in the files: the cast is exact
+        src = t[k][:, lo - (t["tmin"] if k in ("cp_tab", "h_tab") else t["ti1"]):][:, :hi - lo + 1]
+        assert np.array_equal(keep[k].astype(np.float64), src), k
+    np.savez_compressed(os.path.join(gold, "troyes_tables_szl.npz"), **keep)
 
     # ---- C1 mechanism ---------------------------------------------------------
     rich = yamlsub.load(os.path.join(test, "TSR-Rich-31/INPUT/TSR-Rich-31.yaml"))

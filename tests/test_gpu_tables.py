@@ -89,3 +89,33 @@ def test_handle_from_files_matches_handle_from_arrays(tmp_path):
     assert torch.equal(a.chemistry_source(roi_t.clone(), T_t), b.chemistry_source(roi_t.clone(), T_t))
     Z = torch.cat([roi_t, T_t[:, None]], dim=1).contiguous()
     assert torch.equal(a.rhs_native(Z), b.rhs_native(Z))
+
+
+def test_general_and_rhs_native_on_the_reference_troyes_tables():
+    """FLINT's general loop and rhs_native on the Troyes tables the reference
+    ships only as SZL binaries (chemistry-Arrhenius.szplt, thermo.szplt, read by
+    the library's reader when the fixture was made; rows 280-3000 K): 17
+    elementary and three-body reactions, so bit for bit with the oracle."""
+    from test_szl import troyes_tables
+    t = troyes_tables()
+    rng = np.random.default_rng(31)
+    n = 5003
+    T = rng.uniform(300.0, 2990.0, n)
+    Y = rng.dirichlet(np.full(t["ns"], 0.4), n)
+    rho = rng.uniform(0.05, 20.0, n)
+    roi = rho[:, None] * Y
+    orc = TableOracle(t)
+    ref = orc.general(roi, T)
+    gpu = tables.Tables(t)
+    roi_t, T_t = cuda(roi, T)
+    w = gpu.chemistry_source(roi_t, T_t)
+    torch.cuda.synchronize()
+    assert np.array_equal(w.cpu().numpy(), ref)
+    # rhs_native at the bars of test_rhs_native: 1e-12 of the cell's largest
+    # species term, 1e-11 relative on dT/dt
+    Z = np.hstack([roi, T[:, None]])
+    F_ref = orc.rhs_native(Z)
+    F = gpu.rhs_native(cuda(Z)[0]).cpu().numpy()
+    scale = np.abs(F_ref[:, :-1]).max(axis=1, keepdims=True) + 1e-300
+    assert np.max(np.abs(F[:, :-1] - F_ref[:, :-1]) / scale) < 1e-12
+    np.testing.assert_allclose(F[:, -1], F_ref[:, -1], rtol=1e-11)
