@@ -83,6 +83,15 @@ class Reaction:
     collider: str = None     # explicit collider species "(+AR)"
 
 
+def _orders_custom(self):
+    """True when the reaction's forward orders differ from its reactant coefficients."""
+    return any(self.orders.get(nm, nu) != nu for nm, nu in self.reactants.items()) or \
+        any(nm not in self.reactants for nm in self.orders)
+
+
+Reaction.orders_custom = _orders_custom
+
+
 @dataclass
 class Mechanism:
     name: str
@@ -209,6 +218,68 @@ class Mechanism:
             for e, n in s.composition.items():
                 E[self.elements.index(e), k] = n
         return E
+
+    # ------------------------------------------------------------------ YTF
+    def ytf_form(self):
+        """This mechanism as FLINT's generator writes it into a Fortran routine
+        (utils/YTF.py:96-232, the Lib_ChemMech/*.f90 family), so that the
+        kernels compute what such a routine computes:
+
+        * the concentration factors of the forward and reverse rates are the
+          stoichiometric coefficients truncated to integers (stoich_to_mult,
+          YTF.py:20-27, int(n) repetitions); custom orders are not used
+          ("no custom orders are implemented", YTF.py:2); the net coefficients
+          of the species sums keep their full values (YTF.py:246-249) -- where
+          truncation changes a product's power the reverse rate differs, so
+          such mechanisms (none among the generated routines) are refused;
+        * third-body efficiencies as the routine prints them, '%.8g'
+          (format_eff, YTF.py:29-34); zero efficiencies of three-body
+          reactions are dropped (YTF.py:140), which changes no value;
+        * falloff reactions take the efficiencies listed in the YAML and 1.0
+          for every other species (efficiencies.get(sp, 1.0), YTF.py:156-158
+          and :191-193): a reaction's default efficiency is not used;
+        * an elementary termolecular reaction in which one species appears on
+          both sides ("H + 2 O2 <=> HO2 + O2", "2 H + H2 <=> 2 H2") is the
+          three-body reaction with that species as the third body, as Cantera
+          reads it for the generator: one unit of it leaves both sides and
+          becomes M (the routine's "M=coi(k)"); the rates of progress are the
+          same products.  Bimolecular ones ("CH2(S) + H2O <=> CH2 + H2O")
+          stay elementary, as in the routines.
+        """
+        import copy
+        out = copy.deepcopy(self)
+        out.name = self.name + " (YTF form)"
+        names = [sp.name for sp in self.species]
+        for r in out.reactions:
+            both = [nm for nm in r.reactants if nm in r.products]
+            termolecular = max(sum(r.reactants.values()), sum(r.products.values())) == 3.0
+            if r.rtype == TYPE_ELEMENTARY and len(both) == 1 and termolecular and not r.orders_custom():
+                x = both[0]
+                r.rtype, r.collider, r.default_eff, r.efficiencies = TYPE_THREEBODY, x, 0.0, None
+                r.reactants = {nm: (nu - 1.0 if nm == x else nu) for nm, nu in r.reactants.items()}
+                r.reactants = {nm: nu for nm, nu in r.reactants.items() if nu > 0.0}
+                r.products = {nm: (nu - 1.0 if nm == x else nu) for nm, nu in r.products.items()}
+                r.products = {nm: nu for nm, nu in r.products.items() if nu > 0.0}
+        for r in out.reactions:
+            for nm, nu in r.products.items():
+                if nu != int(nu):
+                    raise ValueError(f"{r.equation}: non-integer product coefficient {nu} "
+                                     "(the routine's reverse power would differ from Kc's)")
+            r.orders = {nm: float(int(nu)) for nm, nu in r.reactants.items() if int(nu) > 0}
+            if r.rtype == TYPE_ELEMENTARY:
+                continue
+            if r.rtype == TYPE_THREEBODY:
+                if r.collider is not None:
+                    continue
+                effs = {nm: float(f"{(r.efficiencies or {}).get(nm, r.default_eff):.8g}") for nm in names}
+            else:
+                effs = {nm: float(f"{(r.efficiencies or {}).get(nm, 1.0):.8g}") for nm in names}
+                if r.collider is not None:
+                    effs = {nm: 1.0 for nm in names}
+                r.collider = None
+            r.default_eff = 1.0
+            r.efficiencies = {nm: e for nm, e in effs.items() if e != 1.0}
+        return out
 
     # ------------------------------------------------------------------ json
     def to_json(self):

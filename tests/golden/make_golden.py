@@ -16,6 +16,10 @@ except unit conversion of YAML rate parameters into the IR):
                                    Troyes chemistry-Arrhenius.szplt (kf, kb) and thermo.szplt,
                                    TSR-Rich-31 chemistry-Troe.szplt and thermo.szplt,
                                    TSR-GP-24 chemistry-Troe.szplt
+* tests/golden/fortran_forms.json  the generated Fortran mechanism routines
+                                   (src/lib/Lib_ChemMech/*.f90) parsed into their rate
+                                   sources, concentration factors, third bodies and
+                                   omegadot terms
 * tests/golden/troyes_tables_szl.npz  the whole Troyes table set (phase.txt,
                                    chemistry-info.txt and the two .szplt tables, read by
                                    the library's reader), rows 280-3000 K
@@ -96,6 +100,78 @@ def szl_zones(path):
             cols.append(np.frombuffer(d, dtype=dt, count=I, offset=off).astype(np.float64))
         out.append((titles[z], np.stack(cols, axis=1)))
     return out
+
+
+# the generated Fortran mechanism routines (utils/YTF.py's output form) and the
+# IR fixture of the same mechanism
+FORTRAN_FORMS = [("TSR-CDF-13.f90", "mech_tsr_cdf_13.json"), ("TSR-GP-24.f90", "mech_tsr_gp_24.json"),
+                 ("TSR-Rich-31.f90", "mech_tsr_rich_31.json"), ("ZK.f90", "mech_zk.json"),
+                 ("coria.f90", "mech_coria.json"), ("cross.f90", "mech_cross.json"),
+                 ("ecker.f90", "mech_ecker.json"), ("pelucchi.f90", "mech_pelucchi.json"),
+                 ("smooke.f90", "mech_smooke.json"), ("troyes.f90", "mech_troyes.json")]
+
+
+def parse_fortran_form(path):
+    """One generated mechanism routine (src/lib/Lib_ChemMech/*.f90) as data.
+
+    Per reaction, in the routine's order: the rate source ("arrh" f_kf/f_kb
+    row a, "troe" / "lind" f_k_troe / f_k_lindemann row a, 1-based), the
+    species of each concentration factor of prodf and prodb (0-based, repeated
+    for powers), whether prodf/prodb carry the third body M, and M itself as
+    {species: efficiency} ("sum" = every species with 1); per species the
+    omegadot terms [reaction, nu_product, nu_reactant].  The concentration
+    clamp of the routine's first loop, if any, is recorded as written."""
+    import re
+    lines = open(path).read().splitlines()
+    rx, cur_M, cur_k = {}, None, None
+    omega = {}
+    clamp = None
+    for ln in lines:
+        s = ln.split("!")[0].strip().replace(" ", "")
+        if not s:
+            continue
+        if s.startswith("roi(is)=max(roi(is),0"):
+            clamp = "roi = max(roi, 0)"
+        m = re.match(r"M=(.*)$", s)
+        if m:
+            e = m.group(1)
+            if e.startswith("sum("):
+                cur_M = "sum"
+            else:
+                cur_M = {}
+                for term in e.split("+"):
+                    t = re.match(r"coi\((\d+)\)(?:\*([0-9.eEdD+-]+))?$", term)
+                    assert t, (path, term)
+                    cur_M[int(t.group(1)) - 1] = float((t.group(2) or "1").replace("d", "e").replace("D", "e"))
+            continue
+        m = re.match(r"k=f_k_(troe|lindemann)\((\d+),", s)
+        if m:
+            cur_k = ("troe" if m.group(1) == "troe" else "lind", int(m.group(2)))
+            continue
+        m = re.match(r"prod([fb])\((\d+)\)=(.*)$", s)
+        if m:
+            side, r, e = m.group(1), int(m.group(2)) - 1, m.group(3)
+            d = rx.setdefault(r, {})
+            src = re.match(r"f_k([fb])\((\d+),", e)
+            if src:
+                d["kind"], d["table_index"] = "arrh", int(src.group(2))
+            else:
+                assert e.startswith(f"k({1 if side == 'f' else 2})"), (path, e)
+                d["kind"], d["table_index"] = cur_k
+            d["fwd" if side == "f" else "bwd"] = sorted(int(x) - 1 for x in re.findall(r"coi\((\d+)\)", e))
+            d["M" + side] = e.endswith("*M")
+            if e.endswith("*M") or d["kind"] != "arrh":
+                d["M"] = cur_M
+            continue
+        m = re.match(r"omegadot\((\d+)\)=(.*)$", s)
+        if m:
+            k, e = int(m.group(1)) - 1, m.group(2)
+            omega[k] = [[int(r) - 1, float(a), float(b)] for a, b, r in
+                        re.findall(r"\(([0-9.]+)-([0-9.]+)\)\*\(prodf\((\d+)\)", e)]
+    n = max(rx) + 1
+    assert sorted(rx) == list(range(n)), path
+    return {"reactions": [rx[r] for r in range(n)], "omegadot": [omega.get(k, []) for k in range(max(omega) + 1)],
+            "clamp": clamp}
 
 
 def sample_rows(rows, temps):
@@ -186,6 +262,14 @@ def main(ref):
         src = t[k][:, lo - (t["tmin"] if k in ("cp_tab", "h_tab") else t["ti1"]):][:, :hi - lo + 1]
         assert np.array_equal(keep[k].astype(np.float64), src), k
     np.savez_compressed(os.path.join(gold, "troyes_tables_szl.npz"), **keep)
+
+    # ---- the generated Fortran mechanism routines ------------------------------
+    forms = {}
+    for fname, mname in FORTRAN_FORMS:
+        f = parse_fortran_form(os.path.join(ref, "src/lib/Lib_ChemMech", fname))
+        f.update({"source": "src/lib/Lib_ChemMech/" + fname, "mechanism": mname})
+        forms[os.path.splitext(fname)[0]] = f
+    json.dump(forms, open(os.path.join(gold, "fortran_forms.json"), "w"), indent=0)
 
     # ---- C1 mechanism ---------------------------------------------------------
     rich = yamlsub.load(os.path.join(test, "TSR-Rich-31/INPUT/TSR-Rich-31.yaml"))
