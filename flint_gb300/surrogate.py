@@ -515,7 +515,8 @@ def main():
            "loss_history": {str(k): h for k, h in hist.items()},
            "gate": sur.gate, "diagnostics": getattr(calibrate, "diag", {}),
            "calibration": None if best is None else
-           {"accept_frac": best[0], "max_dT": best[2], "max_dY": best[3]}}
+           {"accept_frac": best[0], "max_dT": best[2], "max_dY": best[3], "val_cells": int(v["T0"].shape[0]),
+            "margin": args.margin}}
     if args.save_val and getattr(calibrate, "data", None) is not None:
         np.savez_compressed(os.path.splitext(args.out)[0] + "_val.npz", **calibrate.data)
     sur.save(args.out, extra=rep)
