@@ -351,7 +351,7 @@ def run_ours(args):
                         "cells_per_gpu": n, "mechanism": "synthetic-31sp-160r (12 third-body, 6 Troe)"})
                       | {"path": "plain FP64 integrator", "l2": "flushed (256 MiB write) between timed steps",
                          "cuda_graph": graph_note,
-                         "reactor_layout": {0: "by size", 1: "shared memory", 2: "global slot, 8 warps/block", 3: "global slot, 4 warps/block"}[layout]
+                         "reactor_layout": REACTOR_LAYOUTS[layout]
                          + " (autotuned on 16,384 cells)"},
             "e2e": {"value": n * ws / e2e_t, "unit": "cell-steps/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
@@ -367,6 +367,8 @@ def run_ours(args):
         torch.distributed.destroy_process_group()
 
 
+REACTOR_LAYOUTS = {0: "by size", 1: "shared memory", 2: "global slot, 8 warps/block",
+                   3: "global slot, 4 warps/block", 4: "global slot, 2 blocks of 8 warps/SM (128 registers)"}
 SURROGATE_CKPT = os.path.join(REPO, "flint_gb300", "data", "surrogate_c3.bin")
 SURROGATE_CKPT_C5 = os.path.join(REPO, "flint_gb300", "data", "surrogate_c5.bin")
 SUR_CELLS = 1048576
@@ -527,7 +529,7 @@ def run_surrogate(args):
                        "network": (f"MLP {'-'.join(str(d) for d in sur.dims)} GELU x{sur.n_nets} (ensemble), "
                                    "split-bf16 mma.sync forward, fp32 accumulate"),
                        "l2": "flushed (256 MiB write) between timed steps", "cuda_graph": graph_note,
-                       "reactor_layout": {0: "by size", 1: "shared memory", 2: "global slot, 8 warps/block", 3: "global slot, 4 warps/block"}[layout]
+                       "reactor_layout": REACTOR_LAYOUTS[layout]
                        + " (autotuned on 16,384 cells)"},
             "surrogate": {"accepted": int(acc), "rejected": int(rej), "accept_frac": acc / max(acc + rej, 1),
                           "plain_fp64_cell_steps_per_s": plain, "plain_sample_cells": m,
@@ -600,7 +602,7 @@ def run_kernel_workload(args):
     from flint_gb300 import mechgen
     from flint_gb300.api import Chemistry, kernel_launches
     dev = torch.device("cuda", 0)
-    if args.workload == "c1-wdot":
+    if args.workload.startswith("c1-"):
         n = args.cells or 65536
         T, p, Y = mechgen.c1_states(n)
         chem = Chemistry.from_config("c1")
@@ -627,14 +629,19 @@ def run_kernel_workload(args):
         roi_d = torch.from_numpy(rho[:, None] * Y).to(dev)
         Tc_d = torch.from_numpy(Tc).to(dev)
     if args.generated:
-        if jac is not None:
-            raise SystemExit("--generated covers wdot/cp/h only")
         from flint_gb300.ytf_cuda import GeneratedMechanism
         gen = GeneratedMechanism(chem.mech)
+    tuning = None
+    if tab is None and gen is None:
+        # the source-term kernels' block size, tuned on a sample of these states (untimed)
+        ms = min(n, 65536)
+        tuning = chem.wdot_autotune(Td[:ms], pd[:ms], Yd[:ms])
 
     def step():
         if tab is not None:
             tab.chemistry_source(roi_d, Tc_d, omegadot=w)
+        elif gen is not None and jac is not None:
+            gen.wdot_jac(Td, pd, Yd, wdot=w, jac=jac)
         elif gen is not None:
             gen.wdot(Td, pd, Yd, wdot=w, cp=cp, h=h)
         elif jac is None:
@@ -659,10 +666,12 @@ def run_kernel_workload(args):
     bytes_per_state = 8 * (2 + 2 * chem.ns) + (8 * nv * nv if jac is not None else 16)
     roof = None
     kf = KINETICS_FLOPS.get(chem.mech.name)
-    if kf is not None and gen is None and tab is None:
+    if kf is not None and tab is None:
         fl = kf["jac" if jac is not None else "rhs"]
         peak = chem_peak_fp64()
-        roof = {"bound": "fp64", "kernel": f"k_wdot_warp<{int(jac is not None)}>",
+        roof = {"bound": "fp64", "kernel": (f"ytf_<mech>_{'jac_' if jac is not None else ''}kernel" if gen else
+                                            f"k_wdot_warp<{int(jac is not None)}>"),
+                "flops_note": "the data-driven kernel's FP64 operations per state, for both kernels",
                 "flops_per_state": fl, "achieved": n * fl / t / 1e12, "peak": peak, "unit": "TFLOP/s",
                 "frac": (n * fl / t / 1e12) / peak if peak else None,
                 "peak_source": "DFMA probe kernel measured in this run",
@@ -674,6 +683,7 @@ def run_kernel_workload(args):
                       "gpu_launches": kernel_launches() - l0,
                       "hbm_gbs_algorithmic": n * bytes_per_state / t / 1e9,
                       "bytes_per_state": bytes_per_state, "roofline": roof, "parity": parity,
+                      "tuning": tuning,
                       "cpu_baseline": None if args.no_cpu_baseline else
                       cpu_baseline_kernels(chem.mech, T, p, Y, jac is not None, tab)}))
 
@@ -761,7 +771,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cells", type=int, default=None)
     ap.add_argument("--workload", default="reactor",
-                    choices=["reactor", "reactor-c5", "c1-wdot", "c2-wdot", "c2-wdotjac", "c5-wdot", "c5-wdotjac",
+                    choices=["reactor", "reactor-c5", "c1-wdot", "c1-wdotjac", "c2-wdot", "c2-wdotjac", "c5-wdot",
+                             "c5-wdotjac",
                              "c2-general"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-parity", action="store_true",

@@ -64,6 +64,19 @@ class Chemistry:
         native.check(self.L.flint_mech_create(C.byref(desc), C.byref(h)), "flint_mech_create")
         self.h = h
         self.ns, self.nr = mech.ns, mech.nr
+        self._gen, self._use_gen, self._use_gen_jac = None, False, False
+
+    def use_generated(self, on=True, jac=None):
+        """Serve wdot (and, with jac, wdot + Jacobian; cell-major device
+        tensors) from the mechanism's generated kernels (flint_gb300.ytf_cuda)
+        instead of the library's data-driven ones; flint_gb300.autotune makes
+        these choices by timing both.  jac=None leaves the Jacobian's choice."""
+        if (on or jac) and self._gen is None:
+            from .ytf_cuda import GeneratedMechanism
+            self._gen = GeneratedMechanism(self.mech)
+        self._use_gen = bool(on)
+        if jac is not None:
+            self._use_gen_jac = bool(jac)
 
     @classmethod
     def from_ir(cls, blob, mech: Mechanism = None):
@@ -73,6 +86,7 @@ class Chemistry:
         (species names and the element matrix are not in the blob)."""
         obj = cls.__new__(cls)
         obj.mech, obj.L = mech, native.lib()
+        obj._gen, obj._use_gen, obj._use_gen_jac = None, False, False
         h = C.c_void_p()
         native.check(obj.L.flint_mech_create_from_ir(bytes(blob), len(blob), C.byref(h)), "flint_mech_create_from_ir")
         obj.h = h
@@ -105,6 +119,9 @@ class Chemistry:
             import torch
             if wdot is None:
                 wdot = torch.empty_like(Y)
+            if self._use_gen and layout == CELL_MAJOR:
+                self._gen.wdot(T, p, Y, wdot=wdot, cp=cp, h=h, alloc=False)
+                return wdot, cp, h
             native.check(self.L.flint_wdot_batch(self.h, n, layout, _dptr(T), _dptr(p), _dptr(Y), _dptr(wdot),
                                                  _dptr(cp), _dptr(h), _stream()), "flint_wdot_batch")
             return wdot, cp, h
@@ -138,6 +155,9 @@ class Chemistry:
             import torch
             if jac is None:
                 jac = torch.empty((n, nv, nv), dtype=torch.float64, device=T.device)
+            if self._use_gen_jac and layout == CELL_MAJOR:
+                self._gen.wdot_jac(T, p, Y, wdot=wdot, jac=jac)
+                return wdot, jac
             native.check(self.L.flint_wdot_jac_batch(self.h, n, layout, _dptr(T), _dptr(p), _dptr(Y), _dptr(wdot),
                                                      _dptr(jac), _stream()), "flint_wdot_jac_batch")
             return wdot, jac
@@ -193,12 +213,39 @@ class Chemistry:
     def reactor_autotune(self, T, p, Y, dt, rtol=1e-8, atol=1e-14, max_steps=20000, max_order=5):
         """Time the reactor's layouts on these cells (device tensors, left
         unchanged) and keep the fastest for this handle; returns the layout
-        (1 shared memory, 2 global slot / 8 warps per block, 3 global slot / 4 warps)."""
+        (1 shared memory, 2 global slot / 8 warps per block, 3 global slot / 4 warps,
+        4 global slot / two blocks of 8 warps per SM)."""
         opts = native.reactor_opts(rtol, atol, max_steps, max_order)
         lay = C.c_int(0)
         native.check(self.L.flint_reactor_autotune(self.h, T.shape[0], _dptr(T), _dptr(p), _dptr(Y), _dptr(dt),
                                                    C.byref(opts), C.byref(lay), _stream()), "flint_reactor_autotune")
         return lay.value
+
+    def reactor_autotune_times(self):
+        """{layout: ms} of the last reactor_autotune on this handle."""
+        lays = (C.c_int * 8)()
+        ms = (C.c_float * 8)()
+        cnt = C.c_int(0)
+        native.check(self.L.flint_reactor_autotune_times(self.h, lays, ms, 8, C.byref(cnt)),
+                     "flint_reactor_autotune_times")
+        return {int(lays[i]): float(ms[i]) for i in range(min(cnt.value, 8))}
+
+    def wdot_autotune(self, T, p, Y):
+        """Time the source-term kernels at each block size on these cells (device
+        tensors, cell-major) and keep the fastest; returns the handle's tuning."""
+        t = native.Tuning()
+        native.check(self.L.flint_wdot_autotune(self.h, T.shape[0], _dptr(T), _dptr(p), _dptr(Y), C.byref(t),
+                                                _stream()), "flint_wdot_autotune")
+        return {f: getattr(t, f) for f, _ in native.Tuning._fields_ if f != "reserved"}
+
+    def tuning(self):
+        t = native.Tuning()
+        native.check(self.L.flint_tuning_get(self.h, C.byref(t)), "flint_tuning_get")
+        return {f: getattr(t, f) for f, _ in native.Tuning._fields_ if f != "reserved"}
+
+    def set_tuning(self, reactor_layout=0, wdot_threads=0, jac_threads=0):
+        t = native.Tuning(int(reactor_layout), int(wdot_threads), int(jac_threads), 0)
+        native.check(self.L.flint_tuning_set(self.h, C.byref(t)), "flint_tuning_set")
 
     def reactor_advance(self, T, p, Y, dt, rtol=1e-8, atol=1e-14, max_steps=20000, max_order=5,
                         tmin=200.0, tmax=6000.0, status=None, nsteps=None, constant_volume=False):

@@ -57,6 +57,11 @@ struct flint_mech_s {
   double* djsave = nullptr;
   int jslots = 0;
   int rx_layout = 0;       // reactor layout chosen by flint_reactor_autotune (0: by size)
+  int tuned_n = 0;         // layouts the last flint_reactor_autotune timed, and their times
+  int tuned_layout[8] = {0};
+  float tuned_ms[8] = {0.f};
+  int wdot_threads = 0;    // threads per block of the source-term warp kernels (0: default)
+  int jac_threads = 0;
   // Jacobian work area of the warp kernels for 32-63 species
   double* dwscratch = nullptr;
   // staging buffers of the *_host entry points (grow only)
@@ -438,7 +443,7 @@ int flint_wdot_batch(flint_mech_t h, int64_t n, int layout, const double* T, con
   if (rc) return rc;
   if (n == 0) return FLINT_OK;
   if (!T || !p || !Y || !wdot) return fail(FLINT_ERR_ARG, "NULL array");
-  cudaError_t e = launch_wdot(h->dimg, h->L, n, layout, T, p, Y, wdot, cp, hm, (cudaStream_t)stream);
+  cudaError_t e = launch_wdot(h->dimg, h->L, n, layout, T, p, Y, wdot, cp, hm, (cudaStream_t)stream, h->wdot_threads);
   return e == cudaSuccess ? FLINT_OK : cuda_fail(e, "flint_wdot_batch");
 }
 
@@ -491,7 +496,8 @@ int flint_wdot_jac_batch(flint_mech_t h, int64_t n, int layout, const double* T,
     cudaError_t ea = cudaMalloc(&h->dwscratch, (size_t)need * sizeof(double));
     if (ea != cudaSuccess) { h->dwscratch = nullptr; return fail(FLINT_ERR_NOMEM, "Jacobian work area: %s", cudaGetErrorString(ea)); }
   }
-  cudaError_t e = launch_wdot_jac(h->dimg, h->L, n, layout, T, p, Y, wdot, jac, h->dwscratch, (cudaStream_t)stream);
+  cudaError_t e = launch_wdot_jac(h->dimg, h->L, n, layout, T, p, Y, wdot, jac, h->dwscratch, (cudaStream_t)stream,
+                                  0, h->jac_threads);
   return e == cudaSuccess ? FLINT_OK : cuda_fail(e, "flint_wdot_jac_batch");
 }
 
@@ -566,7 +572,8 @@ int flint_reactor_autotune(flint_mech_t h, int64_t n, const double* T, const dou
   rc = ensure_jsave(h);
   if (rc) return rc;
   h->rx_layout = REACTOR_LAYOUT_AUTO;
-  int cand[4];
+  h->tuned_n = 0;
+  int cand[8];
   const int nc = reactor_layout_candidates(h->L, cand);
   if (n > 0) {
     // time the sample under each layout on private copies (the caller's arrays stay as they are)
@@ -594,6 +601,7 @@ int flint_reactor_autotune(flint_mech_t h, int64_t n, const double* T, const dou
       }
       float ms = 0.f;
       if (!e) e = cudaEventElapsedTime(&ms, e0, e1);
+      if (!e && c < 8) { h->tuned_layout[c] = cand[c]; h->tuned_ms[c] = ms; h->tuned_n = c + 1; }
       if (!e && (c == 0 || ms < best)) { best = ms; h->rx_layout = cand[c]; }
     }
     if (e0) cudaEventDestroy(e0);
@@ -602,6 +610,95 @@ int flint_reactor_autotune(flint_mech_t h, int64_t n, const double* T, const dou
     if (e) { h->rx_layout = REACTOR_LAYOUT_AUTO; return cuda_fail(e, "flint_reactor_autotune"); }
   }
   if (layout_out) *layout_out = h->rx_layout;
+  return FLINT_OK;
+}
+
+int flint_reactor_autotune_times(flint_mech_t h, int* layouts, float* ms, int cap, int* count) {
+  if (!h || cap < 0 || (cap > 0 && (!layouts || !ms)) || !count) return fail(FLINT_ERR_ARG, "NULL argument");
+  *count = h->tuned_n;
+  for (int i = 0; i < h->tuned_n && i < cap; ++i) { layouts[i] = h->tuned_layout[i]; ms[i] = h->tuned_ms[i]; }
+  return FLINT_OK;
+}
+
+int flint_tuning_get(flint_mech_t h, flint_tuning* t) {
+  if (!h || !t) return fail(FLINT_ERR_ARG, "NULL argument");
+  t->reactor_layout = h->rx_layout;
+  t->wdot_threads = h->wdot_threads;
+  t->jac_threads = h->jac_threads;
+  t->reserved = 0;
+  return FLINT_OK;
+}
+
+int flint_tuning_set(flint_mech_t h, const flint_tuning* t) {
+  if (!h || !t) return fail(FLINT_ERR_ARG, "NULL argument");
+  if (h->table) return fail(FLINT_ERR_MECH, "this entry point needs an analytic (NASA-7/Arrhenius) mechanism");
+  bool ok = t->reactor_layout == REACTOR_LAYOUT_AUTO;
+  int cand[8];
+  const int nc = reactor_layout_candidates(h->L, cand);
+  for (int c = 0; c < nc; ++c) ok |= cand[c] == t->reactor_layout;
+  if (!ok) return fail(FLINT_ERR_ARG, "reactor layout %d does not fit this mechanism on this device", t->reactor_layout);
+  int bc[4];
+  const int nb = warp_block_candidates(bc);
+  for (int v : {t->wdot_threads, t->jac_threads}) {
+    bool okb = v == 0;
+    for (int c = 0; c < nb; ++c) okb |= bc[c] == v;
+    if (!okb) return fail(FLINT_ERR_ARG, "%d threads per block: the source-term kernels take 0, 64, 128 or 256", v);
+  }
+  h->rx_layout = t->reactor_layout;
+  h->wdot_threads = t->wdot_threads;
+  h->jac_threads = t->jac_threads;
+  return FLINT_OK;
+}
+
+int flint_wdot_autotune(flint_mech_t h, int64_t n, const double* T, const double* p, const double* Y,
+                        flint_tuning* out, void* stream) {
+  int rc = check_common(h, n, FLINT_CELL_MAJOR);
+  if (rc) return rc;
+  if (n < 1 || !T || !p || !Y) return fail(FLINT_ERR_ARG, "flint_wdot_autotune needs a sample of cells");
+  const int64_t need = warp_jac_scratch_doubles(h->L);
+  if (need > 0 && !h->dwscratch) {
+    cudaError_t ea = cudaMalloc(&h->dwscratch, (size_t)need * sizeof(double));
+    if (ea != cudaSuccess) { h->dwscratch = nullptr; return fail(FLINT_ERR_NOMEM, "Jacobian work area: %s", cudaGetErrorString(ea)); }
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  const int ns = h->L.ns, nv = ns + 1;
+  double *w = nullptr, *J = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  cudaError_t e = cudaMalloc(&w, (size_t)n * ns * sizeof(double));
+  if (!e) e = cudaMalloc(&J, (size_t)n * nv * nv * sizeof(double));
+  if (!e) e = cudaEventCreate(&e0);
+  if (!e) e = cudaEventCreate(&e1);
+  int cand[4];
+  const int nc = warp_block_candidates(cand);
+  int best_w = 0, best_j = 0;
+  float tw = 0.f, tj = 0.f;
+  for (int jac = 0; jac < 2 && !e; ++jac) {
+    if (!jac && use_small_kernel(h->L)) continue;   // the thread-per-cell kernel serves this mechanism
+    for (int c = 0; c < nc && !e; ++c) {
+      float ms = 0.f;
+      for (int rep = 0; rep < 3 && !e; ++rep) {   // the first run of each block size warms up
+        e = cudaEventRecord(e0, st);
+        if (!e) e = jac ? launch_wdot_jac(h->dimg, h->L, n, FLINT_CELL_MAJOR, T, p, Y, w, J, h->dwscratch, st, 0, cand[c])
+                        : launch_wdot(h->dimg, h->L, n, FLINT_CELL_MAJOR, T, p, Y, w, nullptr, nullptr, st, cand[c]);
+        if (!e) e = cudaEventRecord(e1, st);
+        if (!e) e = cudaEventSynchronize(e1);
+        float one = 0.f;
+        if (!e) e = cudaEventElapsedTime(&one, e0, e1);
+        if (rep > 0) ms += one;
+      }
+      if (e) break;
+      if (jac) { if (c == 0 || ms < tj) { tj = ms; best_j = cand[c]; } }
+      else { if (c == 0 || ms < tw) { tw = ms; best_w = cand[c]; } }
+    }
+  }
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  cudaFree(w);
+  cudaFree(J);
+  if (e) return cuda_fail(e, "flint_wdot_autotune");
+  h->wdot_threads = best_w;
+  h->jac_threads = best_j;
+  if (out) return flint_tuning_get(h, out);
   return FLINT_OK;
 }
 

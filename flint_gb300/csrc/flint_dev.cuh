@@ -125,9 +125,12 @@ __device__ inline void stage_image(uint8_t* smem, const uint8_t* __restrict__ g,
 // ln2/64 is split into a 32-bit head and a tail (the classic fdlibm split of
 // ln2) so that n*head is exact.  2^(j/64) comes from the 64-entry table staged
 // with the mechanism.  10 FP64 operations; |x| >= 700, NaN and Inf take the
-// CUDA library path.  Accuracy is tested against CUDA's exp (tests/test_gpu_parity.py).
+// CUDA library path (the range test compares the high word as an integer, so
+// it costs no FP64-pipe slot: |x| < 700 exactly when it is below 0x4085E000,
+// the high word of 700.0).  Accuracy is tested against CUDA's exp
+// (tests/test_gpu_parity.py).
 __device__ __forceinline__ double fexp(double x, const double* __restrict__ tab) {
-  if (!(fabs(x) < 700.0)) return exp(x);
+  if ((__double2hiint(x) & 0x7fffffff) >= 0x4085E000) return exp(x);
   const double SHIFT = 6755399441055744.0;               // 1.5 * 2^52
   const double INV_L = 92.33248261689366;                // 64 / ln2
   const double L_HI = 0.01083042469326756;               // 0x1.62e42fee00000p-7
@@ -425,10 +428,11 @@ __device__ void warp_kinetics(const MechView& m, const WarpScratch& s, int lane,
     lg_in = lg_in > 1e-300 ? lg_in : 1e-300;
     const double lg = log10(lg_in);
     const double logPr = __shfl_sync(FULL, lg, lane < NF ? lane + NF : 0);
-    // two divisions per lane for the blend: 1/(den (1 + Pr)) yields both
-    // 1/den and 1/(1 + Pr); 1/opf the other
+    // one division per lane for the blend (an FP64 division is a dozen pipe
+    // instructions): with Q = den^2 + x^2, 1/(den (1 + Pr) Q) yields 1/den,
+    // 1/(1 + Pr) and 1/Q, and 1/(1 + f1^2) = den^2 / Q
     double Fb = 1.0, G = 0.0, dlnF_T = 0.0, fexp_arg = 0.0;
-    double opf = 1.0, iopf = 1.0, x = 0.0, nn = 0.0, logFc = 0.0, den = 1.0, iden = 1.0, f1 = 0.0;
+    double iopf = 1.0, x = 0.0, nn = 0.0, logFc = 0.0, den = 1.0, iden = 1.0, f1 = 0.0;
     double iopr = 1.0;
     if (lane < NF && troe) {
       logFc = lg;
@@ -437,12 +441,13 @@ __device__ void warp_kinetics(const MechView& m, const WarpScratch& s, int lane,
       x = logPr + cc;
       den = nn - 0.14 * x;
       const double opr = 1.0 + Pr;
-      const double rr = 1.0 / (den * opr);
-      iden = rr * opr;
-      iopr = rr * den;
+      const double Q = fma(den, den, x * x);
+      const double dQ = den * Q;
+      const double rr = 1.0 / (dQ * opr);
+      iden = rr * opr * Q;
+      iopr = rr * dQ;
       f1 = x * iden;
-      opf = 1.0 + f1 * f1;
-      iopf = 1.0 / opf;
+      iopf = den * den * (rr * opr * den);
       fexp_arg = 2.302585092994045684 * (logFc * iopf);
     } else if (lane < NF) {
       iopr = 1.0 / (1.0 + Pr);

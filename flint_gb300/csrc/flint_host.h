@@ -43,8 +43,12 @@ inline cudaError_t set_smem(const void* fn, size_t bytes) {
   return e;
 }
 
+// threads: threads per block of the warp kernels (64, 128 or 256; 0 = 256)
 cudaError_t launch_wdot(const uint8_t* img, const ImageLayout& L, int64_t n, int layout, const double* T,
-                        const double* p, const double* Y, double* wdot, double* cp, double* h, cudaStream_t st);
+                        const double* p, const double* Y, double* wdot, double* cp, double* h, cudaStream_t st,
+                        int threads = 0);
+int warp_block_candidates(int* out);
+bool use_small_kernel(const ImageLayout& L);   // wdot of <= 8 species: thread per cell
 cudaError_t launch_species_thermo(const uint8_t* img, const ImageLayout& L, int64_t n, const double* T, double* cp,
                                   double* h, double* s, double* g, cudaStream_t st);
 cudaError_t launch_thermo(const uint8_t* img, const ImageLayout& L, int64_t n, int layout, const double* T,
@@ -53,7 +57,7 @@ cudaError_t launch_chemistry_source(const uint8_t* img, const ImageLayout& L, in
                                     const double* T, double* omegadot, cudaStream_t st);
 cudaError_t launch_wdot_jac(const uint8_t* img, const ImageLayout& L, int64_t n, int layout, const double* T,
                             const double* p, const double* Y, double* wdot, double* jac, double* gscratch,
-                            cudaStream_t st, int cv = 0);   // cv: constant volume, p holds rho
+                            cudaStream_t st, int cv = 0, int threads = 0);   // cv: constant volume, p holds rho
 int64_t warp_jac_scratch_doubles(const ImageLayout& L);
 cudaError_t launch_rhs(const uint8_t* img, const ImageLayout& L, int64_t n, const double* T, const double* p,
                        const double* Y, double* f, cudaStream_t st, int cv = 0);
@@ -61,7 +65,8 @@ int reactor_slots(const ImageLayout& L);
 size_t reactor_slot_bytes(const ImageLayout& L);
 // Reactor layouts: the Newton matrix in shared memory (8 warps per block) or in
 // the warp's global slot (8 or 4 warps per block).
-enum { REACTOR_LAYOUT_AUTO = 0, REACTOR_LAYOUT_SHARED = 1, REACTOR_LAYOUT_GLOBAL = 2, REACTOR_LAYOUT_GLOBAL4 = 3 };
+enum { REACTOR_LAYOUT_AUTO = 0, REACTOR_LAYOUT_SHARED = 1, REACTOR_LAYOUT_GLOBAL = 2, REACTOR_LAYOUT_GLOBAL4 = 3,
+       REACTOR_LAYOUT_GLOBAL2B = 4 };
 // The layouts possible for this mechanism (what the autotuner chooses between); returns their count.
 int reactor_layout_candidates(const ImageLayout& L, int* out);
 cudaError_t launch_reactor(const uint8_t* img, const ImageLayout& L, int64_t n, double* T, const double* p,

@@ -12,6 +12,7 @@
 //
 // All kernels are grid-stride loops over cells sized to whole waves of the 152
 // SMs, so any N (including 0 and ragged tails) is handled without a tail kernel.
+#include <algorithm>
 #include <atomic>
 #include "flint_dev.cuh"
 #include "flint_host.h"
@@ -358,16 +359,25 @@ static int64_t grid_for(const void* fn, int threads, size_t smem, int64_t work_i
 
 size_t small_smem(const ImageLayout& L) { return L.bytes + 3 * SMALL_NSMAX * SMALL_THREADS * sizeof(double); }
 // Jacobian work area in global memory: 33-63 species, or a shared-memory
-// layout too large for a block.
+// layout too large for a block of 256 threads (the choice does not depend on
+// the block size a caller tunes, so one kernel serves every block size).
 static bool warp_gj(const ImageLayout& L, bool jac) {
   if (L.nsp > 32) return true;
   if (!jac) return false;
   return L.bytes + (WARP_THREADS / 32) * scratch_doubles(L.nsp, L.nrpad, true) * sizeof(double) > device_smem_optin();
 }
 
-size_t warp_smem(const ImageLayout& L, bool jac) {
-  if (warp_gj(L, jac)) return L.bytes + (WARP_THREADS / 32) * scratch_small_doubles(L.nsp, L.nrpad) * sizeof(double);
-  return L.bytes + (WARP_THREADS / 32) * scratch_doubles(L.nsp, L.nrpad, jac) * sizeof(double);
+static int warp_block(int threads) { return threads == 64 || threads == 128 ? threads : WARP_THREADS; }
+
+size_t warp_smem(const ImageLayout& L, bool jac, int threads) {
+  const int wpb = warp_block(threads) / 32;
+  if (warp_gj(L, jac)) return L.bytes + wpb * scratch_small_doubles(L.nsp, L.nrpad) * sizeof(double);
+  return L.bytes + wpb * scratch_doubles(L.nsp, L.nrpad, jac) * sizeof(double);
+}
+
+int warp_block_candidates(int* out) {
+  out[0] = 64; out[1] = 128; out[2] = WARP_THREADS;
+  return 3;
 }
 
 template <bool JAC>
@@ -378,37 +388,45 @@ static const void* warp_fn(const ImageLayout& L) {
 
 // Global Jacobian work area needed by the warp kernels (doubles), for a grid
 // of full waves; 0 when it lives in shared memory.
+// (enough for the resident warps of every block size)
 int64_t warp_jac_scratch_doubles(const ImageLayout& L) {
   if (!warp_gj(L, true)) return 0;
-  size_t sm = warp_smem(L, true);
   const void* fn = warp_fn<true>(L);
-  if (set_smem(fn, sm) != cudaSuccess) return 0;
-  int per_sm = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, WARP_THREADS, sm);
-  if (per_sm < 1) per_sm = 1;
-  return (int64_t)per_sm * device_sms() * (WARP_THREADS / 32) * scratch_jac_doubles(L.nsp, L.nrpad);
+  int64_t most = 0;
+  int cand[4];
+  const int nc = warp_block_candidates(cand);
+  for (int c = 0; c < nc; ++c) {
+    const size_t sm = warp_smem(L, true, cand[c]);
+    if (set_smem(fn, sm) != cudaSuccess) return 0;
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, cand[c], sm);
+    if (per_sm < 1) per_sm = 1;
+    most = std::max(most, (int64_t)per_sm * device_sms() * (cand[c] / 32));
+  }
+  return most * scratch_jac_doubles(L.nsp, L.nrpad);
 }
 
 template <bool JAC>
 static cudaError_t launch_warp(const uint8_t* img, const ImageLayout& L, int64_t n, int layout, const double* T,
                                const double* p, const double* Y, double* wdot, double* cp, double* h, double* jac,
-                               double* rhs, double* gscratch, cudaStream_t st, int cv = 0) {
-  size_t sm = warp_smem(L, JAC);
+                               double* rhs, double* gscratch, cudaStream_t st, int cv = 0, int threads = 0) {
+  const int bt = warp_block(threads);
+  size_t sm = warp_smem(L, JAC, bt);
   const void* fn = warp_fn<JAC>(L);
   cudaError_t e = set_smem(fn, sm);
   if (e != cudaSuccess) return e;
   const bool gj = warp_gj(L, JAC);
   if (gj && JAC && !gscratch) return cudaErrorInvalidValue;
-  int64_t g = grid_for(fn, WARP_THREADS, sm, n * 32);
+  int64_t g = grid_for(fn, bt, sm, n * 32);
   if (L.nsp > 32)
-    k_wdot_warp<JAC, 2, true><<<(unsigned)g, WARP_THREADS, sm, st>>>(img, L, n, layout, T, p, Y, wdot, cp, h, jac,
-                                                                      rhs, gscratch, cv);
+    k_wdot_warp<JAC, 2, true><<<(unsigned)g, bt, sm, st>>>(img, L, n, layout, T, p, Y, wdot, cp, h, jac, rhs,
+                                                            gscratch, cv);
   else if (gj)
-    k_wdot_warp<JAC, 1, true><<<(unsigned)g, WARP_THREADS, sm, st>>>(img, L, n, layout, T, p, Y, wdot, cp, h, jac,
-                                                                      rhs, gscratch, cv);
+    k_wdot_warp<JAC, 1, true><<<(unsigned)g, bt, sm, st>>>(img, L, n, layout, T, p, Y, wdot, cp, h, jac, rhs,
+                                                            gscratch, cv);
   else
-    k_wdot_warp<JAC, 1, false><<<(unsigned)g, WARP_THREADS, sm, st>>>(img, L, n, layout, T, p, Y, wdot, cp, h, jac,
-                                                                       rhs, nullptr, cv);
+    k_wdot_warp<JAC, 1, false><<<(unsigned)g, bt, sm, st>>>(img, L, n, layout, T, p, Y, wdot, cp, h, jac, rhs,
+                                                             nullptr, cv);
   count_launch();
   return cudaGetLastError();
 }
@@ -417,7 +435,7 @@ bool use_small_kernel(const ImageLayout& L) { return L.ns <= SMALL_NSMAX && L.ns
 
 cudaError_t launch_wdot(const uint8_t* img, const ImageLayout& L, int64_t n, int layout, const double* T,
                         const double* p, const double* Y, double* wdot, double* cp, double* h,
-                        cudaStream_t st) {
+                        cudaStream_t st, int threads) {
   if (n <= 0) return cudaSuccess;
   if (use_small_kernel(L)) {
     size_t sm = small_smem(L);
@@ -427,7 +445,7 @@ cudaError_t launch_wdot(const uint8_t* img, const ImageLayout& L, int64_t n, int
     count_launch();
     return cudaGetLastError();
   }
-  return launch_warp<false>(img, L, n, layout, T, p, Y, wdot, cp, h, nullptr, nullptr, nullptr, st);
+  return launch_warp<false>(img, L, n, layout, T, p, Y, wdot, cp, h, nullptr, nullptr, nullptr, st, 0, threads);
 }
 
 cudaError_t launch_thermo(const uint8_t* img, const ImageLayout& L, int64_t n, int layout, const double* T,
@@ -466,9 +484,10 @@ cudaError_t launch_chemistry_source(const uint8_t* img, const ImageLayout& L, in
 
 cudaError_t launch_wdot_jac(const uint8_t* img, const ImageLayout& L, int64_t n, int layout, const double* T,
                             const double* p, const double* Y, double* wdot, double* jac, double* gscratch,
-                            cudaStream_t st, int cv) {
+                            cudaStream_t st, int cv, int threads) {
   if (n <= 0) return cudaSuccess;
-  return launch_warp<true>(img, L, n, layout, T, p, Y, wdot, nullptr, nullptr, jac, nullptr, gscratch, st, cv);
+  return launch_warp<true>(img, L, n, layout, T, p, Y, wdot, nullptr, nullptr, jac, nullptr, gscratch, st, cv,
+                           threads);
 }
 
 cudaError_t launch_rhs(const uint8_t* img, const ImageLayout& L, int64_t n, const double* T, const double* p,

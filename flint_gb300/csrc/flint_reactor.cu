@@ -237,9 +237,11 @@ static size_t reactor_smem_spl1(const ImageLayout& L) {
 
 // layout: REACTOR_LAYOUT_AUTO picks shared memory whenever the block fits;
 // REACTOR_LAYOUT_SHARED / _GLOBAL force one (the autotuner times both).
+// REACTOR_LAYOUT_GLOBAL2B: global slots, two blocks of 8 warps per SM (16
+// resident warps) from a build capped at 128 registers per thread.
 static bool reactor_gj(const ImageLayout& L, int layout = REACTOR_LAYOUT_AUTO) {
   if (spl_of(L) > 1 || reactor_smem_spl1(L) > device_smem_optin()) return true;
-  return layout == REACTOR_LAYOUT_GLOBAL || layout == REACTOR_LAYOUT_GLOBAL4;
+  return layout == REACTOR_LAYOUT_GLOBAL || layout == REACTOR_LAYOUT_GLOBAL4 || layout == REACTOR_LAYOUT_GLOBAL2B;
 }
 
 // Threads per block: 8 warps, or 4 in the GLOBAL4 layout (half the resident
@@ -253,8 +255,8 @@ static int64_t reactor_slot_doubles_of(const ImageLayout& L, int layout = REACTO
   return (int64_t)(32 * spl) * (32 * spl) + (reactor_gj(L, layout) ? scratch_jac_doubles(L.nsp, L.nrpad) : 0);
 }
 
-template <int SPL, bool GJ>
-__global__ void __launch_bounds__(REACTOR_THREADS)
+template <int SPL, bool GJ, int MINB = 1>
+__global__ void __launch_bounds__(REACTOR_THREADS, MINB)
 k_reactor(const uint8_t* __restrict__ img, ImageLayout L, int64_t n, double* __restrict__ Tg,
           const double* __restrict__ pg, double* __restrict__ Yg, const double* __restrict__ dtg,
           flint_reactor_opts o, int* __restrict__ status_g, int* __restrict__ nsteps_g,
@@ -590,7 +592,9 @@ size_t reactor_smem(const ImageLayout& L, int layout = REACTOR_LAYOUT_AUTO) {
 }
 
 static const void* reactor_fn(const ImageLayout& L, int layout = REACTOR_LAYOUT_AUTO) {
-  if (spl_of(L) > 1) return (const void*)k_reactor<2, true>;
+  const bool two = layout == REACTOR_LAYOUT_GLOBAL2B;
+  if (spl_of(L) > 1) return two ? (const void*)k_reactor<2, true, 2> : (const void*)k_reactor<2, true>;
+  if (two) return (const void*)k_reactor<1, true, 2>;
   return reactor_gj(L, layout) ? (const void*)k_reactor<1, true> : (const void*)k_reactor<1, false>;
 }
 
@@ -606,7 +610,7 @@ static int slots_of(const ImageLayout& L, int layout) {
 // Resident-warp slots and bytes per slot that serve every layout.
 int reactor_slots(const ImageLayout& L) {
   if (spl_of(L) < 1 || spl_of(L) > 2) return 0;
-  return std::max(slots_of(L, REACTOR_LAYOUT_AUTO),
+  return std::max(std::max(slots_of(L, REACTOR_LAYOUT_AUTO), slots_of(L, REACTOR_LAYOUT_GLOBAL2B)),
                   std::max(slots_of(L, REACTOR_LAYOUT_GLOBAL), slots_of(L, REACTOR_LAYOUT_GLOBAL4)));
 }
 
@@ -620,6 +624,7 @@ int reactor_layout_candidates(const ImageLayout& L, int* out) {
   if (spl_of(L) == 1 && reactor_smem_spl1(L) <= device_smem_optin()) out[k++] = REACTOR_LAYOUT_SHARED;
   out[k++] = REACTOR_LAYOUT_GLOBAL;
   out[k++] = REACTOR_LAYOUT_GLOBAL4;
+  out[k++] = REACTOR_LAYOUT_GLOBAL2B;
   return k;
 }
 
@@ -669,7 +674,13 @@ cudaError_t launch_reactor(const uint8_t* img, const ImageLayout& L, int64_t n, 
   if (e != cudaSuccess) return e;
   const int64_t sd = reactor_slot_doubles_of(L, layout);
   unsigned long long* wc = reinterpret_cast<unsigned long long*>(work_counter);
-  if (spl_of(L) > 1)
+  if (layout == REACTOR_LAYOUT_GLOBAL2B && spl_of(L) > 1)
+    k_reactor<2, true, 2><<<(unsigned)blocks, threads, sm, st>>>(img, L, n, T, p, Y, dt, o, status, nsteps, wc,
+                                                                          jsave, sd, n_dev);
+  else if (layout == REACTOR_LAYOUT_GLOBAL2B)
+    k_reactor<1, true, 2><<<(unsigned)blocks, threads, sm, st>>>(img, L, n, T, p, Y, dt, o, status, nsteps, wc,
+                                                                          jsave, sd, n_dev);
+  else if (spl_of(L) > 1)
     k_reactor<2, true><<<(unsigned)blocks, threads, sm, st>>>(img, L, n, T, p, Y, dt, o, status, nsteps, wc,
                                                                        jsave, sd, n_dev);
   else if (reactor_gj(L, layout))

@@ -53,6 +53,12 @@ class ReactorOpts(C.Structure):
                 ("tmin", C.c_double), ("tmax", C.c_double)]
 
 
+class Tuning(C.Structure):
+    """flint_tuning."""
+    _fields_ = [("reactor_layout", C.c_int), ("wdot_threads", C.c_int), ("jac_threads", C.c_int),
+                ("reserved", C.c_int)]
+
+
 def reactor_opts(rtol=1e-8, atol=1e-14, max_steps=20000, max_order=5, tmin=200.0, tmax=6000.0,
                  constant_volume=False):
     return ReactorOpts(rtol, atol, max_steps, max_order, 1 if constant_volume else 0, 0, tmin, tmax)
@@ -115,6 +121,10 @@ def lib():
     L.flint_reactor_default_opts.argtypes = [C.POINTER(ReactorOpts)]
     L.flint_reactor_advance_noalloc.argtypes = [vp, i64, vp, vp, vp, vp, C.POINTER(ReactorOpts), vp, vp, vp]
     L.flint_reactor_stats.argtypes = [vp, C.POINTER(C.c_int64)]
+    L.flint_reactor_autotune_times.argtypes = [vp, _ip, C.POINTER(C.c_float), C.c_int, _ip]
+    L.flint_tuning_get.argtypes = [vp, C.POINTER(Tuning)]
+    L.flint_tuning_set.argtypes = [vp, C.POINTER(Tuning)]
+    L.flint_wdot_autotune.argtypes = [vp, i64, vp, vp, vp, C.POINTER(Tuning), vp]
     L.flint_probe_fp64_peak.argtypes = [C.POINTER(C.c_double)]
     L.flint_selftest_exp.argtypes = [vp, i64, vp, vp, vp]
     L.flint_mech_create_tables.argtypes = [C.POINTER(TableDesc), C.POINTER(vp)]

@@ -321,10 +321,38 @@ int flint_reactor_advance(flint_mech_t mech, int64_t n, double* T, const double*
  * the L1 cache that holds the slots).  Times flint_reactor_advance under each
  * possible layout on a sample of cells (n of them, device arrays; the caller's
  * arrays are not modified), keeps the fastest for later calls on this handle,
- * and reports it in *layout (1 shared, 2 global / 8 warps, 3 global / 4 warps).
+ * and reports it in *layout (1 shared, 2 global / 8 warps, 3 global / 4 warps,
+ * 4 global / two blocks of 8 warps per SM from a build capped at 128 registers).
  * No reference counterpart. */
 int flint_reactor_autotune(flint_mech_t mech, int64_t n, const double* T, const double* p, const double* Y,
                            const double* dt, const flint_reactor_opts* opts, int* layout, void* stream);
+/* The layouts the last flint_reactor_autotune on this handle timed and their
+ * times [ms] (at most cap of them; *count = how many were timed).  No
+ * reference counterpart. */
+int flint_reactor_autotune_times(flint_mech_t mech, int* layouts, float* ms, int cap, int* count);
+/* The tuning a handle runs with: the reactor layout (0 = by size, 1-4 as
+ * flint_reactor_autotune reports them) and the threads per block of the
+ * warp-per-cell source-term kernels, for wdot (flint_wdot_batch) and for
+ * wdot + Jacobian (flint_wdot_jac_batch): 64, 128 or 256, 0 = 256.  No
+ * reference counterpart. */
+typedef struct {
+  int reactor_layout;
+  int wdot_threads;
+  int jac_threads;
+  int reserved;
+} flint_tuning;
+int flint_tuning_get(flint_mech_t mech, flint_tuning* tuning);
+/* Apply a tuning chosen earlier (a tuning cache) without timing; a layout or
+ * block size that does not fit this mechanism on the current device is
+ * refused (FLINT_ERR_ARG) and nothing changes. */
+int flint_tuning_set(flint_mech_t mech, const flint_tuning* tuning);
+/* Empirical choice of the source-term kernels' block size: times
+ * flint_wdot_batch and flint_wdot_jac_batch at every block size on a sample
+ * of cells (n of them, device arrays, cell-major; outputs go to private
+ * buffers), keeps the fastest for this handle and reports the handle's tuning
+ * in *tuning (may be NULL).  No reference counterpart. */
+int flint_wdot_autotune(flint_mech_t mech, int64_t n, const double* T, const double* p, const double* Y,
+                        flint_tuning* tuning, void* stream);
 
 /* flint_reactor_advance without any device allocation.  No counterpart in the
  * reference.  For callers that must not have a library call cudaMalloc: CFD
