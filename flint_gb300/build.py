@@ -15,7 +15,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_lib")
 BUILD = os.path.join(HERE, "_build")
 SOURCES = ["flint_abi.cu", "flint_kernels.cu", "flint_reactor.cu", "flint_table.cu", "flint_mlp.cu",
-           "flint_surrogate.cu", "flint_files.cu", "flint_ir.cu"]
+           "flint_surrogate.cu", "flint_files.cu", "flint_ir.cu", "flint_umma.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
          "-Xptxas", "-v"]

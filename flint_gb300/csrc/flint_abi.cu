@@ -822,6 +822,19 @@ int flint_surrogate_counts(flint_surrogate_t s, int64_t* counts) {
   return rc ? fail(rc, "flint_surrogate_counts: %s", cudaGetErrorString(cudaGetLastError())) : FLINT_OK;
 }
 
+int flint_surrogate_set_forward(flint_surrogate_t s, int mode, int* kind) {
+  if (!s) return fail(FLINT_ERR_ARG, "NULL handle");
+  if (surrogate_set_forward(s->s, mode)) return fail(FLINT_ERR_ARG, "forward mode %d (0 fused tcgen05, 1 mma.sync)", mode);
+  if (kind) *kind = surrogate_forward_kind(s->s);
+  return FLINT_OK;
+}
+
+int flint_surrogate_check(flint_surrogate_t s, int* err) {
+  if (!s || !err) return fail(FLINT_ERR_ARG, "NULL argument");
+  int rc = surrogate_check(s->s, err);
+  return rc ? cuda_fail(cudaGetLastError(), "flint_surrogate_check") : FLINT_OK;
+}
+
 int flint_surrogate_evaluate(flint_surrogate_t s, int64_t n, double* T, const double* p, double* Y,
                              const double* dt, const flint_surrogate_gate* gate, double* metrics, void* stream) {
   if (!s || !gate || !metrics) return fail(FLINT_ERR_ARG, "NULL argument");

@@ -101,6 +101,9 @@ int surrogate_advance(Surrogate* s, int64_t n, double* T, const double* p, doubl
                       double* jsave, int jslots, double* metrics, bool want_counts, cudaStream_t st,
                       int reactor_layout = REACTOR_LAYOUT_AUTO);
 void surrogate_counts(Surrogate* s, int64_t* acc, int64_t* rej);
+int surrogate_set_forward(Surrogate* s, int mode);
+int surrogate_forward_kind(Surrogate* s);
+int surrogate_check(Surrogate* s, int* err);
 int surrogate_read_counts(Surrogate* s, int64_t* acc, int64_t* rej);
 
 // tabulated (reference general-loop) path, flint_table.cu

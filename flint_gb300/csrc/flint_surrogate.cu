@@ -32,6 +32,7 @@
 
 #include "flint_host.h"
 #include "flint_mlp.h"
+#include "flint_umma.h"
 
 namespace flint {
 
@@ -47,6 +48,13 @@ struct Net {
   float *w = nullptr, *g = nullptr, *m1 = nullptr, *m2 = nullptr;
   __nv_bfloat16* wb = nullptr;
   int64_t step = 0;
+  // the fused tcgen05 inference forward (flint_umma.cu): packed BF16 hi/lo
+  // weights, refreshed from w whenever w changed
+  bool ufits = false, udirty = true;
+  UmmaNet u{};
+  uint8_t* upk = nullptr;
+  float* ubias = nullptr;
+  int64_t* uoff = nullptr;   // device: off_w[nl], off_b[nl]
 };
 
 struct Surrogate {
@@ -77,6 +85,8 @@ struct Surrogate {
   int *cst = nullptr, *cns = nullptr;
   int64_t last_accepted = 0, last_rejected = 0, last_fallback_steps = 0;
   int64_t last_n = 0;       // cells of the last advance (its rejected count stays on the device)
+  int fwd_mode = 0;         // 0: fused tcgen05 forward where it fits, 1: per-layer mma.sync GEMMs
+  int* uerr = nullptr;      // device word: a wait of the fused forward timed out
 };
 
 // ------------------------------------------------------------------ kernels
@@ -114,15 +124,22 @@ struct GateParams {
   double Tlo, Thi, lpl, lph, ldl, ldh;
 };
 
-// Post-processing and gate, one thread per cell.  Accepted cells are written
+// Post-processing and gate, one warp per cell.  Accepted cells are written
 // in place; rejected ones are listed for the fallback (their T, Y untouched).
+// Species k on lane k % 32 (slot k / 32): the per-cell arrays are registers,
+// the loads and stores of Y and of the network outputs are coalesced, and the
+// NASA-7 evaluations of the enthalpy Newton run across the lanes.  Sums are
+// warp butterflies (identical on every lane), so every decision is
+// warp-uniform; the small normal-equation solve of the projection runs
+// redundantly on all lanes.
+template <int SPL>
 __global__ void __launch_bounds__(SURR_THREADS)
-k_post(const uint8_t* __restrict__ img, ImageLayout L, int64_t n, int64_t base, double* __restrict__ T,
-       const double* __restrict__ p, double* __restrict__ Y, const double* __restrict__ dt,
-       const float* __restrict__ yn, const float* __restrict__ yn2, const float* __restrict__ ym,
-       const float* __restrict__ ys, const double* __restrict__ proj, const double* __restrict__ Bm, int ne,
-       GateParams gp, int* __restrict__ status, int* __restrict__ nsteps, int64_t* __restrict__ rej_idx,
-       unsigned long long* __restrict__ rej_count, double* __restrict__ metrics) {
+k_post_warp(const uint8_t* __restrict__ img, ImageLayout L, int64_t n, int64_t base, double* __restrict__ T,
+            const double* __restrict__ p, double* __restrict__ Y, const double* __restrict__ dt,
+            const float* __restrict__ yn, const float* __restrict__ yn2, const float* __restrict__ ym,
+            const float* __restrict__ ys, const double* __restrict__ Bm, int ne, GateParams gp,
+            int* __restrict__ status, int* __restrict__ nsteps, int64_t* __restrict__ rej_idx,
+            unsigned long long* __restrict__ rej_count, double* __restrict__ metrics) {
   extern __shared__ __align__(16) uint8_t smem[];
   stage_image(smem, img, L.bytes);
   MechView m;
@@ -131,55 +148,75 @@ k_post(const uint8_t* __restrict__ img, ImageLayout L, int64_t n, int64_t base, 
   double* sB = reinterpret_cast<double*>(smem + L.bytes);
   for (int i = threadIdx.x; i < ne * ns; i += blockDim.x) sB[i] = Bm[i];
   __syncthreads();
-  double dY[MAXS], Y1[MAXS];
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+  const int lane = threadIdx.x & 31;
+  const int64_t nwarps = (int64_t)gridDim.x * (blockDim.x >> 5);
+  for (int64_t i = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); i < n; i += nwarps) {
     const int64_t cell = base + i;
     const double T0 = T[cell], dti = dt[cell], pc = p[cell];
     bool ok = isfinite(T0) && isfinite(pc) && pc > 0.0 && isfinite(dti) && dti > 0.0;
     ok = ok && T0 >= gp.Tlo && T0 <= gp.Thi;
     const double lp = log10(pc), ld = log10(dti);
     ok = ok && lp >= gp.lpl && lp <= gp.lph && ld >= gp.ldl && ld <= gp.ldh;
-    double dTn = 0.0, ens = 0.0, ensT = 0.0;
-    for (int k = 0; k < ns; ++k) {
-      dY[k] = (double)ym[k] + (double)ys[k] * (double)yn[i * nout + k];
-      if (yn2) {
-        double d2 = (double)ym[k] + (double)ys[k] * (double)yn2[i * nout + k];
-        ens = fmax(ens, fabs(d2 - dY[k]));
-        dY[k] = 0.5 * (dY[k] + d2);
+    double dY[SPL], Y0[SPL], Y1[SPL];
+    bool fixedk[SPL];
+    double ensl = 0.0;
+#pragma unroll
+    for (int j = 0; j < SPL; ++j) {
+      const int k = lane + 32 * j;
+      dY[j] = 0.0; Y0[j] = 0.0; fixedk[j] = k >= ns;
+      if (k < ns) {
+        dY[j] = (double)ym[k] + (double)ys[k] * (double)yn[i * nout + k];
+        if (yn2) {
+          const double d2 = (double)ym[k] + (double)ys[k] * (double)yn2[i * nout + k];
+          ensl = fmax(ensl, fabs(d2 - dY[j]));
+          dY[j] = 0.5 * (dY[j] + d2);
+        }
+        Y0[j] = Y[cell * ns + k];
       }
+      Y1[j] = Y0[j] + dY[j];
     }
-    dTn = (double)ym[ns] + (double)ys[ns] * (double)yn[i * nout + ns];
+    const double ens = warp_max(ensl);
+    double dTn = (double)ym[ns] + (double)ys[ns] * (double)yn[i * nout + ns], ensT = 0.0;
     if (yn2) {
-      double d2 = (double)ym[ns] + (double)ys[ns] * (double)yn2[i * nout + ns];
+      const double d2 = (double)ym[ns] + (double)ys[ns] * (double)yn2[i * nout + ns];
       ensT = fabs(d2 - dTn);
       dTn = 0.5 * (dTn + d2);
     }
     // element residual of the raw prediction
     double er = 0.0;
     for (int e = 0; e < ne; ++e) {
-      double s = 0.0;
-      for (int k = 0; k < ns; ++k) s += sB[e * ns + k] * dY[k];
-      er = fmax(er, fabs(s));
+      double sl = 0.0;
+#pragma unroll
+      for (int j = 0; j < SPL; ++j) {
+        const int k = lane + 32 * j;
+        if (k < ns) sl += sB[e * ns + k] * dY[j];
+      }
+      er = fmax(er, fabs(warp_sum(sl)));
     }
     // conservative, non-negative mass fractions: project dY onto element
     // conservation over the free species, clip negatives to zero (they leave
     // the free set), repeat (active-set least-squares, at most NPASS passes;
     // the last pass clips nothing, so a result still negative there is rejected)
-    unsigned long long fixed = 0ull;   // bit k: species k clipped at zero
-    double clipped = 0.0;
-    for (int k = 0; k < ns; ++k) Y1[k] = Y[cell * ns + k] + dY[k];
+    double clippedl = 0.0;
     bool clean = false;
     for (int pass = 0; pass < NPASS && !clean; ++pass) {
       double r[8], G[8][8], lam[8];
       for (int e = 0; e < ne; ++e) {
-        double se = 0.0;
-        for (int k = 0; k < ns; ++k) se += sB[e * ns + k] * (Y1[k] - Y[cell * ns + k]);
-        r[e] = se;
-        for (int f = 0; f < ne; ++f) {
-          double g = 0.0;
-          for (int k = 0; k < ns; ++k)
-            if (!((fixed >> k) & 1ull)) g += sB[e * ns + k] * sB[f * ns + k];
-          G[e][f] = g;
+        double sl = 0.0;
+#pragma unroll
+        for (int j = 0; j < SPL; ++j) {
+          const int k = lane + 32 * j;
+          if (k < ns) sl += sB[e * ns + k] * (Y1[j] - Y0[j]);
+        }
+        r[e] = warp_sum(sl);
+        for (int f = e; f < ne; ++f) {
+          double gl = 0.0;
+#pragma unroll
+          for (int j = 0; j < SPL; ++j) {
+            const int k = lane + 32 * j;
+            if (!fixedk[j]) gl += sB[e * ns + k] * sB[f * ns + k];
+          }
+          G[e][f] = G[f][e] = warp_sum(gl);
         }
       }
       // solve G lam = r (Gauss-Jordan, partial pivoting; empty rows get lam = 0)
@@ -205,43 +242,57 @@ k_post(const uint8_t* __restrict__ img, ImageLayout L, int64_t n, int64_t base, 
         }
       }
       for (int e = 0; e < ne; ++e) if (!live[e]) lam[e] = 0.0;
-      clean = true;
-      for (int k = 0; k < ns; ++k) {
-        if ((fixed >> k) & 1ull) continue;
+      bool clip = false;
+#pragma unroll
+      for (int j = 0; j < SPL; ++j) {
+        const int k = lane + 32 * j;
+        if (fixedk[j]) continue;
         double corr = 0.0;
         for (int e = 0; e < ne; ++e) corr += sB[e * ns + k] * lam[e];
-        Y1[k] -= corr;
-        if (Y1[k] < 0.0 && pass < NPASS - 1) {
-          clipped += -Y1[k];
-          Y1[k] = 0.0;
-          fixed |= 1ull << k;
-          clean = false;
+        Y1[j] -= corr;
+        if (Y1[j] < 0.0 && pass < NPASS - 1) {
+          clippedl += -Y1[j];
+          Y1[j] = 0.0;
+          fixedk[j] = true;
+          clip = true;
         }
       }
+      clean = !__any_sync(FULL, clip);
     }
-    double ymin = 1.0;
-    for (int k = 0; k < ns; ++k) ymin = fmin(ymin, Y1[k]);
+    double yminl = 1.0;
+#pragma unroll
+    for (int j = 0; j < SPL; ++j)
+      if (lane + 32 * j < ns) yminl = fmin(yminl, Y1[j]);
+    const double ymin = -warp_max(-yminl);
     // realizability measure reported to the gate: clipped mass (negative) or
     // the most negative mass fraction left
-    const double yreal = fmin(-clipped, ymin);
+    const double yreal = fmin(-warp_sum(clippedl), ymin);
     // energy: h(T1, Y1) = h(T0, Y0), Newton from the network's temperature
-    double h0 = 0.0;
+    double h0l = 0.0;
     {
       const double lnT = log(T0), invT = 1.0 / T0;
-      for (int k = 0; k < ns; ++k) h0 += Y[cell * ns + k] * nasa7(m, k, T0, lnT, invT).hRT * m.invmw[k];
-      h0 *= T0;
+#pragma unroll
+      for (int j = 0; j < SPL; ++j) {
+        const int k = lane + 32 * j;
+        if (k < ns) h0l += Y0[j] * nasa7(m, k, T0, lnT, invT).hRT * m.invmw[k];
+      }
     }
+    const double h0 = warp_sum(h0l) * T0;
     double T1 = T0 + dTn;
     bool conv = isfinite(T1) && T1 > 200.0 && T1 < 6000.0;
     for (int it = 0; it < 8 && conv; ++it) {
       const double lnT = log(T1), invT = 1.0 / T1;
-      double h = 0.0, cpm = 0.0;
-      for (int k = 0; k < ns; ++k) {
-        SpThermo th = nasa7(m, k, T1, lnT, invT);
-        h += Y1[k] * th.hRT * m.invmw[k];
-        cpm += Y1[k] * th.cpR * m.invmw[k];
+      double hl = 0.0, cl = 0.0;
+#pragma unroll
+      for (int j = 0; j < SPL; ++j) {
+        const int k = lane + 32 * j;
+        if (k < ns) {
+          SpThermo th = nasa7(m, k, T1, lnT, invT);
+          hl += Y1[j] * th.hRT * m.invmw[k];
+          cl += Y1[j] * th.cpR * m.invmw[k];
+        }
       }
-      const double dT = (h * T1 - h0) / cpm;
+      const double dT = (warp_sum(hl) * T1 - h0) / warp_sum(cl);
       T1 -= dT;
       if (!(T1 > 200.0 && T1 < 6000.0)) conv = false;
       if (fabs(dT) < 1e-10 * T1) break;
@@ -250,24 +301,33 @@ k_post(const uint8_t* __restrict__ img, ImageLayout L, int64_t n, int64_t base, 
     if (metrics) {
       // evaluation mode: every cell takes the surrogate result, the gate
       // quantities are reported instead of applied
-      double* mt = metrics + i * 6;
-      mt[0] = dTres; mt[1] = er; mt[2] = yreal; mt[3] = ensT; mt[4] = ens;
-      mt[5] = (ok && ymin >= 0.0) ? 1.0 : 0.0;   // the gate's fixed conditions
-      for (int k = 0; k < ns; ++k) Y[cell * ns + k] = Y1[k];
-      T[cell] = conv ? T1 : T0 + dTn;
+      if (lane == 0) {
+        double* mt = metrics + i * 6;
+        mt[0] = dTres; mt[1] = er; mt[2] = yreal; mt[3] = ensT; mt[4] = ens;
+        mt[5] = (ok && ymin >= 0.0) ? 1.0 : 0.0;   // the gate's fixed conditions
+        T[cell] = conv ? T1 : T0 + dTn;
+      }
+#pragma unroll
+      for (int j = 0; j < SPL; ++j)
+        if (lane + 32 * j < ns) Y[cell * ns + lane + 32 * j] = Y1[j];
       continue;
     }
     ok = ok && conv && dTres <= gp.max_dT_resid && er <= gp.max_elem_resid && yreal >= gp.min_Y && ymin >= 0.0;
     if (yn2) ok = ok && ensT <= gp.max_ens_dT && ens <= gp.max_ens_dY;
     if (ok) {
-      for (int k = 0; k < ns; ++k) Y[cell * ns + k] = Y1[k];
-      T[cell] = T1;
-      if (status) status[cell] = FLINT_CELL_OK;
-      if (nsteps) nsteps[cell] = 0;
-    } else {
+#pragma unroll
+      for (int j = 0; j < SPL; ++j)
+        if (lane + 32 * j < ns) Y[cell * ns + lane + 32 * j] = Y1[j];
+      if (lane == 0) {
+        T[cell] = T1;
+        if (status) status[cell] = FLINT_CELL_OK;
+        if (nsteps) nsteps[cell] = 0;
+      }
+    } else if (lane == 0) {
       unsigned long long slot = atomicAdd(rej_count, 1ull);
       rej_idx[slot] = cell;
     }
+    __syncwarp();
   }
 }
 
@@ -306,6 +366,14 @@ static int blocks_for(int64_t n, int threads) {
 static cudaError_t net_forward(Surrogate* s, Net& nt, int64_t n, const float* X, float* out, bool keep,
                                cudaStream_t st) {
   cudaError_t e = cudaSuccess;
+  if (!keep && s->fwd_mode == 0 && nt.ufits) {
+    if (nt.udirty) {
+      e = umma_pack(nt.u, nt.w, nt.uoff, nt.uoff + nt.nl, nt.upk, nt.ubias, st);
+      if (e) return e;
+      nt.udirty = false;
+    }
+    return launch_mlp_umma(nt.u, nt.upk, nt.ubias, n, X, out, s->uerr, st);
+  }
   for (int l = 0; l < nt.nl && !e; ++l) {
     GemmArgs g{};
     g.M = (int)n; g.N = nt.dims[l + 1]; g.K = nt.dims[l];
@@ -379,6 +447,7 @@ static int alloc_fb(Surrogate* s, int64_t n) {
 
 static void net_free(Net& nt) {
   cudaFree(nt.w); cudaFree(nt.g); cudaFree(nt.m1); cudaFree(nt.m2); cudaFree(nt.wb);
+  cudaFree(nt.upk); cudaFree(nt.ubias); cudaFree(nt.uoff);
   nt = Net();
 }
 
@@ -389,7 +458,7 @@ void surrogate_free(Surrogate* s) {
   for (int l = 0; l < MAXL; ++l) { fr(s->Z[l]); fr(s->A[l]); }
   fr(s->dz0); fr(s->dz1); fr(s->yhat); fr(s->xf); fr(s->yout2); fr(s->rej_idx); fr(s->rej_count);
   fr(s->cT); fr(s->cp); fr(s->cY); fr(s->cdt); fr(s->cst); fr(s->cns); fr(s->loss);
-  fr(s->xmean); fr(s->xstd); fr(s->ymean); fr(s->ystd); fr(s->proj); fr(s->Bm);
+  fr(s->xmean); fr(s->xstd); fr(s->ymean); fr(s->ystd); fr(s->proj); fr(s->Bm); fr(s->uerr);
   delete s;
 }
 
@@ -412,6 +481,17 @@ static int net_init(Net& nt, int nl, const int* dims, const float* w0) {
   if (!e) e = cudaMemset(nt.m1, 0, off * sizeof(float));
   if (!e) e = cudaMemset(nt.m2, 0, off * sizeof(float));
   if (!e) e = launch_to_bf16(nt.w, nt.wb, off, nullptr);
+  nt.ufits = umma_fits(nl, dims);
+  if (!e && nt.ufits) {
+    const int64_t bytes = umma_describe(nl, dims, &nt.u);
+    std::vector<int64_t> offs(2 * nl);
+    for (int l = 0; l < nl; ++l) { offs[l] = nt.off_w[l]; offs[nl + l] = nt.off_b[l]; }
+    e = cudaMalloc(&nt.upk, bytes);
+    if (!e) e = cudaMalloc(&nt.ubias, (size_t)nl * 256 * sizeof(float));
+    if (!e) e = cudaMalloc(&nt.uoff, offs.size() * sizeof(int64_t));
+    if (!e) e = cudaMemcpy(nt.uoff, offs.data(), offs.size() * sizeof(int64_t), cudaMemcpyHostToDevice);
+    nt.udirty = true;
+  }
   if (!e) e = cudaDeviceSynchronize();
   return e ? FLINT_ERR_CUDA : 0;
 }
@@ -482,6 +562,8 @@ int surrogate_create(const uint8_t* mimg, const ImageLayout& L, unsigned int* co
   if (!e) e = cudaMalloc(&s->Bm, std::max(ne, 1) * ns * 8);
   if (!e) e = cudaMalloc(&s->loss, 8);
   if (!e) e = cudaMalloc(&s->rej_count, 8);
+  if (!e) e = cudaMalloc(&s->uerr, sizeof(int));
+  if (!e) e = cudaMemset(s->uerr, 0, sizeof(int));
   if (!e) e = cudaMemcpy(s->xmean, d->x_mean, s->n_in * 4, cudaMemcpyHostToDevice);
   if (!e) e = cudaMemcpy(s->xstd, d->x_std, s->n_in * 4, cudaMemcpyHostToDevice);
   if (!e) e = cudaMemcpy(s->ymean, d->y_mean, s->n_out * 4, cudaMemcpyHostToDevice);
@@ -555,6 +637,7 @@ int surrogate_train_step(Surrogate* s, int net, int64_t n, const float* X, const
   const float b1 = 0.9f, b2 = 0.999f;
   const float bc1 = 1.f - powf(b1, (float)nt.step), bc2 = 1.f - powf(b2, (float)nt.step);
   if (launch_adam(nt.w, nt.g, nt.m1, nt.m2, nt.wb, nt.P, lr, b1, b2, 1e-8f, bc1, bc2, 0.f, st)) return FLINT_ERR_CUDA;
+  nt.udirty = true;
   if (loss_out) {
     if (cudaMemcpyAsync(loss_out, s->loss, 8, cudaMemcpyDeviceToHost, st)) return FLINT_ERR_CUDA;
     if (cudaStreamSynchronize(st)) return FLINT_ERR_CUDA;
@@ -578,6 +661,7 @@ int surrogate_state(Surrogate* s, int net, float* host, int64_t* step, int get) 
     if (!e) e = cudaMemcpy(nt.m2, host + 2 * P, P * 4, cudaMemcpyHostToDevice);
     if (!e) e = launch_to_bf16(nt.w, nt.wb, P, nullptr);
     if (!e) e = cudaDeviceSynchronize();
+    nt.udirty = true;
     if (step) nt.step = *step;
   }
   return e ? FLINT_ERR_CUDA : 0;
@@ -604,16 +688,27 @@ int surrogate_advance(Surrogate* s, int64_t n, double* T, const double* p, doubl
   gp.Tlo = gate->T_lo; gp.Thi = gate->T_hi; gp.lpl = gate->log10p_lo; gp.lph = gate->log10p_hi;
   gp.ldl = gate->log10dt_lo; gp.ldh = gate->log10dt_hi;
   const size_t psm = s->L.bytes + (size_t)(std::max(s->ne, 1) * s->ns) * sizeof(double);
-  if (set_smem((const void*)k_post, psm)) return FLINT_ERR_CUDA;
+  const bool two = s->L.nsp > 32;
+  const void* post_fn = two ? (const void*)k_post_warp<2> : (const void*)k_post_warp<1>;
+  if (set_smem(post_fn, psm)) return FLINT_ERR_CUDA;
   if (cudaMemsetAsync(s->rej_count, 0, 8, st)) return FLINT_ERR_CUDA;
   for (int64_t b = 0; b < n; b += s->cap) {
     const int64_t m = std::min<int64_t>(s->cap, n - b);
     if (surrogate_features(s, m, T + b, p + b, Y + b * s->ns, dt + b, s->xf, st)) return FLINT_ERR_CUDA;
     if (net_forward(s, s->net[0], m, s->xf, s->yhat, false, st)) return FLINT_ERR_CUDA;
     if (s->nnets > 1 && net_forward(s, s->net[1], m, s->xf, s->yout2, false, st)) return FLINT_ERR_CUDA;
-    k_post<<<blocks_for(m, SURR_THREADS), SURR_THREADS, psm, st>>>(
-        s->mimg, s->L, m, b, T, p, Y, dt, s->yhat, s->nnets > 1 ? s->yout2 : nullptr, s->ymean, s->ystd, s->proj,
-        s->Bm, s->ne, gp, status, nsteps, s->rej_idx, s->rej_count, metrics ? metrics + b * 6 : nullptr);
+    const unsigned pb = (unsigned)std::min<int64_t>((m + SURR_THREADS / 32 - 1) / (SURR_THREADS / 32),
+                                                    (int64_t)device_sms() * 16);
+    if (two)
+      k_post_warp<2><<<pb, SURR_THREADS, psm, st>>>(s->mimg, s->L, m, b, T, p, Y, dt, s->yhat,
+                                                    s->nnets > 1 ? s->yout2 : nullptr, s->ymean, s->ystd, s->Bm,
+                                                    s->ne, gp, status, nsteps, s->rej_idx, s->rej_count,
+                                                    metrics ? metrics + b * 6 : nullptr);
+    else
+      k_post_warp<1><<<pb, SURR_THREADS, psm, st>>>(s->mimg, s->L, m, b, T, p, Y, dt, s->yhat,
+                                                    s->nnets > 1 ? s->yout2 : nullptr, s->ymean, s->ystd, s->Bm,
+                                                    s->ne, gp, status, nsteps, s->rej_idx, s->rej_count,
+                                                    metrics ? metrics + b * 6 : nullptr);
     count_launch();
     if (cudaGetLastError()) return FLINT_ERR_CUDA;
   }
@@ -637,6 +732,20 @@ int surrogate_advance(Surrogate* s, int64_t n, double* T, const double* p, doubl
   s->last_rejected = (int64_t)nrej;
   s->last_accepted = n - (int64_t)nrej;
   return 0;
+}
+
+int surrogate_set_forward(Surrogate* s, int mode) {
+  if (mode != 0 && mode != 1) return FLINT_ERR_ARG;
+  s->fwd_mode = mode;
+  return 0;
+}
+
+int surrogate_forward_kind(Surrogate* s) { return s->fwd_mode == 0 && s->net[0].ufits ? 0 : 1; }
+
+// The fused forward's error word (waits for the device); 0 when no wait of it timed out.
+int surrogate_check(Surrogate* s, int* err) {
+  if (cudaDeviceSynchronize() != cudaSuccess) return FLINT_ERR_CUDA;
+  return cudaMemcpy(err, s->uerr, sizeof(int), cudaMemcpyDeviceToHost) == cudaSuccess ? 0 : FLINT_ERR_CUDA;
 }
 
 void surrogate_counts(Surrogate* s, int64_t* acc, int64_t* rej) { *acc = s->last_accepted; *rej = s->last_rejected; }

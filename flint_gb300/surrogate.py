@@ -70,6 +70,8 @@ def _bind(L):
                                           C.POINTER(SurrogateGate), vp, vp, C.POINTER(C.c_int64), vp]
     L.flint_surrogate_counts.argtypes = [vp, C.POINTER(C.c_int64)]
     L.flint_surrogate_evaluate.argtypes = [vp, i64, vp, vp, vp, vp, C.POINTER(SurrogateGate), vp, vp]
+    L.flint_surrogate_set_forward.argtypes = [vp, C.c_int, C.POINTER(C.c_int)]
+    L.flint_surrogate_check.argtypes = [vp, C.POINTER(C.c_int)]
     L._surrogate_bound = True
 
 
@@ -221,6 +223,20 @@ class Surrogate:
         native.check(self.L.flint_surrogate_predict(self.h, net, X.shape[0], _ptr(X), _ptr(Yn), _stream()),
                      "flint_surrogate_predict")
         return Yn
+
+    def set_forward(self, mode):
+        """0: the fused tcgen05 inference kernel where the network fits it (the
+        default); 1: one mma.sync GEMM launch per layer.  Returns what runs
+        (0 fused, 1 per-layer)."""
+        kind = C.c_int(-1)
+        native.check(self.L.flint_surrogate_set_forward(self.h, int(mode), C.byref(kind)), "flint_surrogate_set_forward")
+        return kind.value
+
+    def check(self):
+        """The fused forward's error word (0: every bounded wait completed); waits for the device."""
+        e = C.c_int(0)
+        native.check(self.L.flint_surrogate_check(self.h, C.byref(e)), "flint_surrogate_check")
+        return e.value
 
     def get_state(self, net=0):
         buf = np.zeros(3 * self.P, dtype=np.float32)

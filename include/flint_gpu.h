@@ -452,6 +452,19 @@ int flint_surrogate_advance(flint_surrogate_t s, int64_t n, double* T, const dou
  * as replays of a captured CUDA graph).  No reference counterpart. */
 int flint_surrogate_counts(flint_surrogate_t s, int64_t* counts);
 
+/* Which implementation runs the networks' inference forward: 0 (default) the
+ * fused Blackwell kernel -- all layers of a 128-cell tile on one SM,
+ * tcgen05.mma with the accumulator in tensor memory, weights streamed from
+ * L2 by bulk copies -- wherever the network fits it (hidden layers of 256,
+ * inputs and outputs of up to 64); 1 one mma.sync GEMM launch per layer
+ * (always; training uses it).  *kind (may be NULL) reports what mode 0/1
+ * resolves to for this network (0 fused, 1 per-layer).  No reference
+ * counterpart. */
+int flint_surrogate_set_forward(flint_surrogate_t s, int mode, int* kind);
+/* Waits for the device and reads the fused forward's error word: *err != 0
+ * when one of its bounded waits gave up (the outputs of that call are not
+ * valid).  No reference counterpart. */
+int flint_surrogate_check(flint_surrogate_t s, int* err);
 /* Apply the surrogate to every cell (no gate, no fallback; T, Y in place) and
  * write the gate quantities per cell, metrics[cell][6] = {energy residual [K],
  * element residual, realizability (the smaller of -(clipped mass) and the
