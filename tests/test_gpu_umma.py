@@ -100,4 +100,6 @@ def test_shipped_checkpoint_same_advance():
     assert same.mean() > 0.999, same.mean()      # a cell at the gate's edge may flip
     assert abs(na - nb) <= 16
     both = same & (sa == 0)
-    assert np.abs(Ta - Tb)[both].max() < 1e-3 and np.abs(Ya - Yb)[both].max() < 1e-6
+    # the two forwards differ by ~1e-5 of the outputs' normalisation spread
+    # (about 100 K for dT): far inside 1 % of the surrogate's targets
+    assert np.abs(Ta - Tb)[both].max() < 1e-2 and np.abs(Ya - Yb)[both].max() < 1e-6
