@@ -124,22 +124,15 @@ struct GateParams {
   double Tlo, Thi, lpl, lph, ldl, ldh;
 };
 
-// Post-processing and gate, one warp per cell.  Accepted cells are written
+// Post-processing and gate, one thread per cell.  Accepted cells are written
 // in place; rejected ones are listed for the fallback (their T, Y untouched).
-// Species k on lane k % 32 (slot k / 32): the per-cell arrays are registers,
-// the loads and stores of Y and of the network outputs are coalesced, and the
-// NASA-7 evaluations of the enthalpy Newton run across the lanes.  Sums are
-// warp butterflies (identical on every lane), so every decision is
-// warp-uniform; the small normal-equation solve of the projection runs
-// redundantly on all lanes.
-template <int SPL>
 __global__ void __launch_bounds__(SURR_THREADS)
-k_post_warp(const uint8_t* __restrict__ img, ImageLayout L, int64_t n, int64_t base, double* __restrict__ T,
-            const double* __restrict__ p, double* __restrict__ Y, const double* __restrict__ dt,
-            const float* __restrict__ yn, const float* __restrict__ yn2, const float* __restrict__ ym,
-            const float* __restrict__ ys, const double* __restrict__ Bm, int ne, GateParams gp,
-            int* __restrict__ status, int* __restrict__ nsteps, int64_t* __restrict__ rej_idx,
-            unsigned long long* __restrict__ rej_count, double* __restrict__ metrics) {
+k_post(const uint8_t* __restrict__ img, ImageLayout L, int64_t n, int64_t base, double* __restrict__ T,
+       const double* __restrict__ p, double* __restrict__ Y, const double* __restrict__ dt,
+       const float* __restrict__ yn, const float* __restrict__ yn2, const float* __restrict__ ym,
+       const float* __restrict__ ys, const double* __restrict__ proj, const double* __restrict__ Bm, int ne,
+       GateParams gp, int* __restrict__ status, int* __restrict__ nsteps, int64_t* __restrict__ rej_idx,
+       unsigned long long* __restrict__ rej_count, double* __restrict__ metrics) {
   extern __shared__ __align__(16) uint8_t smem[];
   stage_image(smem, img, L.bytes);
   MechView m;
@@ -148,75 +141,55 @@ k_post_warp(const uint8_t* __restrict__ img, ImageLayout L, int64_t n, int64_t b
   double* sB = reinterpret_cast<double*>(smem + L.bytes);
   for (int i = threadIdx.x; i < ne * ns; i += blockDim.x) sB[i] = Bm[i];
   __syncthreads();
-  const int lane = threadIdx.x & 31;
-  const int64_t nwarps = (int64_t)gridDim.x * (blockDim.x >> 5);
-  for (int64_t i = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); i < n; i += nwarps) {
+  double dY[MAXS], Y1[MAXS];
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     const int64_t cell = base + i;
     const double T0 = T[cell], dti = dt[cell], pc = p[cell];
     bool ok = isfinite(T0) && isfinite(pc) && pc > 0.0 && isfinite(dti) && dti > 0.0;
     ok = ok && T0 >= gp.Tlo && T0 <= gp.Thi;
     const double lp = log10(pc), ld = log10(dti);
     ok = ok && lp >= gp.lpl && lp <= gp.lph && ld >= gp.ldl && ld <= gp.ldh;
-    double dY[SPL], Y0[SPL], Y1[SPL];
-    bool fixedk[SPL];
-    double ensl = 0.0;
-#pragma unroll
-    for (int j = 0; j < SPL; ++j) {
-      const int k = lane + 32 * j;
-      dY[j] = 0.0; Y0[j] = 0.0; fixedk[j] = k >= ns;
-      if (k < ns) {
-        dY[j] = (double)ym[k] + (double)ys[k] * (double)yn[i * nout + k];
-        if (yn2) {
-          const double d2 = (double)ym[k] + (double)ys[k] * (double)yn2[i * nout + k];
-          ensl = fmax(ensl, fabs(d2 - dY[j]));
-          dY[j] = 0.5 * (dY[j] + d2);
-        }
-        Y0[j] = Y[cell * ns + k];
+    double dTn = 0.0, ens = 0.0, ensT = 0.0;
+    for (int k = 0; k < ns; ++k) {
+      dY[k] = (double)ym[k] + (double)ys[k] * (double)yn[i * nout + k];
+      if (yn2) {
+        double d2 = (double)ym[k] + (double)ys[k] * (double)yn2[i * nout + k];
+        ens = fmax(ens, fabs(d2 - dY[k]));
+        dY[k] = 0.5 * (dY[k] + d2);
       }
-      Y1[j] = Y0[j] + dY[j];
     }
-    const double ens = warp_max(ensl);
-    double dTn = (double)ym[ns] + (double)ys[ns] * (double)yn[i * nout + ns], ensT = 0.0;
+    dTn = (double)ym[ns] + (double)ys[ns] * (double)yn[i * nout + ns];
     if (yn2) {
-      const double d2 = (double)ym[ns] + (double)ys[ns] * (double)yn2[i * nout + ns];
+      double d2 = (double)ym[ns] + (double)ys[ns] * (double)yn2[i * nout + ns];
       ensT = fabs(d2 - dTn);
       dTn = 0.5 * (dTn + d2);
     }
     // element residual of the raw prediction
     double er = 0.0;
     for (int e = 0; e < ne; ++e) {
-      double sl = 0.0;
-#pragma unroll
-      for (int j = 0; j < SPL; ++j) {
-        const int k = lane + 32 * j;
-        if (k < ns) sl += sB[e * ns + k] * dY[j];
-      }
-      er = fmax(er, fabs(warp_sum(sl)));
+      double s = 0.0;
+      for (int k = 0; k < ns; ++k) s += sB[e * ns + k] * dY[k];
+      er = fmax(er, fabs(s));
     }
     // conservative, non-negative mass fractions: project dY onto element
     // conservation over the free species, clip negatives to zero (they leave
     // the free set), repeat (active-set least-squares, at most NPASS passes;
     // the last pass clips nothing, so a result still negative there is rejected)
-    double clippedl = 0.0;
+    unsigned long long fixed = 0ull;   // bit k: species k clipped at zero
+    double clipped = 0.0;
+    for (int k = 0; k < ns; ++k) Y1[k] = Y[cell * ns + k] + dY[k];
     bool clean = false;
     for (int pass = 0; pass < NPASS && !clean; ++pass) {
       double r[8], G[8][8], lam[8];
       for (int e = 0; e < ne; ++e) {
-        double sl = 0.0;
-#pragma unroll
-        for (int j = 0; j < SPL; ++j) {
-          const int k = lane + 32 * j;
-          if (k < ns) sl += sB[e * ns + k] * (Y1[j] - Y0[j]);
-        }
-        r[e] = warp_sum(sl);
-        for (int f = e; f < ne; ++f) {
-          double gl = 0.0;
-#pragma unroll
-          for (int j = 0; j < SPL; ++j) {
-            const int k = lane + 32 * j;
-            if (!fixedk[j]) gl += sB[e * ns + k] * sB[f * ns + k];
-          }
-          G[e][f] = G[f][e] = warp_sum(gl);
+        double se = 0.0;
+        for (int k = 0; k < ns; ++k) se += sB[e * ns + k] * (Y1[k] - Y[cell * ns + k]);
+        r[e] = se;
+        for (int f = 0; f < ne; ++f) {
+          double g = 0.0;
+          for (int k = 0; k < ns; ++k)
+            if (!((fixed >> k) & 1ull)) g += sB[e * ns + k] * sB[f * ns + k];
+          G[e][f] = g;
         }
       }
       // solve G lam = r (Gauss-Jordan, partial pivoting; empty rows get lam = 0)
@@ -242,57 +215,43 @@ k_post_warp(const uint8_t* __restrict__ img, ImageLayout L, int64_t n, int64_t b
         }
       }
       for (int e = 0; e < ne; ++e) if (!live[e]) lam[e] = 0.0;
-      bool clip = false;
-#pragma unroll
-      for (int j = 0; j < SPL; ++j) {
-        const int k = lane + 32 * j;
-        if (fixedk[j]) continue;
+      clean = true;
+      for (int k = 0; k < ns; ++k) {
+        if ((fixed >> k) & 1ull) continue;
         double corr = 0.0;
         for (int e = 0; e < ne; ++e) corr += sB[e * ns + k] * lam[e];
-        Y1[j] -= corr;
-        if (Y1[j] < 0.0 && pass < NPASS - 1) {
-          clippedl += -Y1[j];
-          Y1[j] = 0.0;
-          fixedk[j] = true;
-          clip = true;
+        Y1[k] -= corr;
+        if (Y1[k] < 0.0 && pass < NPASS - 1) {
+          clipped += -Y1[k];
+          Y1[k] = 0.0;
+          fixed |= 1ull << k;
+          clean = false;
         }
       }
-      clean = !__any_sync(FULL, clip);
     }
-    double yminl = 1.0;
-#pragma unroll
-    for (int j = 0; j < SPL; ++j)
-      if (lane + 32 * j < ns) yminl = fmin(yminl, Y1[j]);
-    const double ymin = -warp_max(-yminl);
+    double ymin = 1.0;
+    for (int k = 0; k < ns; ++k) ymin = fmin(ymin, Y1[k]);
     // realizability measure reported to the gate: clipped mass (negative) or
     // the most negative mass fraction left
-    const double yreal = fmin(-warp_sum(clippedl), ymin);
+    const double yreal = fmin(-clipped, ymin);
     // energy: h(T1, Y1) = h(T0, Y0), Newton from the network's temperature
-    double h0l = 0.0;
+    double h0 = 0.0;
     {
       const double lnT = log(T0), invT = 1.0 / T0;
-#pragma unroll
-      for (int j = 0; j < SPL; ++j) {
-        const int k = lane + 32 * j;
-        if (k < ns) h0l += Y0[j] * nasa7(m, k, T0, lnT, invT).hRT * m.invmw[k];
-      }
+      for (int k = 0; k < ns; ++k) h0 += Y[cell * ns + k] * nasa7(m, k, T0, lnT, invT).hRT * m.invmw[k];
+      h0 *= T0;
     }
-    const double h0 = warp_sum(h0l) * T0;
     double T1 = T0 + dTn;
     bool conv = isfinite(T1) && T1 > 200.0 && T1 < 6000.0;
     for (int it = 0; it < 8 && conv; ++it) {
       const double lnT = log(T1), invT = 1.0 / T1;
-      double hl = 0.0, cl = 0.0;
-#pragma unroll
-      for (int j = 0; j < SPL; ++j) {
-        const int k = lane + 32 * j;
-        if (k < ns) {
-          SpThermo th = nasa7(m, k, T1, lnT, invT);
-          hl += Y1[j] * th.hRT * m.invmw[k];
-          cl += Y1[j] * th.cpR * m.invmw[k];
-        }
+      double h = 0.0, cpm = 0.0;
+      for (int k = 0; k < ns; ++k) {
+        SpThermo th = nasa7(m, k, T1, lnT, invT);
+        h += Y1[k] * th.hRT * m.invmw[k];
+        cpm += Y1[k] * th.cpR * m.invmw[k];
       }
-      const double dT = (warp_sum(hl) * T1 - h0) / warp_sum(cl);
+      const double dT = (h * T1 - h0) / cpm;
       T1 -= dT;
       if (!(T1 > 200.0 && T1 < 6000.0)) conv = false;
       if (fabs(dT) < 1e-10 * T1) break;
@@ -301,33 +260,24 @@ k_post_warp(const uint8_t* __restrict__ img, ImageLayout L, int64_t n, int64_t b
     if (metrics) {
       // evaluation mode: every cell takes the surrogate result, the gate
       // quantities are reported instead of applied
-      if (lane == 0) {
-        double* mt = metrics + i * 6;
-        mt[0] = dTres; mt[1] = er; mt[2] = yreal; mt[3] = ensT; mt[4] = ens;
-        mt[5] = (ok && ymin >= 0.0) ? 1.0 : 0.0;   // the gate's fixed conditions
-        T[cell] = conv ? T1 : T0 + dTn;
-      }
-#pragma unroll
-      for (int j = 0; j < SPL; ++j)
-        if (lane + 32 * j < ns) Y[cell * ns + lane + 32 * j] = Y1[j];
+      double* mt = metrics + i * 6;
+      mt[0] = dTres; mt[1] = er; mt[2] = yreal; mt[3] = ensT; mt[4] = ens;
+      mt[5] = (ok && ymin >= 0.0) ? 1.0 : 0.0;   // the gate's fixed conditions
+      for (int k = 0; k < ns; ++k) Y[cell * ns + k] = Y1[k];
+      T[cell] = conv ? T1 : T0 + dTn;
       continue;
     }
     ok = ok && conv && dTres <= gp.max_dT_resid && er <= gp.max_elem_resid && yreal >= gp.min_Y && ymin >= 0.0;
     if (yn2) ok = ok && ensT <= gp.max_ens_dT && ens <= gp.max_ens_dY;
     if (ok) {
-#pragma unroll
-      for (int j = 0; j < SPL; ++j)
-        if (lane + 32 * j < ns) Y[cell * ns + lane + 32 * j] = Y1[j];
-      if (lane == 0) {
-        T[cell] = T1;
-        if (status) status[cell] = FLINT_CELL_OK;
-        if (nsteps) nsteps[cell] = 0;
-      }
-    } else if (lane == 0) {
+      for (int k = 0; k < ns; ++k) Y[cell * ns + k] = Y1[k];
+      T[cell] = T1;
+      if (status) status[cell] = FLINT_CELL_OK;
+      if (nsteps) nsteps[cell] = 0;
+    } else {
       unsigned long long slot = atomicAdd(rej_count, 1ull);
       rej_idx[slot] = cell;
     }
-    __syncwarp();
   }
 }
 
@@ -688,27 +638,16 @@ int surrogate_advance(Surrogate* s, int64_t n, double* T, const double* p, doubl
   gp.Tlo = gate->T_lo; gp.Thi = gate->T_hi; gp.lpl = gate->log10p_lo; gp.lph = gate->log10p_hi;
   gp.ldl = gate->log10dt_lo; gp.ldh = gate->log10dt_hi;
   const size_t psm = s->L.bytes + (size_t)(std::max(s->ne, 1) * s->ns) * sizeof(double);
-  const bool two = s->L.nsp > 32;
-  const void* post_fn = two ? (const void*)k_post_warp<2> : (const void*)k_post_warp<1>;
-  if (set_smem(post_fn, psm)) return FLINT_ERR_CUDA;
+  if (set_smem((const void*)k_post, psm)) return FLINT_ERR_CUDA;
   if (cudaMemsetAsync(s->rej_count, 0, 8, st)) return FLINT_ERR_CUDA;
   for (int64_t b = 0; b < n; b += s->cap) {
     const int64_t m = std::min<int64_t>(s->cap, n - b);
     if (surrogate_features(s, m, T + b, p + b, Y + b * s->ns, dt + b, s->xf, st)) return FLINT_ERR_CUDA;
     if (net_forward(s, s->net[0], m, s->xf, s->yhat, false, st)) return FLINT_ERR_CUDA;
     if (s->nnets > 1 && net_forward(s, s->net[1], m, s->xf, s->yout2, false, st)) return FLINT_ERR_CUDA;
-    const unsigned pb = (unsigned)std::min<int64_t>((m + SURR_THREADS / 32 - 1) / (SURR_THREADS / 32),
-                                                    (int64_t)device_sms() * 16);
-    if (two)
-      k_post_warp<2><<<pb, SURR_THREADS, psm, st>>>(s->mimg, s->L, m, b, T, p, Y, dt, s->yhat,
-                                                    s->nnets > 1 ? s->yout2 : nullptr, s->ymean, s->ystd, s->Bm,
-                                                    s->ne, gp, status, nsteps, s->rej_idx, s->rej_count,
-                                                    metrics ? metrics + b * 6 : nullptr);
-    else
-      k_post_warp<1><<<pb, SURR_THREADS, psm, st>>>(s->mimg, s->L, m, b, T, p, Y, dt, s->yhat,
-                                                    s->nnets > 1 ? s->yout2 : nullptr, s->ymean, s->ystd, s->Bm,
-                                                    s->ne, gp, status, nsteps, s->rej_idx, s->rej_count,
-                                                    metrics ? metrics + b * 6 : nullptr);
+    k_post<<<blocks_for(m, SURR_THREADS), SURR_THREADS, psm, st>>>(
+        s->mimg, s->L, m, b, T, p, Y, dt, s->yhat, s->nnets > 1 ? s->yout2 : nullptr, s->ymean, s->ystd, s->proj,
+        s->Bm, s->ne, gp, status, nsteps, s->rej_idx, s->rej_count, metrics ? metrics + b * 6 : nullptr);
     count_launch();
     if (cudaGetLastError()) return FLINT_ERR_CUDA;
   }
