@@ -254,15 +254,15 @@ def fuel_air_states(n, mech, seed, T0=(900.0, 1600.0), patm=(1.0, 20.0), phi=(0.
     return T, p, np.ascontiguousarray(Y), dt
 
 
-def c3_states(n, mech=None, seed=1003):
+def c3_states(n, mech=None, seed=1003, log10dt=(-6.0, -4.0)):
     mech = mech or load("c2")
-    return fuel_air_states(n, mech, seed)
+    return fuel_air_states(n, mech, seed, log10dt=log10dt)
 
 
-def c5_states(n, mech=None, seed=1005):
+def c5_states(n, mech=None, seed=1005, log10dt=(-7.0, -4.0)):
     mech = mech or load("c5")
     return fuel_air_states(n, mech, seed, T0=(900.0, 2000.0), patm=(1.0, 40.0), phi=(0.4, 3.0),
-                           log10dt=(-7.0, -4.0))
+                           log10dt=log10dt)
 
 
 def main():

@@ -478,14 +478,18 @@ def main():
     ap.add_argument("--seed", type=int, default=7)
     ap.add_argument("--margin", type=float, default=0.8)
     ap.add_argument("--lr", type=float, default=1e-3)
+    ap.add_argument("--hard", type=int, default=0,
+                    help="extra training cells drawn from the top half-decade of dt only, where the largest "
+                         "errors of a network trained on the plain distribution lie (validation stays plain)")
     ap.add_argument("--config", default="c2", choices=["c2", "c5"],
                     help="c2: 31 species, c3 reactor states; c5: 54 species, scale-up states")
     args = ap.parse_args()
     import torch
     chem = Chemistry.from_config(args.config)
-    states = mechgen.fuel_air_states
-    if args.config == "c5":
-        states = lambda n, mech, seed: mechgen.c5_states(n, mech, seed)   # noqa: E731
+    base = mechgen.c5_states if args.config == "c5" else mechgen.c3_states
+    states = lambda n, mech, seed: base(n, mech, seed)   # noqa: E731
+    hi = -4.0
+    hard_states = lambda n, mech, seed: base(n, mech, seed, log10dt=(hi - 0.5, hi))   # noqa: E731
     if args.cmd == "calibrate":
         sur = Surrogate.load(chem, args.checkpoint)
         v = generate(chem, args.val, seed=6000 + args.seed, states=states)
@@ -505,6 +509,10 @@ def main():
         return
     t0 = time.time()
     d = generate(chem, args.cells, seed=5000 + args.seed, states=states)
+    if args.hard:
+        h = generate(chem, args.hard, seed=7000 + args.seed, states=hard_states)
+        d = {k: torch.cat([d[k], h[k]]) if torch.is_tensor(d[k]) else d[k] + h[k] for k in d}
+        del h
     v = generate(chem, args.val, seed=6000 + args.seed, states=states)
     tgen = time.time() - t0
     bath = chem.mech.index("N2")
@@ -526,7 +534,8 @@ def main():
     print("calibration diagnostics", json.dumps(getattr(calibrate, "diag", {})))
     if best is not None:
         sur.gate.update(best[1])
-    rep = {"train_cells": int(d["T0"].shape[0]), "val_cells": int(v["T0"].shape[0]), "gen_s": tgen,
+    rep = {"train_cells": int(d["T0"].shape[0]), "hard_cells": args.hard, "val_cells": int(v["T0"].shape[0]),
+           "gen_s": tgen,
            "train_s": ttrain, "steps": args.steps, "batch": args.batch, "val_loss": val_loss,
            "loss_history": {str(k): h for k, h in hist.items()},
            "gate": sur.gate, "diagnostics": getattr(calibrate, "diag", {}),
