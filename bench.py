@@ -347,7 +347,7 @@ def run_ours(args):
                                     "4,194,304-cell scale-up), T0 900-2000 K, p 1-40 atm, phi 0.4-3, dt 1e-7..1e-4 s, "
                                     "rtol 1e-8 atol 1e-14",
                         "cells_per_gpu": n, "mechanism": "synthetic-54sp-320r (20 third-body, 12 Troe)"} if c5 else
-                       {"workload": "reactor-c3: 31sp/160r constant-p BDF/Newton, 262144 cells, rtol 1e-8 atol 1e-14",
+                       {"workload": f"reactor-c3: 31sp/160r constant-p BDF/Newton, {n} cells, rtol 1e-8 atol 1e-14",
                         "cells_per_gpu": n, "mechanism": "synthetic-31sp-160r (12 third-body, 6 Troe)"})
                       | {"path": "plain FP64 integrator", "l2": "flushed (256 MiB write) between timed steps",
                          "cuda_graph": graph_note,
@@ -483,7 +483,65 @@ def run_surrogate(args):
     dT = (Ts[:m] - Tp).abs()
     dY = (Ys[:m] - Yp).abs().amax(dim=1)
     accm = (sts[:m] == 0) & (nsts[:m] == 0)
-    # ---- end to end through pinned host buffers
+    # ---- end to end through pinned host buffers, and the dominant kernel alone
+    # (--no-e2e skips both: the scale-up run, whose fallback alone takes minutes)
+    e2e_line, roof = None, None
+    if not args.no_e2e:
+        e2e_line, roof = surrogate_e2e_and_roofline(args, chem, sur, dev, stream, flush, T0, p0, Y0, dt0, Td0, Yd0, pd,
+                                                    dtd, st, nst, sts, nsts, n, ws, t_sur, plain_stats, t_plain)
+    line = {"metric": METRIC, "value": n * ws / t_sur, "unit": "cell-steps/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t_sur * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64 (integrator, gate) + bf16/fp32 (network)",
+            "data": "synthetic (seeded states, seeded synthetic mechanism)",
+            "config": {"workload": (f"reactor-c5: surrogate+fallback, 54sp/320r, {n} cells, rtol 1e-8 atol 1e-14"
+                                    if c5 else
+                                    f"reactor-c4: surrogate+fallback, 31sp/160r, {n} cells, rtol 1e-8 atol 1e-14"),
+                       "cells_per_gpu": n, "path": "surrogate + FP64 BDF fallback",
+                       "network": (f"MLP {'-'.join(str(d) for d in sur.dims)} GELU x{sur.n_nets} (ensemble), "
+                                   + ("split-bf16 fused tcgen05 forward (TMEM accumulator), fp32 accumulate"
+                                      if fwd_kind == 0 else "split-bf16 mma.sync forward, fp32 accumulate")),
+                       "forward_wait_errors": sur.check(),
+                       "l2": "flushed (256 MiB write) between timed steps", "cuda_graph": graph_note,
+                       "reactor_layout": REACTOR_LAYOUTS[layout]
+                       + " (autotuned on 16,384 cells)"},
+            "surrogate": {"accepted": int(acc), "rejected": int(rej), "accept_frac": acc / max(acc + rej, 1),
+                          "plain_fp64_cell_steps_per_s": plain, "plain_sample_cells": m,
+                          "speedup_vs_plain": (n / t_sur) / plain,
+                          "max_abs_dT_K": float(dT.max()), "max_abs_dY": float(dY.max()),
+                          "max_abs_dT_accepted_K": float(dT[accm].max()) if accm.any() else 0.0,
+                          "max_abs_dY_accepted": float(dY[accm].max()) if accm.any() else 0.0,
+                          "miss": miss_report(dT, dY, accm, sur),
+                          "target": {"dT_K": 1.0, "dY": 1e-4}, "gate": sur.gate},
+            "e2e": e2e_line,
+            "gpu_launches": launches, "clocks": clk,
+            "roofline": roof}
+    if rank == 0 and not args.no_cpu_baseline:
+        cb, (To, Yo, so_, no) = cpu_baseline(chem.mech, T0, p0, Y0, dt0, want_state=True)
+        line["cpu_baseline"] = cb
+        # the same cells' end states from the FP64 oracle: the errors the target names
+        Tsn, Ysn = Ts[:no].cpu().numpy(), Ys[:no].cpu().numpy()
+        acc_o = ((sts[:no] == 0) & (nsts[:no] == 0)).cpu().numpy()
+        eTo = np.abs(Tsn - To)
+        eYo = np.abs(Ysn - Yo).max(axis=1)
+        line["surrogate"]["vs_oracle"] = {
+            "cells": int(no), "oracle_failed": int((so_ != 0).sum()),
+            "max_abs_dT_K": float(eTo.max()), "max_abs_dY": float(eYo.max()),
+            "max_abs_dT_accepted_K": float(eTo[acc_o].max()) if acc_o.any() else 0.0,
+            "max_abs_dY_accepted": float(eYo[acc_o].max()) if acc_o.any() else 0.0}
+    if rank == 0:
+        print(json.dumps(line))
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+def surrogate_e2e_and_roofline(args, chem, sur, dev, stream, flush, T0, p0, Y0, dt0, Td0, Yd0, pd, dtd, st, nst,
+                               sts, nsts, n, ws, t_sur, plain_stats, t_plain):
+    """The surrogate step end to end through pinned host buffers (host copies in
+    the timed region), and the fallback reactor timed alone on the rejected
+    cells for the roofline.  Returns (e2e, roofline)."""
+    import torch
+    from flint_gb300 import dist as fdist
+    from flint_gb300.api import reactor_stats
     Th = torch.from_numpy(T0).pin_memory(); ph = torch.from_numpy(p0).pin_memory()
     Yh = torch.from_numpy(Y0).pin_memory(); dth = torch.from_numpy(dt0).pin_memory()
     To = torch.empty_like(Th).pin_memory(); Yo = torch.empty_like(Yh).pin_memory()
@@ -520,59 +578,18 @@ def run_surrogate(args):
     fbk = reactor_stats(chem)
     ops = fp64_ops(fbk, chem.ns, chem.mech.name)
     peak = chem_peak_fp64()
-    line = {"metric": METRIC, "value": n * ws / t_sur, "unit": "cell-steps/s", "n_gpus": ws, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": t_sur * 1e3, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64 (integrator, gate) + bf16/fp32 (network)",
-            "data": "synthetic (seeded states, seeded synthetic mechanism)",
-            "config": {"workload": (f"reactor-c5: surrogate+fallback, 54sp/320r, {n} cells, rtol 1e-8 atol 1e-14"
-                                    if c5 else
-                                    f"reactor-c4: surrogate+fallback, 31sp/160r, {n} cells, rtol 1e-8 atol 1e-14"),
-                       "cells_per_gpu": n, "path": "surrogate + FP64 BDF fallback",
-                       "network": (f"MLP {'-'.join(str(d) for d in sur.dims)} GELU x{sur.n_nets} (ensemble), "
-                                   + ("split-bf16 fused tcgen05 forward (TMEM accumulator), fp32 accumulate"
-                                      if fwd_kind == 0 else "split-bf16 mma.sync forward, fp32 accumulate")),
-                       "forward_wait_errors": sur.check(),
-                       "l2": "flushed (256 MiB write) between timed steps", "cuda_graph": graph_note,
-                       "reactor_layout": REACTOR_LAYOUTS[layout]
-                       + " (autotuned on 16,384 cells)"},
-            "surrogate": {"accepted": int(acc), "rejected": int(rej), "accept_frac": acc / max(acc + rej, 1),
-                          "plain_fp64_cell_steps_per_s": plain, "plain_sample_cells": m,
-                          "speedup_vs_plain": (n / t_sur) / plain,
-                          "max_abs_dT_K": float(dT.max()), "max_abs_dY": float(dY.max()),
-                          "max_abs_dT_accepted_K": float(dT[accm].max()) if accm.any() else 0.0,
-                          "max_abs_dY_accepted": float(dY[accm].max()) if accm.any() else 0.0,
-                          "miss": miss_report(dT, dY, accm, sur),
-                          "target": {"dT_K": 1.0, "dY": 1e-4}, "gate": sur.gate},
-            "e2e": {"value": n * ws / t_e2e, "unit": "cell-steps/s", "h2d_bytes_per_step": h2d,
-                    "d2h_bytes_per_step": d2h},
-            "gpu_launches": launches, "clocks": clk,
-            "roofline": {"bound": "fp64", "kernel": "k_reactor (the fallback: rejected cells, timed alone)",
-                         "achieved": ops / t_fb / 1e12, "peak": peak, "unit": "TFLOP/s",
-                         "frac": (ops / t_fb / 1e12) / peak if peak else None,
-                         "traffic": (REACTOR_DRAM_BYTES_PER_CELL[chem.mech.name] * int(ridx.numel())
-                                     if chem.mech.name in REACTOR_DRAM_BYTES_PER_CELL else None),
-                         "traffic_note": "ncu DRAM bytes per cell of a k_reactor launch x cells of this launch",
-                         "peak_source": "DFMA probe kernel measured in this run (MEASURED_PEAKS.json has no FP64 figure)",
-                         "kernel_seconds": t_fb, "share_of_step": t_fb / t_sur, "fallback_cells": int(ridx.numel()),
-                         "events_per_launch": fbk, "ops_per_launch": ops,
-                         "plain_leg": {"events": plain_stats, "seconds": t_plain}}}
-    if rank == 0 and not args.no_cpu_baseline:
-        cb, (To, Yo, so_, no) = cpu_baseline(chem.mech, T0, p0, Y0, dt0, want_state=True)
-        line["cpu_baseline"] = cb
-        # the same cells' end states from the FP64 oracle: the errors the target names
-        Tsn, Ysn = Ts[:no].cpu().numpy(), Ys[:no].cpu().numpy()
-        acc_o = ((sts[:no] == 0) & (nsts[:no] == 0)).cpu().numpy()
-        eTo = np.abs(Tsn - To)
-        eYo = np.abs(Ysn - Yo).max(axis=1)
-        line["surrogate"]["vs_oracle"] = {
-            "cells": int(no), "oracle_failed": int((so_ != 0).sum()),
-            "max_abs_dT_K": float(eTo.max()), "max_abs_dY": float(eYo.max()),
-            "max_abs_dT_accepted_K": float(eTo[acc_o].max()) if acc_o.any() else 0.0,
-            "max_abs_dY_accepted": float(eYo[acc_o].max()) if acc_o.any() else 0.0}
-    if rank == 0:
-        print(json.dumps(line))
-    if ws > 1:
-        torch.distributed.destroy_process_group()
+    e2e_line = {"value": n * ws / t_e2e, "unit": "cell-steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}
+    roof = {"bound": "fp64", "kernel": "k_reactor (the fallback: rejected cells, timed alone)",
+            "achieved": ops / t_fb / 1e12, "peak": peak, "unit": "TFLOP/s",
+            "frac": (ops / t_fb / 1e12) / peak if peak else None,
+            "traffic": (REACTOR_DRAM_BYTES_PER_CELL[chem.mech.name] * int(ridx.numel())
+                        if chem.mech.name in REACTOR_DRAM_BYTES_PER_CELL else None),
+            "traffic_note": "ncu DRAM bytes per cell of a k_reactor launch x cells of this launch",
+            "peak_source": "DFMA probe kernel measured in this run (MEASURED_PEAKS.json has no FP64 figure)",
+            "kernel_seconds": t_fb, "share_of_step": t_fb / t_sur, "fallback_cells": int(ridx.numel()),
+            "events_per_launch": fbk, "ops_per_launch": ops,
+            "plain_leg": {"events": plain_stats, "seconds": t_plain}}
+    return e2e_line, roof
 
 
 def miss_report(dT, dY, accm, sur, target_dT=1.0, target_dY=1e-4):
@@ -787,6 +804,9 @@ def main():
     ap.add_argument("--path", default="auto", choices=["auto", "surrogate", "plain"],
                     help="surrogate+fallback (headline, needs the trained checkpoint) or the plain integrator")
     ap.add_argument("--checkpoint", default=SURROGATE_CKPT)
+    ap.add_argument("--no-e2e", action="store_true",
+                    help="surrogate path: skip the end-to-end timing and the fallback-alone roofline run "
+                         "(the 4,194,304-cell scale-up, where each fallback takes minutes)")
     ap.add_argument("--plain-sample", type=int, default=None,
                     help="surrogate path: the plain integrator re-solves (and judges) only the first N cells "
                          "(default: every cell)")

@@ -158,6 +158,11 @@ __device__ inline double warp_max(double v) {
   return v;
 }
 
+// Bit pattern of |x|: for non-negative doubles the integer order of the bit
+// patterns is the numeric order, so maxima and pivot searches can run on the
+// integer pipe instead of as FP64 compares (NaN, 0x7ff8..., sorts above +inf).
+__device__ __forceinline__ long long absbits(double x) { return __double_as_longlong(x) & 0x7fffffffffffffffLL; }
+
 // NASA-7 thermo of species k at T (lane-local).
 struct SpThermo { double cpR, hRT, sR, dcpR; };
 
@@ -346,8 +351,8 @@ __device__ void warp_kinetics(const MechView& m, const WarpScratch& s, int lane,
     if (k < ns) yw += Yk[j] * m.invmw[k];
   }
   double sumYW = warp_sum(yw);
-  // 1/T, 1/sumYW and 1/p from one division (an FP64 division costs a dozen
-  // pipe instructions; the warp would otherwise pay for three)
+  // 1/T, 1/sumYW and 1/p from one reciprocal (the warp would otherwise pay
+  // for three)
   const double rr = 1.0 / (T * sumYW * p);
   const double invT = rr * sumYW * p;
   double wbar = rr * T * p;

@@ -4,6 +4,7 @@
 #include <string>
 #include <vector>
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 #include "flint_dev.cuh"
 #include "../../include/flint_gpu.h"
 
@@ -33,6 +34,15 @@ cudaError_t probe_fp64(double* tflops);
 cudaError_t launch_exp_selftest(const uint8_t* img, const ImageLayout& L, int64_t n, const double* x, double* y,
                                 cudaStream_t st);
 int device_sms();
+// NVTX range over a scope of host code (the phase that enqueues a group of
+// launches), so that a profiler can attribute kernels to phases; a no-op
+// unless a tool is attached.
+struct NvtxRange {
+  explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+  NvtxRange(const NvtxRange&) = delete;
+  NvtxRange& operator=(const NvtxRange&) = delete;
+};
 // Largest dynamic shared memory a block may opt into on the current device.
 size_t device_smem_optin();
 // Opt a kernel into `bytes` of dynamic shared memory.  A refusal is returned

@@ -26,6 +26,7 @@
 // are heuristics and are evaluated in FP32 (the oracle does the same); every
 // quantity of the solution itself stays FP64.
 #include <algorithm>
+#include <cmath>
 #include <mutex>
 
 #include "flint_dev.cuh"
@@ -36,17 +37,24 @@ namespace flint {
 constexpr int REACTOR_THREADS = 256;
 constexpr int MAX_DEVICES = 64;
 
-struct BdfL { double l[6][6]; };
+// il1[q] = 1 / l_1 and Eq[q] = 1 / ((q + 1) l_1 + 1) of order q: per-order
+// constants of every step, tabulated so that a step carries two fewer FP64
+// divisions (each a dozen FP64-pipe instructions on this GPU).
+struct BdfL { double l[6][6]; double il1[6]; double Eq[6]; };
 
 // l^(q)_j = coefficient of x^j in prod_{i=1..q} (1 + x/i)  (Nordsieck BDF of order q).
 static void bdf_coeffs(BdfL& B) {
-  for (int q = 0; q < 6; ++q)
+  for (int q = 0; q < 6; ++q) {
     for (int j = 0; j < 6; ++j) B.l[q][j] = 0.0;
+    B.il1[q] = 0.0; B.Eq[q] = 0.0;
+  }
   for (int q = 1; q <= 5; ++q) {
     double* l = B.l[q];
     l[0] = 1.0;
     for (int i = 1; i <= q; ++i)
       for (int j = i; j >= 1; --j) l[j] += l[j - 1] / (double)i;
+    B.il1[q] = 1.0 / l[1];
+    B.Eq[q] = 1.0 / std::fma((double)(q + 1), l[1], 1.0);
   }
 }
 
@@ -68,52 +76,61 @@ constexpr int MSBJ = 50;
 constexpr int JSLOT = 32 * 32;   // doubles per saved-Jacobian slot of up to 31 species
 
 // Component k = lane + 32 j of the state lives in slot j (SPL slots per lane).
+// inv_nv = 1 / nv, formed once per cell (a division per norm is a dozen
+// FP64-pipe instructions).
 template <int SPL>
-__device__ inline double wrms(const double (&v)[SPL], const double (&w)[SPL], int lane, int nv) {
+__device__ inline double wrms(const double (&v)[SPL], const double (&w)[SPL], int lane, int nv, double inv_nv) {
   double t = 0.0;
 #pragma unroll
   for (int j = 0; j < SPL; ++j) {
     const double a = (lane + 32 * j < nv) ? v[j] * w[j] : 0.0;
     t += a * a;
   }
-  return sqrt(warp_sum(t) / nv);
+  return sqrt(warp_sum(t) * inv_nv);
 }
 
-// Weighted max norm (the Newton convergence test); fmax is exact, so the
-// butterfly leaves the same value on every lane.
+// Weighted max norm (the Newton convergence test), the maximum taken on the
+// bit patterns; the butterfly leaves the same value on every lane.  A NaN
+// component makes the norm NaN (the iteration then counts as diverged).
 template <int SPL>
 __device__ inline double wmax(const double (&v)[SPL], const double (&w)[SPL], int lane, int nv) {
-  double t = 0.0;
+  long long t = 0;
 #pragma unroll
   for (int j = 0; j < SPL; ++j)
-    if (lane + 32 * j < nv) t = fmax(t, fabs(v[j] * w[j]));
-  return warp_max(t);
+    if (lane + 32 * j < nv) t = max(t, absbits(v[j] * w[j]));
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) t = max(t, __shfl_xor_sync(FULL, t, o));
+  return __longlong_as_double(t);
 }
 
 // LU of the rows (row r = lane + 32 j) held at A[r*ld ...], partial pivoting by
-// the largest |a| (lowest row on ties); the pivot order goes to piv[step] and
-// each row remembers its step in mystep (rows are not swapped).  U's diagonal
-// is stored as its reciprocal, so a solve has no division (an FP64 division is
-// a dozen FP64-pipe instructions; a solve would otherwise carry one per column).
+// the largest |a| (lowest row on ties; compared as bit patterns, see absbits);
+// the pivot order goes to piv[step] and each row remembers its step in mystep
+// (rows are not swapped).  Stored: L's multipliers; U with unit diagonal (each
+// pivot row's entries right of the pivot divided by the pivot, by the lanes in
+// parallel) and in the diagonal's place the pivot's reciprocal.  A solve then
+// scales once per lane and has no per-column multiply or division (an FP64
+// division is a dozen FP64-pipe instructions on this GPU, and a uniform
+// per-column multiply costs a whole warp instruction for one value).
 template <int SPL>
 __device__ inline void warp_lu(double* A, int ld, int nv, int lane, int* piv, int (&mystep)[SPL]) {
 #pragma unroll
   for (int j = 0; j < SPL; ++j) mystep[j] = (lane + 32 * j < nv) ? -1 : 1 << 20;
   for (int k = 0; k < nv; ++k) {
-    double cand = -1.0;
+    long long cand = -1;
     int who = lane;
 #pragma unroll
     for (int j = 0; j < SPL; ++j) {
       const int r = lane + 32 * j;
       if (r < nv && mystep[j] < 0) {
-        const double v = fabs(A[r * ld + k]);
+        const long long v = absbits(A[r * ld + k]);
         if (v > cand) { cand = v; who = r; }
       }
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
-      double oc = __shfl_xor_sync(FULL, cand, o);
-      int ow = __shfl_xor_sync(FULL, who, o);
+      const long long oc = __shfl_xor_sync(FULL, cand, o);
+      const int ow = __shfl_xor_sync(FULL, who, o);
       if (oc > cand || (oc == cand && ow < who)) { cand = oc; who = ow; }
     }
 #pragma unroll
@@ -123,16 +140,23 @@ __device__ inline void warp_lu(double* A, int ld, int nv, int lane, int* piv, in
     double* prow = A + who * ld;
     const double inv = 1.0 / prow[k];
     __syncwarp();
-    // the pivot's reciprocal replaces U's diagonal entry: the solves multiply
+    // U row of the pivot: entries right of the pivot scaled to a unit diagonal;
+    // the pivot's reciprocal in the diagonal's place
+#pragma unroll
+    for (int j = 0; j < SPL; ++j) {
+      const int c = lane + 32 * j;
+      if (c > k && c < nv) prow[c] *= inv;
+    }
     if (lane == (who & 31)) prow[k] = inv;
+    __syncwarp();
 #pragma unroll
     for (int j = 0; j < SPL; ++j) {
       const int r = lane + 32 * j;
       if (r < nv && mystep[j] < 0) {
         double* row = A + r * ld;
-        const double l = row[k] * inv;
-        row[k] = l;
-        for (int c = k + 1; c < nv; ++c) row[c] -= l * prow[c];
+        const double a = row[k];
+        row[k] = a * inv;
+        for (int c = k + 1; c < nv; ++c) row[c] -= a * prow[c];
       }
     }
     __syncwarp();
@@ -154,14 +178,19 @@ __device__ inline void warp_lu_solve(const double* A, int ld, int nv, int lane, 
       if (r < nv && mystep[j] > k) b[j] -= A[r * ld + k] * yk;
     }
   }
-  // backward by columns: x_c = b_{piv[c]} / U_{piv[c], c}
+  // backward by columns on the unit-diagonal U: each row's y first divided by
+  // its pivot (the stored reciprocal), then x_c = y_{piv[c]}
   double x[SPL];
 #pragma unroll
-  for (int j = 0; j < SPL; ++j) x[j] = 0.0;
+  for (int j = 0; j < SPL; ++j) {
+    x[j] = 0.0;
+    const int r = lane + 32 * j;
+    if (r < nv) b[j] *= A[r * ld + mystep[j]];
+  }
   for (int c = nv - 1; c >= 0; --c) {
     const int pc = piv[c];
     const double src = (SPL == 1 || (pc >> 5) == 0) ? b[0] : b[SPL - 1];
-    const double xc = __shfl_sync(FULL, src, pc & 31) * A[pc * ld + c];
+    const double xc = __shfl_sync(FULL, src, pc & 31);
 #pragma unroll
     for (int j = 0; j < SPL; ++j) {
       const int r = lane + 32 * j;
@@ -285,6 +314,7 @@ k_reactor(const uint8_t* __restrict__ img, ImageLayout L, int64_t n, double* __r
     pivs = reinterpret_cast<int*>(reinterpret_cast<double*>(smem + L.bytes) + (blockDim.x >> 5) * sd) + wid * 64 * SPL;
   }
   const int ns = m.ns, nv = ns + 1;
+  const double inv_nv = 1.0 / nv;
   const int ld = s.ldj;
   const BdfL& B = c_bdf;
   unsigned long long n_rhs = 0, n_jac = 0, n_newt = 0, n_rej = 0, n_lu = 0;
@@ -360,7 +390,7 @@ k_reactor(const uint8_t* __restrict__ img, ImageLayout L, int64_t n, double* __r
       rhs(y, f);
 #pragma unroll
       for (int j = 0; j < SPL; ++j) ewt[j] = (lane + 32 * j < nv) ? 1.0 / (o.rtol * fabs(y[j]) + atol) : 0.0;
-      const double fn = wrms<SPL>(f, ewt, lane, nv);
+      const double fn = wrms<SPL>(f, ewt, lane, nv, inv_nv);
       double h = (fn * tout > 1.0) ? 1.0 / fn : tout;
 #pragma unroll
       for (int j = 0; j < SPL; ++j) z[1][j] = h * f[j];
@@ -409,7 +439,15 @@ k_reactor(const uint8_t* __restrict__ img, ImageLayout L, int64_t n, double* __r
           double ypred[SPL];
 #pragma unroll
           for (int j = 0; j < SPL; ++j) ypred[j] = z[0][j];
-          if (!have_J || need_J || fabs(gamma / gammaJ - 1.0) > DGMAX || nst >= nstP + MSBP) {
+          // gamma / gammaJ once per attempt: the refresh test and the Newton
+          // correction scale share it (1 after a refresh)
+          double gamrat = 1.0;
+          bool refresh = !have_J || need_J || nst >= nstP + MSBP;
+          if (!refresh) {
+            gamrat = gamma / gammaJ;
+            refresh = fabs(gamrat - 1.0) > DGMAX;
+          }
+          if (refresh) {
             const int eval_J = (!have_J || need_J || nst >= nstJ + MSBJ) ? 1 : 0;
             if (eval_J) {
               ++n_jac;
@@ -420,15 +458,16 @@ k_reactor(const uint8_t* __restrict__ img, ImageLayout L, int64_t n, double* __r
             for (int j = 0; j < SPL; ++j) mystep[j] = pivs[32 * SPL + lane + 32 * j];
             ++n_lu;
             gammaJ = gamma; nstP = nst; crate = 1.0;
+            gamrat = 1.0;
           }
-          const double gamrat = gamma / gammaJ;
           double yv[SPL];
 #pragma unroll
           for (int j = 0; j < SPL; ++j) { e[j] = 0.0; yv[j] = ypred[j]; }
           int conv = 0;
           double delp = 0.0;
-          const double Eq = 1.0 / ((double)(q + 1) * l1 + 1.0);
-          const double il1 = 1.0 / l1;
+          const double Eq = B.Eq[q];
+          const double il1 = B.il1[q];
+          const double sc = gamrat != 1.0 ? 2.0 / (1.0 + gamrat) : 1.0;
           for (int mi = 0; mi < 3; ++mi) {
             ++n_newt;
             rhs(yv, f);
@@ -437,7 +476,6 @@ k_reactor(const uint8_t* __restrict__ img, ImageLayout L, int64_t n, double* __r
             for (int j = 0; j < SPL; ++j) bv[j] = (lane + 32 * j < nv) ? gamma * f[j] - z[1][j] * il1 - e[j] : 0.0;
             warp_lu_solve<SPL>(s.Jr, ld, nv, lane, pivs, mystep, bv);
             if (gamrat != 1.0) {
-              const double sc = 2.0 / (1.0 + gamrat);
 #pragma unroll
               for (int j = 0; j < SPL; ++j) bv[j] *= sc;
             }
@@ -466,7 +504,7 @@ k_reactor(const uint8_t* __restrict__ img, ImageLayout L, int64_t n, double* __r
             h *= eta; ialth = q + 1; have_eprev = 0; need_J = 1; last = 0;
             continue;
           }
-          dsm = Eq * wrms<SPL>(e, ewt, lane, nv);
+          dsm = Eq * wrms<SPL>(e, ewt, lane, nv, inv_nv);
           if (!(dsm <= 1.0)) {
 #pragma unroll
             for (int jj = 0; jj < 6; ++jj)
@@ -516,7 +554,7 @@ k_reactor(const uint8_t* __restrict__ img, ImageLayout L, int64_t n, double* __r
 #pragma unroll
               for (int jj = 2; jj <= 5; ++jj) if (jj == q) zq[j] = z[jj][j];
             }
-            const double ddn = wrms<SPL>(zq, ewt, lane, nv) * fact / ((double)q * B.l[q - 1][1]);
+            const double ddn = wrms<SPL>(zq, ewt, lane, nv, inv_nv) * fact / ((double)q * B.l[q - 1][1]);
             etadn = 1.0 / ((double)powf((float)(1.3 * ddn), 1.0f / (float)q) + 1.3e-6);
           }
           if (q < qmax && have_eprev) {
@@ -524,7 +562,7 @@ k_reactor(const uint8_t* __restrict__ img, ImageLayout L, int64_t n, double* __r
             double de[SPL];
 #pragma unroll
             for (int j = 0; j < SPL; ++j) de[j] = e[j] - eprev[j];
-            const double dup = wrms<SPL>(de, ewt, lane, nv) / (Kq * (double)(q + 2) * B.l[q + 1][1]);
+            const double dup = wrms<SPL>(de, ewt, lane, nv, inv_nv) / (Kq * (double)(q + 2) * B.l[q + 1][1]);
             etaup = 1.0 / ((double)powf((float)(1.4 * dup), 1.0f / (float)(q + 2)) + 1.4e-6);
           }
           int newq = q;
@@ -654,6 +692,7 @@ cudaError_t launch_reactor(const uint8_t* img, const ImageLayout& L, int64_t n, 
                            const unsigned long long* n_dev, int layout) {
   if (n <= 0) return cudaSuccess;
   if (spl_of(L) < 1 || spl_of(L) > 2) return cudaErrorInvalidValue;
+  NvtxRange nvtx("reactor.advance");
   size_t sm = reactor_smem(L, layout);
   const void* fn = reactor_fn(L, layout);
   cudaError_t e = set_smem(fn, sm);

@@ -39,7 +39,6 @@ namespace flint {
 constexpr int MAXL = 8;
 constexpr int MAXS = 64;   // species of a surrogate mechanism (the reactor's limit, 63)
 constexpr int NPASS = 8;   // active-set passes of the conservative projection
-constexpr int SURR_THREADS = 128;
 
 struct Net {
   int nl = 0;
@@ -67,7 +66,7 @@ struct Surrogate {
   Net net[2];
   float *xmean, *xstd, *ymean, *ystd;   // device, host copies below
   std::vector<float> hxm, hxs, hym, hys;
-  double* proj;             // [ns][ns] projector (device)
+  double* G0;               // [ne][ne] B B^T (device)
   double* Bm;               // [ne][ns] element rows divided by W (device)
   int ne;
   // workspaces
@@ -124,160 +123,255 @@ struct GateParams {
   double Tlo, Thi, lpl, lph, ldl, ldh;
 };
 
-// Post-processing and gate, one thread per cell.  Accepted cells are written
-// in place; rejected ones are listed for the fallback (their T, Y untouched).
-__global__ void __launch_bounds__(SURR_THREADS)
+// Post-processing and gate, one thread per cell, POST_CELLS cells per block.
+// The block stages the species part of the mechanism image (thermo only), the
+// element rows B and G0 = B B^T, and works on chunks of POST_CELLS cells whose
+// per-species arrays live in shared memory as [k][POST_CELLS] (a warp's 32
+// lanes touch 32 consecutive doubles); the chunk's mass fractions and network
+// outputs are read, and the accepted mass fractions written, by coalesced
+// block-wide loops over the chunk's contiguous rows.  Accepted cells are
+// written in place; rejected ones are listed for the fallback (their T, Y
+// untouched).
+constexpr int POST_CELLS = 64;
+
+struct PostSmem {
+  int head, n9;      // image bytes staged: [0, o_A) (species sections) and the NASA-9 block
+  int oB, oG;        // B [ne][ns], G0 [ne][ne]
+  int oY0, oD;       // [ns][POST_CELLS] each: Y0; the increment dY, Y1 after the projection
+  int odT, oensT, oens, oacc;   // per cell
+  int bytes;
+};
+
+__host__ __device__ inline PostSmem post_smem(const ImageLayout& L, int ne) {
+  PostSmem S;
+  auto up = [](int b) { return (b + 15) & ~15; };
+  S.head = L.o_A;
+  S.n9 = L.o_nasa9 >= 0 ? 8 * 32 * L.nsp : 0;
+  S.oB = up(S.head + S.n9);
+  S.oG = up(S.oB + 8 * (ne > 0 ? ne : 1) * L.ns);
+  S.oY0 = up(S.oG + 8 * (ne > 0 ? ne * ne : 1));
+  S.oD = S.oY0 + 8 * L.ns * POST_CELLS;
+  S.odT = S.oD + 8 * L.ns * POST_CELLS;
+  S.oensT = S.odT + 8 * POST_CELLS;
+  S.oens = S.oensT + 8 * POST_CELLS;
+  S.oacc = S.oens + 8 * POST_CELLS;
+  S.bytes = S.oacc + 4 * POST_CELLS;
+  return S;
+}
+
+__global__ void __launch_bounds__(POST_CELLS)
 k_post(const uint8_t* __restrict__ img, ImageLayout L, int64_t n, int64_t base, double* __restrict__ T,
        const double* __restrict__ p, double* __restrict__ Y, const double* __restrict__ dt,
        const float* __restrict__ yn, const float* __restrict__ yn2, const float* __restrict__ ym,
-       const float* __restrict__ ys, const double* __restrict__ proj, const double* __restrict__ Bm, int ne,
+       const float* __restrict__ ys, const double* __restrict__ G0, const double* __restrict__ Bm, int ne,
        GateParams gp, int* __restrict__ status, int* __restrict__ nsteps, int64_t* __restrict__ rej_idx,
        unsigned long long* __restrict__ rej_count, double* __restrict__ metrics) {
   extern __shared__ __align__(16) uint8_t smem[];
-  stage_image(smem, img, L.bytes);
+  const PostSmem S = post_smem(L, ne);
+  const int t = threadIdx.x;
+  {
+    const int4* src = reinterpret_cast<const int4*>(img);
+    int4* dst = reinterpret_cast<int4*>(smem);
+    for (int i = t; i < S.head / 16; i += POST_CELLS) dst[i] = __ldg(src + i);
+    if (S.n9) {
+      const int4* s9 = reinterpret_cast<const int4*>(img + L.o_nasa9);
+      int4* d9 = reinterpret_cast<int4*>(smem + S.head);
+      for (int i = t; i < S.n9 / 16; i += POST_CELLS) d9[i] = __ldg(s9 + i);
+    }
+  }
   MechView m;
-  m.bind(L, smem);
+  m.bind(L, smem);   // only the species sections (and NASA-9, below) are staged
+  m.nasa9 = S.n9 ? reinterpret_cast<const double*>(smem + S.head) : nullptr;
   const int ns = m.ns, nout = ns + 1;
-  double* sB = reinterpret_cast<double*>(smem + L.bytes);
-  for (int i = threadIdx.x; i < ne * ns; i += blockDim.x) sB[i] = Bm[i];
+  double* sB = reinterpret_cast<double*>(smem + S.oB);
+  double* sG = reinterpret_cast<double*>(smem + S.oG);
+  for (int i = t; i < ne * ns; i += POST_CELLS) sB[i] = Bm[i];
+  for (int i = t; i < ne * ne; i += POST_CELLS) sG[i] = G0[i];
+  double* sY0 = reinterpret_cast<double*>(smem + S.oY0);
+  double* sD = reinterpret_cast<double*>(smem + S.oD);
+  double* sdT = reinterpret_cast<double*>(smem + S.odT);
+  double* sensT = reinterpret_cast<double*>(smem + S.oensT);
+  unsigned long long* sens = reinterpret_cast<unsigned long long*>(smem + S.oens);
+  int* sacc = reinterpret_cast<int*>(smem + S.oacc);
   __syncthreads();
-  double dY[MAXS], Y1[MAXS];
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t cell = base + i;
-    const double T0 = T[cell], dti = dt[cell], pc = p[cell];
-    bool ok = isfinite(T0) && isfinite(pc) && pc > 0.0 && isfinite(dti) && dti > 0.0;
-    ok = ok && T0 >= gp.Tlo && T0 <= gp.Thi;
-    const double lp = log10(pc), ld = log10(dti);
-    ok = ok && lp >= gp.lpl && lp <= gp.lph && ld >= gp.ldl && ld <= gp.ldh;
-    double dTn = 0.0, ens = 0.0, ensT = 0.0;
-    for (int k = 0; k < ns; ++k) {
-      dY[k] = (double)ym[k] + (double)ys[k] * (double)yn[i * nout + k];
+  for (int64_t c0 = (int64_t)blockIdx.x * POST_CELLS; c0 < n; c0 += (int64_t)gridDim.x * POST_CELLS) {
+    const int nc = (int)(n - c0 < POST_CELLS ? n - c0 : POST_CELLS);
+    const int64_t cell0 = base + c0;
+    // the chunk's rows: Y0 [nc][ns] and the network outputs [nc][nout] (dY, dT),
+    // de-normalised and (two networks) averaged, with the ensemble spreads
+    for (int idx = t; idx < nc * ns; idx += POST_CELLS) {
+      const int c = idx / ns, k = idx - c * ns;
+      sY0[k * POST_CELLS + c] = Y[cell0 * ns + idx];
+    }
+    sens[t] = 0ull;
+    __syncthreads();
+    for (int idx = t; idx < nc * nout; idx += POST_CELLS) {
+      const int c = idx / nout, k = idx - c * nout;
+      const int64_t o = c0 * nout + idx;
+      double d = (double)ym[k] + (double)ys[k] * (double)yn[o];
+      double spread = 0.0;
       if (yn2) {
-        double d2 = (double)ym[k] + (double)ys[k] * (double)yn2[i * nout + k];
-        ens = fmax(ens, fabs(d2 - dY[k]));
-        dY[k] = 0.5 * (dY[k] + d2);
+        const double d2 = (double)ym[k] + (double)ys[k] * (double)yn2[o];
+        spread = fabs(d2 - d);
+        d = 0.5 * (d + d2);
+      }
+      if (k < ns) {
+        sD[k * POST_CELLS + c] = d;
+        if (yn2) atomicMax(&sens[c], (unsigned long long)absbits(spread));   // max of non-negative doubles
+      } else {
+        sdT[c] = d;
+        sensT[c] = spread;
       }
     }
-    dTn = (double)ym[ns] + (double)ys[ns] * (double)yn[i * nout + ns];
-    if (yn2) {
-      double d2 = (double)ym[ns] + (double)ys[ns] * (double)yn2[i * nout + ns];
-      ensT = fabs(d2 - dTn);
-      dTn = 0.5 * (dTn + d2);
-    }
-    // element residual of the raw prediction
-    double er = 0.0;
-    for (int e = 0; e < ne; ++e) {
-      double s = 0.0;
-      for (int k = 0; k < ns; ++k) s += sB[e * ns + k] * dY[k];
-      er = fmax(er, fabs(s));
-    }
-    // conservative, non-negative mass fractions: project dY onto element
-    // conservation over the free species, clip negatives to zero (they leave
-    // the free set), repeat (active-set least-squares, at most NPASS passes;
-    // the last pass clips nothing, so a result still negative there is rejected)
-    unsigned long long fixed = 0ull;   // bit k: species k clipped at zero
-    double clipped = 0.0;
-    for (int k = 0; k < ns; ++k) Y1[k] = Y[cell * ns + k] + dY[k];
-    bool clean = false;
-    for (int pass = 0; pass < NPASS && !clean; ++pass) {
-      double r[8], G[8][8], lam[8];
+    __syncthreads();
+    if (t < nc) {
+      const int64_t i = c0 + t, cell = cell0 + t;
+      double* y0 = sY0 + t;    // species k at y0[k * POST_CELLS]
+      double* dY = sD + t;
+      const double T0 = T[cell], dti = dt[cell], pc = p[cell];
+      bool ok = isfinite(T0) && isfinite(pc) && pc > 0.0 && isfinite(dti) && dti > 0.0;
+      ok = ok && T0 >= gp.Tlo && T0 <= gp.Thi;
+      const double lp = log10(pc), ld = log10(dti);
+      ok = ok && lp >= gp.lpl && lp <= gp.lph && ld >= gp.ldl && ld <= gp.ldh;
+      const double dTn = sdT[t], ensT = yn2 ? sensT[t] : 0.0;
+      const double ens = yn2 ? __longlong_as_double((long long)sens[t]) : 0.0;
+      // element residual of the raw prediction
+      double er = 0.0;
       for (int e = 0; e < ne; ++e) {
-        double se = 0.0;
-        for (int k = 0; k < ns; ++k) se += sB[e * ns + k] * (Y1[k] - Y[cell * ns + k]);
-        r[e] = se;
-        for (int f = 0; f < ne; ++f) {
-          double g = 0.0;
-          for (int k = 0; k < ns; ++k)
-            if (!((fixed >> k) & 1ull)) g += sB[e * ns + k] * sB[f * ns + k];
-          G[e][f] = g;
+        double s = 0.0;
+        for (int k = 0; k < ns; ++k) s += sB[e * ns + k] * dY[k * POST_CELLS];
+        er = fmax(er, fabs(s));
+      }
+      // conservative, non-negative mass fractions: project dY onto element
+      // conservation over the free species, clip negatives to zero (they leave
+      // the free set), repeat (active-set least-squares, at most NPASS passes;
+      // the last pass clips nothing, so a result still negative there is
+      // rejected).  dY holds the increment Y1 - Y0 throughout; G over the free
+      // species is G0 less the clipped species' terms.
+      unsigned long long fixed = 0ull;   // bit k: species k clipped at zero
+      double clipped = 0.0;
+      bool clean = false;
+      for (int pass = 0; pass < NPASS && !clean; ++pass) {
+        double r[8], G[8][8], lam[8];
+        for (int e = 0; e < ne; ++e) {
+          double se = 0.0;
+          for (int k = 0; k < ns; ++k) se += sB[e * ns + k] * dY[k * POST_CELLS];
+          r[e] = se;
+          for (int f = 0; f < ne; ++f) {
+            double g = sG[e * ne + f];
+            for (unsigned long long fx = fixed; fx; fx &= fx - 1) {
+              const int k = __ffsll((long long)fx) - 1;
+              g -= sB[e * ns + k] * sB[f * ns + k];
+            }
+            G[e][f] = g;
+          }
+        }
+        // solve G lam = r (Gauss-Jordan, partial pivoting; empty rows get lam = 0)
+        for (int e = 0; e < ne; ++e) lam[e] = r[e];
+        int live[8];
+        for (int c = 0; c < ne; ++c) {
+          int pr = c; double best = fabs(G[c][c]);
+          for (int q = c + 1; q < ne; ++q) if (fabs(G[q][c]) > best) { best = fabs(G[q][c]); pr = q; }
+          live[c] = best > 1e-300;
+          if (!live[c]) continue;
+          if (pr != c) {
+            for (int f = 0; f < ne; ++f) { double tt = G[c][f]; G[c][f] = G[pr][f]; G[pr][f] = tt; }
+            double tt = lam[c]; lam[c] = lam[pr]; lam[pr] = tt;
+          }
+          const double inv = 1.0 / G[c][c];
+          for (int f = 0; f < ne; ++f) G[c][f] *= inv;
+          lam[c] *= inv;
+          for (int q = 0; q < ne; ++q) {
+            if (q == c) continue;
+            const double fq = G[q][c];
+            for (int f = 0; f < ne; ++f) G[q][f] -= fq * G[c][f];
+            lam[q] -= fq * lam[c];
+          }
+        }
+        for (int e = 0; e < ne; ++e) if (!live[e]) lam[e] = 0.0;
+        clean = true;
+        for (int k = 0; k < ns; ++k) {
+          if ((fixed >> k) & 1ull) continue;
+          double corr = 0.0;
+          for (int e = 0; e < ne; ++e) corr += sB[e * ns + k] * lam[e];
+          const double d = dY[k * POST_CELLS] - corr;
+          const double yk = y0[k * POST_CELLS];
+          if (yk + d < 0.0 && pass < NPASS - 1) {
+            clipped += -(yk + d);
+            dY[k * POST_CELLS] = -yk;    // Y1 = 0
+            fixed |= 1ull << k;
+            clean = false;
+          } else {
+            dY[k * POST_CELLS] = d;
+          }
         }
       }
-      // solve G lam = r (Gauss-Jordan, partial pivoting; empty rows get lam = 0)
-      for (int e = 0; e < ne; ++e) lam[e] = r[e];
-      int live[8];
-      for (int c = 0; c < ne; ++c) {
-        int pr = c; double best = fabs(G[c][c]);
-        for (int q = c + 1; q < ne; ++q) if (fabs(G[q][c]) > best) { best = fabs(G[q][c]); pr = q; }
-        live[c] = best > 1e-300;
-        if (!live[c]) continue;
-        if (pr != c) {
-          for (int f = 0; f < ne; ++f) { double t = G[c][f]; G[c][f] = G[pr][f]; G[pr][f] = t; }
-          double t = lam[c]; lam[c] = lam[pr]; lam[pr] = t;
-        }
-        const double inv = 1.0 / G[c][c];
-        for (int f = 0; f < ne; ++f) G[c][f] *= inv;
-        lam[c] *= inv;
-        for (int q = 0; q < ne; ++q) {
-          if (q == c) continue;
-          const double fq = G[q][c];
-          for (int f = 0; f < ne; ++f) G[q][f] -= fq * G[c][f];
-          lam[q] -= fq * lam[c];
-        }
-      }
-      for (int e = 0; e < ne; ++e) if (!live[e]) lam[e] = 0.0;
-      clean = true;
+      // dY -> Y1 (in place) and its minimum
+      double ymin = 1.0;
+      double* y1 = dY;
       for (int k = 0; k < ns; ++k) {
-        if ((fixed >> k) & 1ull) continue;
-        double corr = 0.0;
-        for (int e = 0; e < ne; ++e) corr += sB[e * ns + k] * lam[e];
-        Y1[k] -= corr;
-        if (Y1[k] < 0.0 && pass < NPASS - 1) {
-          clipped += -Y1[k];
-          Y1[k] = 0.0;
-          fixed |= 1ull << k;
-          clean = false;
+        const double v = y0[k * POST_CELLS] + dY[k * POST_CELLS];
+        y1[k * POST_CELLS] = v;
+        ymin = fmin(ymin, v);
+      }
+      // realizability measure reported to the gate: clipped mass (negative) or
+      // the most negative mass fraction left
+      const double yreal = fmin(-clipped, ymin);
+      // energy: h(T1, Y1) = h(T0, Y0), Newton from the network's temperature
+      double h0 = 0.0;
+      {
+        const double lnT = log(T0), invT = 1.0 / T0;
+        for (int k = 0; k < ns; ++k) h0 += y0[k * POST_CELLS] * nasa7(m, k, T0, lnT, invT).hRT * m.invmw[k];
+        h0 *= T0;
+      }
+      double T1 = T0 + dTn;
+      bool conv = isfinite(T1) && T1 > 200.0 && T1 < 6000.0;
+      for (int it = 0; it < 8 && conv; ++it) {
+        const double lnT = log(T1), invT = 1.0 / T1;
+        double h = 0.0, cpm = 0.0;
+        for (int k = 0; k < ns; ++k) {
+          SpThermo th = nasa7(m, k, T1, lnT, invT);
+          const double yw = y1[k * POST_CELLS] * m.invmw[k];
+          h += yw * th.hRT;
+          cpm += yw * th.cpR;
+        }
+        const double dT = (h * T1 - h0) / cpm;
+        T1 -= dT;
+        if (!(T1 > 200.0 && T1 < 6000.0)) conv = false;
+        if (fabs(dT) < 1e-10 * T1) break;
+      }
+      const double dTres = conv ? fabs(T1 - (T0 + dTn)) : 1e300;
+      int accept;
+      if (metrics) {
+        // evaluation mode: every cell takes the surrogate result, the gate
+        // quantities are reported instead of applied
+        double* mt = metrics + i * 6;
+        mt[0] = dTres; mt[1] = er; mt[2] = yreal; mt[3] = ensT; mt[4] = ens;
+        mt[5] = (ok && ymin >= 0.0) ? 1.0 : 0.0;   // the gate's fixed conditions
+        T[cell] = conv ? T1 : T0 + dTn;
+        accept = 1;
+      } else {
+        ok = ok && conv && dTres <= gp.max_dT_resid && er <= gp.max_elem_resid && yreal >= gp.min_Y && ymin >= 0.0;
+        if (yn2) ok = ok && ensT <= gp.max_ens_dT && ens <= gp.max_ens_dY;
+        accept = ok ? 1 : 0;
+        if (ok) {
+          T[cell] = T1;
+          if (status) status[cell] = FLINT_CELL_OK;
+          if (nsteps) nsteps[cell] = 0;
+        } else {
+          unsigned long long slot = atomicAdd(rej_count, 1ull);
+          rej_idx[slot] = cell;
         }
       }
+      sacc[t] = accept;
     }
-    double ymin = 1.0;
-    for (int k = 0; k < ns; ++k) ymin = fmin(ymin, Y1[k]);
-    // realizability measure reported to the gate: clipped mass (negative) or
-    // the most negative mass fraction left
-    const double yreal = fmin(-clipped, ymin);
-    // energy: h(T1, Y1) = h(T0, Y0), Newton from the network's temperature
-    double h0 = 0.0;
-    {
-      const double lnT = log(T0), invT = 1.0 / T0;
-      for (int k = 0; k < ns; ++k) h0 += Y[cell * ns + k] * nasa7(m, k, T0, lnT, invT).hRT * m.invmw[k];
-      h0 *= T0;
+    __syncthreads();
+    // the accepted cells' mass fractions, written back row by row
+    for (int idx = t; idx < nc * ns; idx += POST_CELLS) {
+      const int c = idx / ns, k = idx - c * ns;
+      if (sacc[c]) Y[cell0 * ns + idx] = sD[k * POST_CELLS + c];
     }
-    double T1 = T0 + dTn;
-    bool conv = isfinite(T1) && T1 > 200.0 && T1 < 6000.0;
-    for (int it = 0; it < 8 && conv; ++it) {
-      const double lnT = log(T1), invT = 1.0 / T1;
-      double h = 0.0, cpm = 0.0;
-      for (int k = 0; k < ns; ++k) {
-        SpThermo th = nasa7(m, k, T1, lnT, invT);
-        h += Y1[k] * th.hRT * m.invmw[k];
-        cpm += Y1[k] * th.cpR * m.invmw[k];
-      }
-      const double dT = (h * T1 - h0) / cpm;
-      T1 -= dT;
-      if (!(T1 > 200.0 && T1 < 6000.0)) conv = false;
-      if (fabs(dT) < 1e-10 * T1) break;
-    }
-    const double dTres = conv ? fabs(T1 - (T0 + dTn)) : 1e300;
-    if (metrics) {
-      // evaluation mode: every cell takes the surrogate result, the gate
-      // quantities are reported instead of applied
-      double* mt = metrics + i * 6;
-      mt[0] = dTres; mt[1] = er; mt[2] = yreal; mt[3] = ensT; mt[4] = ens;
-      mt[5] = (ok && ymin >= 0.0) ? 1.0 : 0.0;   // the gate's fixed conditions
-      for (int k = 0; k < ns; ++k) Y[cell * ns + k] = Y1[k];
-      T[cell] = conv ? T1 : T0 + dTn;
-      continue;
-    }
-    ok = ok && conv && dTres <= gp.max_dT_resid && er <= gp.max_elem_resid && yreal >= gp.min_Y && ymin >= 0.0;
-    if (yn2) ok = ok && ensT <= gp.max_ens_dT && ens <= gp.max_ens_dY;
-    if (ok) {
-      for (int k = 0; k < ns; ++k) Y[cell * ns + k] = Y1[k];
-      T[cell] = T1;
-      if (status) status[cell] = FLINT_CELL_OK;
-      if (nsteps) nsteps[cell] = 0;
-    } else {
-      unsigned long long slot = atomicAdd(rej_count, 1ull);
-      rej_idx[slot] = cell;
-    }
+    __syncthreads();
   }
 }
 
@@ -408,7 +502,7 @@ void surrogate_free(Surrogate* s) {
   for (int l = 0; l < MAXL; ++l) { fr(s->Z[l]); fr(s->A[l]); }
   fr(s->dz0); fr(s->dz1); fr(s->yhat); fr(s->xf); fr(s->yout2); fr(s->rej_idx); fr(s->rej_count);
   fr(s->cT); fr(s->cp); fr(s->cY); fr(s->cdt); fr(s->cst); fr(s->cns); fr(s->loss);
-  fr(s->xmean); fr(s->xstd); fr(s->ymean); fr(s->ystd); fr(s->proj); fr(s->Bm); fr(s->uerr);
+  fr(s->xmean); fr(s->xstd); fr(s->ymean); fr(s->ystd); fr(s->G0); fr(s->Bm); fr(s->uerr);
   delete s;
 }
 
@@ -452,6 +546,7 @@ int surrogate_create(const uint8_t* mimg, const ImageLayout& L, unsigned int* co
   if (L.ns > MAXS - 1 || L.ns < 2) { err = "surrogate supports 2..63 species"; return FLINT_ERR_MECH; }
   if (d->bath < 0 || d->bath >= L.ns) { err = "bath species index"; return FLINT_ERR_ARG; }
   if (d->n_nets < 1 || d->n_nets > 2) { err = "n_nets must be 1 or 2"; return FLINT_ERR_ARG; }
+  if (d->n_elements < 0 || d->n_elements > 8) { err = "n_elements must be 0..8"; return FLINT_ERR_ARG; }
   if (!d->weights || !d->x_mean || !d->x_std || !d->y_mean || !d->y_std || !d->elem) { err = "NULL array"; return FLINT_ERR_ARG; }
   auto* s = new Surrogate();
   s->mimg = mimg; s->L = L; s->counter = counter; s->jsave = nullptr; s->jslots = 0;
@@ -470,9 +565,10 @@ int surrogate_create(const uint8_t* mimg, const ImageLayout& L, unsigned int* co
   }
   s->hxm.assign(d->x_mean, d->x_mean + s->n_in); s->hxs.assign(d->x_std, d->x_std + s->n_in);
   s->hym.assign(d->y_mean, d->y_mean + s->n_out); s->hys.assign(d->y_std, d->y_std + s->n_out);
-  // projector P = I - B^T (B B^T)^-1 B with B[e][k] = a_ek / W_k
+  // element rows B[e][k] = a_ek / W_k and G0 = B B^T (the projection's normal
+  // matrix over all species; the gate subtracts the clipped species' terms)
   const int ns = s->ns, ne = s->ne;
-  std::vector<double> Bm((size_t)ne * ns), BBt((size_t)ne * ne, 0.0), Pm((size_t)ns * ns, 0.0);
+  std::vector<double> Bm((size_t)ne * ns), BBt((size_t)ne * ne, 0.0);
   std::vector<double> W(ns);
   cudaMemcpy(W.data(), mimg + L.o_mw, ns * sizeof(double), cudaMemcpyDeviceToHost);
   for (int e = 0; e < ne; ++e)
@@ -480,35 +576,11 @@ int surrogate_create(const uint8_t* mimg, const ImageLayout& L, unsigned int* co
   for (int a = 0; a < ne; ++a)
     for (int b = 0; b < ne; ++b)
       for (int k = 0; k < ns; ++k) BBt[a * ne + b] += Bm[a * ns + k] * Bm[b * ns + k];
-  // invert BBt (small, Gauss-Jordan with partial pivoting); zero rows (absent elements) are skipped
-  std::vector<double> inv((size_t)ne * ne, 0.0);
-  for (int a = 0; a < ne; ++a) inv[a * ne + a] = 1.0;
-  std::vector<int> active(ne, 1);
-  for (int c = 0; c < ne; ++c) {
-    int piv = -1; double best = 0.0;
-    for (int r = c; r < ne; ++r) if (fabs(BBt[r * ne + c]) > best) { best = fabs(BBt[r * ne + c]); piv = r; }
-    if (piv < 0 || best < 1e-300) { active[c] = 0; continue; }
-    for (int j = 0; j < ne; ++j) { std::swap(BBt[c * ne + j], BBt[piv * ne + j]); std::swap(inv[c * ne + j], inv[piv * ne + j]); }
-    double dv = BBt[c * ne + c];
-    for (int j = 0; j < ne; ++j) { BBt[c * ne + j] /= dv; inv[c * ne + j] /= dv; }
-    for (int r = 0; r < ne; ++r) {
-      if (r == c) continue;
-      double f = BBt[r * ne + c];
-      for (int j = 0; j < ne; ++j) { BBt[r * ne + j] -= f * BBt[c * ne + j]; inv[r * ne + j] -= f * inv[c * ne + j]; }
-    }
-  }
-  for (int k = 0; k < ns; ++k)
-    for (int j = 0; j < ns; ++j) {
-      double v = (k == j) ? 1.0 : 0.0;
-      for (int a = 0; a < ne; ++a)
-        for (int b = 0; b < ne; ++b) v -= Bm[a * ns + k] * inv[a * ne + b] * Bm[b * ns + j];
-      Pm[k * ns + j] = v;
-    }
   cudaError_t e = cudaMalloc(&s->xmean, s->n_in * 4);
   if (!e) e = cudaMalloc(&s->xstd, s->n_in * 4);
   if (!e) e = cudaMalloc(&s->ymean, s->n_out * 4);
   if (!e) e = cudaMalloc(&s->ystd, s->n_out * 4);
-  if (!e) e = cudaMalloc(&s->proj, ns * ns * 8);
+  if (!e) e = cudaMalloc(&s->G0, std::max(ne * ne, 1) * 8);
   if (!e) e = cudaMalloc(&s->Bm, std::max(ne, 1) * ns * 8);
   if (!e) e = cudaMalloc(&s->loss, 8);
   if (!e) e = cudaMalloc(&s->rej_count, 8);
@@ -518,7 +590,7 @@ int surrogate_create(const uint8_t* mimg, const ImageLayout& L, unsigned int* co
   if (!e) e = cudaMemcpy(s->xstd, d->x_std, s->n_in * 4, cudaMemcpyHostToDevice);
   if (!e) e = cudaMemcpy(s->ymean, d->y_mean, s->n_out * 4, cudaMemcpyHostToDevice);
   if (!e) e = cudaMemcpy(s->ystd, d->y_std, s->n_out * 4, cudaMemcpyHostToDevice);
-  if (!e) e = cudaMemcpy(s->proj, Pm.data(), ns * ns * 8, cudaMemcpyHostToDevice);
+  if (!e && ne) e = cudaMemcpy(s->G0, BBt.data(), ne * ne * 8, cudaMemcpyHostToDevice);
   if (!e && ne) e = cudaMemcpy(s->Bm, Bm.data(), ne * ns * 8, cudaMemcpyHostToDevice);
   if (e) { surrogate_free(s); err = cudaGetErrorString(e); return FLINT_ERR_CUDA; }
   *out = s;
@@ -637,31 +709,41 @@ int surrogate_advance(Surrogate* s, int64_t n, double* T, const double* p, doubl
   gp.max_ens_dT = gate->max_ens_dT; gp.max_ens_dY = gate->max_ens_dY;
   gp.Tlo = gate->T_lo; gp.Thi = gate->T_hi; gp.lpl = gate->log10p_lo; gp.lph = gate->log10p_hi;
   gp.ldl = gate->log10dt_lo; gp.ldh = gate->log10dt_hi;
-  const size_t psm = s->L.bytes + (size_t)(std::max(s->ne, 1) * s->ns) * sizeof(double);
+  const size_t psm = (size_t)post_smem(s->L, s->ne).bytes;
   if (set_smem((const void*)k_post, psm)) return FLINT_ERR_CUDA;
   if (cudaMemsetAsync(s->rej_count, 0, 8, st)) return FLINT_ERR_CUDA;
   for (int64_t b = 0; b < n; b += s->cap) {
     const int64_t m = std::min<int64_t>(s->cap, n - b);
-    if (surrogate_features(s, m, T + b, p + b, Y + b * s->ns, dt + b, s->xf, st)) return FLINT_ERR_CUDA;
-    if (net_forward(s, s->net[0], m, s->xf, s->yhat, false, st)) return FLINT_ERR_CUDA;
-    if (s->nnets > 1 && net_forward(s, s->net[1], m, s->xf, s->yout2, false, st)) return FLINT_ERR_CUDA;
-    k_post<<<blocks_for(m, SURR_THREADS), SURR_THREADS, psm, st>>>(
-        s->mimg, s->L, m, b, T, p, Y, dt, s->yhat, s->nnets > 1 ? s->yout2 : nullptr, s->ymean, s->ystd, s->proj,
+    {
+      NvtxRange r("surrogate.features");
+      if (surrogate_features(s, m, T + b, p + b, Y + b * s->ns, dt + b, s->xf, st)) return FLINT_ERR_CUDA;
+    }
+    {
+      NvtxRange r("surrogate.network");
+      if (net_forward(s, s->net[0], m, s->xf, s->yhat, false, st)) return FLINT_ERR_CUDA;
+      if (s->nnets > 1 && net_forward(s, s->net[1], m, s->xf, s->yout2, false, st)) return FLINT_ERR_CUDA;
+    }
+    NvtxRange r("surrogate.gate");
+    k_post<<<blocks_for(m, POST_CELLS), POST_CELLS, psm, st>>>(
+        s->mimg, s->L, m, b, T, p, Y, dt, s->yhat, s->nnets > 1 ? s->yout2 : nullptr, s->ymean, s->ystd, s->G0,
         s->Bm, s->ne, gp, status, nsteps, s->rej_idx, s->rej_count, metrics ? metrics + b * 6 : nullptr);
     count_launch();
     if (cudaGetLastError()) return FLINT_ERR_CUDA;
   }
   if (metrics) return 0;
-  k_gather<<<blocks_for(n, 256), 256, 0, st>>>(s->rej_count, s->rej_idx, s->ns, T, p, Y, dt, s->cT, s->cp, s->cY,
-                                                s->cdt);
-  count_launch();
-  cudaError_t e = launch_reactor(s->mimg, s->L, n, s->cT, s->cp, s->cY, s->cdt, o, s->cst, s->cns, s->counter, jsave,
-                                 jslots, st, s->rej_count, reactor_layout);
-  if (e) return FLINT_ERR_CUDA;
-  k_scatter<<<blocks_for(n, 256), 256, 0, st>>>(s->rej_count, s->rej_idx, s->ns, T, Y, s->cT, s->cY, s->cst, s->cns,
-                                                 status, nsteps);
-  count_launch();
-  if (cudaGetLastError()) return FLINT_ERR_CUDA;
+  {
+    NvtxRange r("surrogate.fallback");
+    k_gather<<<blocks_for(n, 256), 256, 0, st>>>(s->rej_count, s->rej_idx, s->ns, T, p, Y, dt, s->cT, s->cp, s->cY,
+                                                  s->cdt);
+    count_launch();
+    cudaError_t e = launch_reactor(s->mimg, s->L, n, s->cT, s->cp, s->cY, s->cdt, o, s->cst, s->cns, s->counter,
+                                   jsave, jslots, st, s->rej_count, reactor_layout);
+    if (e) return FLINT_ERR_CUDA;
+    k_scatter<<<blocks_for(n, 256), 256, 0, st>>>(s->rej_count, s->rej_idx, s->ns, T, Y, s->cT, s->cY, s->cst,
+                                                   s->cns, status, nsteps);
+    count_launch();
+    if (cudaGetLastError()) return FLINT_ERR_CUDA;
+  }
   s->last_accepted = s->last_rejected = -1;
   s->last_n = n;
   if (!want_counts) return 0;   // stays asynchronous on st (and capturable in a CUDA graph)
