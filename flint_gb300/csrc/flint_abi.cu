@@ -159,6 +159,7 @@ static int pack(const flint_mech_desc* d, ImageLayout& L, std::vector<uint8_t>& 
   L.o_cstart = sec(4 * (S + 1)); L.o_lr = sec(4 * std::max(nlist, 1)); L.o_lnu = sec(8 * std::max(nlist, 1));
   L.o_exptab = sec(8 * 64);
   L.o_nasa9 = d->nasa9 ? sec(8 * 32 * S) : -1;
+  L.o_logtab = sec(8 * 3 * 129);
   L.nfall = nfall;
   L.bytes = off;
   img.assign(off, 0);
@@ -235,6 +236,16 @@ static int pack(const flint_mech_desc* d, ImageLayout& L, std::vector<uint8_t>& 
   I(L.o_cstart)[S] = e;
   // 2^(j/64), rounded from extended precision, for the table-driven exp
   for (int j = 0; j < 64; ++j) D(L.o_exptab)[j] = (double)exp2l((long double)j / 64.0L);
+  // flog's table: c_j = 1/(1 + j/128) rounded to double, -ln c_j as hi + lo
+  // (long double: at least 64 significant bits on either host)
+  for (int j = 0; j <= 128; ++j) {
+    const double c = (double)(1.0L / (1.0L + (long double)j / 128.0L));
+    const long double l = -logl((long double)c);
+    const double hi = (double)l;
+    D(L.o_logtab)[3 * j] = c;
+    D(L.o_logtab)[3 * j + 1] = hi;
+    D(L.o_logtab)[3 * j + 2] = (double)(l - (long double)hi);
+  }
   return FLINT_OK;
 }
 
@@ -862,6 +873,12 @@ int flint_selftest_exp(flint_mech_t h, int64_t n, const double* x, double* y, vo
   if (!h || n < 0 || (n > 0 && (!x || !y))) return fail(FLINT_ERR_ARG, "bad argument");
   cudaError_t e = launch_exp_selftest(h->dimg, h->L, n, x, y, (cudaStream_t)stream);
   return e == cudaSuccess ? FLINT_OK : cuda_fail(e, "flint_selftest_exp");
+}
+
+int flint_selftest_log(flint_mech_t h, int64_t n, const double* x, double* y, void* stream) {
+  if (!h || n < 0 || (n > 0 && (!x || !y))) return fail(FLINT_ERR_ARG, "bad argument");
+  cudaError_t e = launch_log_selftest(h->dimg, h->L, n, x, y, (cudaStream_t)stream);
+  return e == cudaSuccess ? FLINT_OK : cuda_fail(e, "flint_selftest_log");
 }
 
 int flint_probe_fp64_peak(double* tflops) {

@@ -65,6 +65,7 @@ struct ImageLayout {
   int o_exptab;                  // double [64]: 2^(j/64)
   int nfall;                     // falloff reactions (the last nfall after sorting; <= 16)
   int o_nasa9;                   // NASA-9 thermo [32][nsp] (nranges, T0..T3, 3 x 9 coefficients); -1 = none
+  int o_logtab;                  // double [129][3]: c_j ~ 1/(1 + j/128), -ln c_j as hi + lo (flog)
 };
 
 struct MechView {
@@ -79,6 +80,7 @@ struct MechView {
   const double *tbd, *tbv, *lnu, *exptab;
   const int *tbp, *tbs;
   const double* nasa9;   // null: NASA-7 (nasa)
+  const double* logtab;
   int nfall;
 
   __host__ __device__ void bind(const ImageLayout& L, const uint8_t* base) {
@@ -100,6 +102,7 @@ struct MechView {
     cstart = (const int*)(base + L.o_cstart); lr = (const int*)(base + L.o_lr);
     lnu = (const double*)(base + L.o_lnu);
     nasa9 = L.o_nasa9 >= 0 ? (const double*)(base + L.o_nasa9) : nullptr;
+    logtab = (const double*)(base + L.o_logtab);
   }
 };
 
@@ -145,6 +148,39 @@ __device__ __forceinline__ double fexp(double x, const double* __restrict__ tab)
   const double res = fma(t, p, t);
   return __hiloint2double(__double2hiint(res) + (k >> 6) * 1048576, __double2loint(res));
 }
+
+// ln x by a 129-point table (the table-driven method of P. T. P. Tang, ACM
+// TOMS 16(4), 1990): x = 2^m y with y in [1, 2), j = round(128 (y - 1)),
+// c_j ~ 1 / (1 + j/128) with -ln c_j tabulated as hi + lo, r = y c_j - 1 by
+// one FMA (|r| <= 2^-8 plus rounding), and
+//   ln x = m ln2 + (-ln c_j) + ln(1 + r),
+// ln(1 + r) by its Taylor polynomial to r^7 (the first omitted term is below
+// 2^-66).  ln2 is split into a 32-bit head and a tail (the fdlibm split) so
+// that m * head is exact.  14 FP64 operations, where the CUDA library's log
+// measured about 33 FP64-pipe slots per value on this GPU.  Zero, subnormal,
+// negative, inf and NaN arguments take the library path (the test is on the
+// integer high word).  Checked against CUDA's log in tests/test_gpu_parity.py.
+__device__ __forceinline__ double flog(double x, const double* __restrict__ tab) {
+  const int hi = __double2hiint(x);
+  if (hi < 0x00100000 || hi >= 0x7ff00000) return log(x);
+  const int mh = hi & 0x000fffff;
+  const int j = (mh + 0x1000) >> 13;                       // 0..128
+  const double y = __hiloint2double(mh | 0x3ff00000, __double2loint(x));
+  const double* t = tab + 3 * j;
+  const double r = fma(y, t[0], -1.0);
+  double q = fma(r, 1.0 / 7.0, -1.0 / 6.0);
+  q = fma(r, q, 0.2);
+  q = fma(r, q, -0.25);
+  q = fma(r, q, 1.0 / 3.0);
+  q = fma(r, q, -0.5);
+  const double l1p = fma(r * r, q, r);                      // ln(1 + r)
+  const double dm = (double)((hi >> 20) - 1023);
+  const double LN2_HI = 6.93147180369123816490e-01;         // 0x1.62e42fee00000p-1
+  const double LN2_LO = 1.90821492927058770002e-10;         // 0x1.a39ef35793c76p-33
+  return fma(dm, LN2_HI, t[1]) + (fma(dm, LN2_LO, t[2]) + l1p);
+}
+
+constexpr double INV_LN10 = 0.43429448190325182765;       // 1 / ln 10
 
 __device__ inline double warp_sum(double v) {
 #pragma unroll
@@ -204,7 +240,7 @@ __device__ inline SpThermo nasa7(const MechView& m, int k, double T, double lnT,
 }
 
 // c^ord by order code (1..3 integral, 4 general) with the derivative d(c^ord)/dc.
-__device__ inline double powc(double c, int code, double ord, double* d, const double* tab) {
+__device__ inline double powc(double c, int code, double ord, double* d, const double* tab, const double* ltab) {
   switch (code) {
     case 1: *d = 1.0; return c;
     case 2: *d = 2.0 * c; return c * c;
@@ -212,7 +248,7 @@ __device__ inline double powc(double c, int code, double ord, double* d, const d
     case 4: {
       double cc = c > 0.0 ? c : 0.0;
       if (cc > 0.0) {
-        double pw = fexp(ord * log(cc), tab);
+        double pw = fexp(ord * flog(cc, ltab), tab);
         *d = ord * pw / cc;
         return pw;
       }
@@ -306,10 +342,10 @@ __device__ inline Falloff falloff_eval(const MechView& m, int r, int type, doubl
       Fc += e2;
       dFc += T2 * invT * invT * e2;
     }
-    double logFc = log10(Fc);
+    double logFc = flog(Fc, m.logtab) * INV_LN10;
     double cc = -0.4 - 0.67 * logFc;
     double nn = 0.75 - 1.27 * logFc;
-    double x = log10(Pr > 1e-300 ? Pr : 1e-300) + cc;
+    double x = flog(Pr > 1e-300 ? Pr : 1e-300, m.logtab) * INV_LN10 + cc;
     double den = nn - 0.14 * x;
     double f1 = x / den;
     double opf = 1.0 + f1 * f1;
@@ -341,7 +377,7 @@ __device__ void warp_kinetics(const MechView& m, const WarpScratch& s, int lane,
                               double T, double pr, CellOutT<SPL>& out, bool cv = false) {
   const double p = pr;
   const int ns = m.ns, nsp = m.nsp, nrpad = m.nrpad;
-  const double lnT = log(T);
+  const double lnT = flog(T, m.logtab);
   const double lnC0 = m.lnpref_rth - lnT;        // ln(p_ref / (R T))
   // mixture molar mass and density
   double yw = 0.0;
@@ -431,7 +467,7 @@ __device__ void warp_kinetics(const MechView& m, const WarpScratch& s, int lane,
     const double Pr_src = __shfl_sync(FULL, Pr, lane >= NF && lane < 2 * NF ? lane - NF : 0);
     double lg_in = lane < NF ? Fc : (lane < 2 * NF ? Pr_src : 1.0);
     lg_in = lg_in > 1e-300 ? lg_in : 1e-300;
-    const double lg = log10(lg_in);
+    const double lg = flog(lg_in, m.logtab) * INV_LN10;
     const double logPr = __shfl_sync(FULL, lg, lane < NF ? lane + NF : 0);
     // one division per lane for the blend (an FP64 division is a dozen pipe
     // instructions): with Q = den^2 + x^2, 1/(den (1 + Pr) Q) yields 1/den,
@@ -488,7 +524,7 @@ __device__ void warp_kinetics(const MechView& m, const WarpScratch& s, int lane,
       for (int sl = 0; sl < MAXSIDE; ++sl) {
         int sp = m.rsp[sl * nrpad + r];
         int oc = rx_ordcode(w, sl);
-        if (sp >= 0) pwf[sl] = powc(s.c[sp], oc, m.rord[sl * nrpad + r], &dpf[sl], tab);
+        if (sp >= 0) pwf[sl] = powc(s.c[sp], oc, m.rord[sl * nrpad + r], &dpf[sl], tab, m.logtab);
         else { pwf[sl] = 1.0; dpf[sl] = 0.0; }
         Pf *= pwf[sl];
       }
@@ -503,7 +539,7 @@ __device__ void warp_kinetics(const MechView& m, const WarpScratch& s, int lane,
             double nu = m.pnu[sl * nrpad + r];
             dG += nu * s.gRT[sp];
             if (JAC) dH += nu * s.hRT[sp];
-            pwr[sl] = powc(s.c[sp], (m.pcode[r] >> (4 * sl)) & 0xf, nu, &dpr[sl], tab);
+            pwr[sl] = powc(s.c[sp], (m.pcode[r] >> (4 * sl)) & 0xf, nu, &dpr[sl], tab, m.logtab);
           } else { pwr[sl] = 1.0; dpr[sl] = 0.0; }
           Pr *= pwr[sl];
           int sq = m.rsp[sl * nrpad + r];

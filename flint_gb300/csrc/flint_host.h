@@ -33,6 +33,8 @@ void count_launch();
 cudaError_t probe_fp64(double* tflops);
 cudaError_t launch_exp_selftest(const uint8_t* img, const ImageLayout& L, int64_t n, const double* x, double* y,
                                 cudaStream_t st);
+cudaError_t launch_log_selftest(const uint8_t* img, const ImageLayout& L, int64_t n, const double* x, double* y,
+                                cudaStream_t st);
 int device_sms();
 // NVTX range over a scope of host code (the phase that enqueues a group of
 // launches), so that a profiler can attribute kernels to phases; a no-op

@@ -43,7 +43,7 @@ k_wdot_small(const uint8_t* __restrict__ img, ImageLayout L, int64_t n, int layo
 #define WS(k) ws[(k) * SMALL_THREADS + t]
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + t; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     const double T = Tg[i];
-    const double lnT = log(T), invT = 1.0 / T;
+    const double lnT = flog(T, m.logtab), invT = 1.0 / T;
     double rho;
     double cpm = 0.0, hm = 0.0, ctot = 0.0;
     if (roi_mode) {
@@ -90,7 +90,7 @@ k_wdot_small(const uint8_t* __restrict__ img, ImageLayout L, int64_t n, int layo
 #pragma unroll
       for (int sl = 0; sl < MAXSIDE; ++sl) {
         int sp = m.rsp[sl * P + r];
-        if (sp >= 0) Pf *= powc(CS(sp), rx_ordcode(w, sl), m.rord[sl * P + r], &d, m.exptab);
+        if (sp >= 0) Pf *= powc(CS(sp), rx_ordcode(w, sl), m.rord[sl * P + r], &d, m.exptab, m.logtab);
       }
       double rvsf = 0.0;
       if (rx_rev(w)) {
@@ -101,7 +101,7 @@ k_wdot_small(const uint8_t* __restrict__ img, ImageLayout L, int64_t n, int layo
           if (sp >= 0) {
             double nu = m.pnu[sl * P + r];
             dG += nu * GS(sp);
-            Pr *= powc(CS(sp), (m.pcode[r] >> (4 * sl)) & 0xf, nu, &d, m.exptab);
+            Pr *= powc(CS(sp), (m.pcode[r] >> (4 * sl)) & 0xf, nu, &d, m.exptab, m.logtab);
           }
           int sq = m.rsp[sl * P + r];
           if (sq >= 0) dG -= m.rnu[sl * P + r] * GS(sq);
@@ -275,6 +275,28 @@ cudaError_t launch_exp_selftest(const uint8_t* img, const ImageLayout& L, int64_
                                 cudaStream_t st) {
   if (n <= 0) return cudaSuccess;
   k_exp_selftest<<<256, 256, L.bytes, st>>>(img, L, n, x, y);
+  count_launch();
+  return cudaGetLastError();
+}
+
+__global__ void k_log_selftest(const uint8_t* __restrict__ img, ImageLayout L, int64_t n,
+                               const double* __restrict__ x, double* __restrict__ y) {
+  extern __shared__ __align__(16) uint8_t smem[];
+  stage_image(smem, img, L.bytes);
+  MechView m;
+  m.bind(L, smem);
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    y[2 * i] = flog(x[i], m.logtab);
+    y[2 * i + 1] = log(x[i]);
+  }
+}
+
+cudaError_t launch_log_selftest(const uint8_t* img, const ImageLayout& L, int64_t n, const double* x, double* y,
+                                cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  cudaError_t e = set_smem((const void*)k_log_selftest, L.bytes);
+  if (e != cudaSuccess) return e;
+  k_log_selftest<<<256, 256, L.bytes, st>>>(img, L, n, x, y);
   count_launch();
   return cudaGetLastError();
 }

@@ -93,18 +93,20 @@ __global__ void k_features(int64_t n, int ns, int bath, const double* __restrict
                            const double* __restrict__ Y, const double* __restrict__ dt,
                            const float* __restrict__ xm, const float* __restrict__ xs, float* __restrict__ X) {
   const int nin = ns + 2;
+  // the logarithmic features in FP32, the precision the network takes them in
+  // (a double log10 per species cost ~35 FP64-pipe slots on this GPU)
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     float* x = X + i * nin;
     int c = 0;
     for (int k = 0; k < ns; ++k) {
       if (k == bath) continue;
-      double y = Y[i * ns + k];
-      x[c] = (float)((log10(y > 1e-20 ? y : 1e-20) - xm[c]) / xs[c]);
+      const double y = Y[i * ns + k];
+      x[c] = (log10f((float)(y > 1e-20 ? y : 1e-20)) - xm[c]) / xs[c];
       ++c;
     }
     x[c] = (float)((T[i] - xm[c]) / xs[c]); ++c;
-    x[c] = (float)((log10(p[i]) - xm[c]) / xs[c]); ++c;
-    x[c] = (float)((log10(dt[i]) - xm[c]) / xs[c]);
+    x[c] = (log10f((float)p[i]) - xm[c]) / xs[c]; ++c;
+    x[c] = (log10f((float)dt[i]) - xm[c]) / xs[c];
   }
 }
 
@@ -118,9 +120,11 @@ __global__ void k_targets(int64_t n, int ns, const double* __restrict__ T0, cons
   }
 }
 
+// The domain bounds of p and dt are given as log10 and compared as values
+// (plo = 10^log10p_lo ...): the same test without two logarithms per cell.
 struct GateParams {
   double max_dT_resid, max_elem_resid, min_Y, max_ens_dT, max_ens_dY;
-  double Tlo, Thi, lpl, lph, ldl, ldh;
+  double Tlo, Thi, plo, phi, dtlo, dthi;
 };
 
 // Post-processing and gate, one thread per cell, POST_CELLS cells per block.
@@ -208,13 +212,17 @@ k_post(const uint8_t* __restrict__ img, ImageLayout L, int64_t n, int64_t base, 
     for (int idx = t; idx < nc * nout; idx += POST_CELLS) {
       const int c = idx / nout, k = idx - c * nout;
       const int64_t o = c0 * nout + idx;
-      double d = (double)ym[k] + (double)ys[k] * (double)yn[o];
-      double spread = 0.0;
+      // in FP32, like the network's outputs (relative rounding 6e-8 of the
+      // increment, far below the targets; the projection and the enthalpy
+      // Newton then work in FP64)
+      float df = fmaf(ys[k], yn[o], ym[k]);
+      float sf = 0.0f;
       if (yn2) {
-        const double d2 = (double)ym[k] + (double)ys[k] * (double)yn2[o];
-        spread = fabs(d2 - d);
-        d = 0.5 * (d + d2);
+        const float d2 = fmaf(ys[k], yn2[o], ym[k]);
+        sf = fabsf(d2 - df);
+        df = 0.5f * (df + d2);
       }
+      const double d = (double)df, spread = (double)sf;
       if (k < ns) {
         sD[k * POST_CELLS + c] = d;
         if (yn2) atomicMax(&sens[c], (unsigned long long)absbits(spread));   // max of non-negative doubles
@@ -231,8 +239,7 @@ k_post(const uint8_t* __restrict__ img, ImageLayout L, int64_t n, int64_t base, 
       const double T0 = T[cell], dti = dt[cell], pc = p[cell];
       bool ok = isfinite(T0) && isfinite(pc) && pc > 0.0 && isfinite(dti) && dti > 0.0;
       ok = ok && T0 >= gp.Tlo && T0 <= gp.Thi;
-      const double lp = log10(pc), ld = log10(dti);
-      ok = ok && lp >= gp.lpl && lp <= gp.lph && ld >= gp.ldl && ld <= gp.ldh;
+      ok = ok && pc >= gp.plo && pc <= gp.phi && dti >= gp.dtlo && dti <= gp.dthi;
       const double dTn = sdT[t], ensT = yn2 ? sensT[t] : 0.0;
       const double ens = yn2 ? __longlong_as_double((long long)sens[t]) : 0.0;
       // element residual of the raw prediction
@@ -320,14 +327,15 @@ k_post(const uint8_t* __restrict__ img, ImageLayout L, int64_t n, int64_t base, 
       // energy: h(T1, Y1) = h(T0, Y0), Newton from the network's temperature
       double h0 = 0.0;
       {
-        const double lnT = log(T0), invT = 1.0 / T0;
+        // ln T enters only the NASA-9 enthalpy (NASA-7's h needs no log)
+        const double lnT = m.nasa9 ? log(T0) : 0.0, invT = 1.0 / T0;
         for (int k = 0; k < ns; ++k) h0 += y0[k * POST_CELLS] * nasa7(m, k, T0, lnT, invT).hRT * m.invmw[k];
         h0 *= T0;
       }
       double T1 = T0 + dTn;
       bool conv = isfinite(T1) && T1 > 200.0 && T1 < 6000.0;
       for (int it = 0; it < 8 && conv; ++it) {
-        const double lnT = log(T1), invT = 1.0 / T1;
+        const double lnT = m.nasa9 ? log(T1) : 0.0, invT = 1.0 / T1;
         double h = 0.0, cpm = 0.0;
         for (int k = 0; k < ns; ++k) {
           SpThermo th = nasa7(m, k, T1, lnT, invT);
@@ -338,7 +346,9 @@ k_post(const uint8_t* __restrict__ img, ImageLayout L, int64_t n, int64_t base, 
         const double dT = (h * T1 - h0) / cpm;
         T1 -= dT;
         if (!(T1 > 200.0 && T1 < 6000.0)) conv = false;
-        if (fabs(dT) < 1e-10 * T1) break;
+        // quadratic convergence: after a correction below 1e-6 T1 the next one
+        // would be below 1e-7 K (|d2h/dT2| / (2 cp) < 1e-3 / K, T1 < 6000 K)
+        if (fabs(dT) < 1e-6 * T1) break;
       }
       const double dTres = conv ? fabs(T1 - (T0 + dTn)) : 1e300;
       int accept;
@@ -707,8 +717,9 @@ int surrogate_advance(Surrogate* s, int64_t n, double* T, const double* p, doubl
   GateParams gp;
   gp.max_dT_resid = gate->max_dT_resid; gp.max_elem_resid = gate->max_elem_resid; gp.min_Y = gate->min_Y;
   gp.max_ens_dT = gate->max_ens_dT; gp.max_ens_dY = gate->max_ens_dY;
-  gp.Tlo = gate->T_lo; gp.Thi = gate->T_hi; gp.lpl = gate->log10p_lo; gp.lph = gate->log10p_hi;
-  gp.ldl = gate->log10dt_lo; gp.ldh = gate->log10dt_hi;
+  gp.Tlo = gate->T_lo; gp.Thi = gate->T_hi;
+  gp.plo = std::pow(10.0, gate->log10p_lo); gp.phi = std::pow(10.0, gate->log10p_hi);
+  gp.dtlo = std::pow(10.0, gate->log10dt_lo); gp.dthi = std::pow(10.0, gate->log10dt_hi);
   const size_t psm = (size_t)post_smem(s->L, s->ne).bytes;
   if (set_smem((const void*)k_post, psm)) return FLINT_ERR_CUDA;
   if (cudaMemsetAsync(s->rej_count, 0, 8, st)) return FLINT_ERR_CUDA;

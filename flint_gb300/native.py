@@ -127,6 +127,7 @@ def lib():
     L.flint_wdot_autotune.argtypes = [vp, i64, vp, vp, vp, C.POINTER(Tuning), vp]
     L.flint_probe_fp64_peak.argtypes = [C.POINTER(C.c_double)]
     L.flint_selftest_exp.argtypes = [vp, i64, vp, vp, vp]
+    L.flint_selftest_log.argtypes = [vp, i64, vp, vp, vp]
     L.flint_mech_create_tables.argtypes = [C.POINTER(TableDesc), C.POINTER(vp)]
     L.flint_tables_read.argtypes = [C.c_char_p, C.c_char_p, C.POINTER(vp)]
     L.flint_tables_desc.argtypes = [vp, C.POINTER(TableDesc)]

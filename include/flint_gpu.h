@@ -506,6 +506,11 @@ int flint_probe_fp64_peak(double* tflops);
  * kernels' exp against the CUDA library. */
 int flint_selftest_exp(flint_mech_t mech, int64_t n, const double* x, double* y, void* stream);
 
+/* Diagnostic: y[2i] = the kernels' table-driven ln(x[i]), y[2i+1] = CUDA's
+ * log(x[i]) (device pointers).  No reference counterpart: lets tests bound the
+ * kernels' log against the CUDA library. */
+int flint_selftest_log(flint_mech_t mech, int64_t n, const double* x, double* y, void* stream);
+
 /* Number of kernels the library launched since load (instrumentation). */
 int64_t flint_kernel_launch_count(void);
 

@@ -158,6 +158,31 @@ def test_table_driven_exp_vs_cuda(c2):
     np.testing.assert_array_equal(yy[same & ~np.isnan(yy[:, 1]), 0], yy[same & ~np.isnan(yy[:, 1]), 1])
 
 
+def test_table_driven_log_vs_cuda(c2):
+    """The kernels' ln (Tang's table method) within 2 ulp of CUDA's log, and
+    within 2e-17 absolutely near x = 1; zero, subnormal, negative, inf and NaN
+    arguments take CUDA's log itself."""
+    import ctypes as C
+    rng = np.random.default_rng(2)
+    x = np.concatenate([10.0 ** rng.uniform(-307, 307, 300000), rng.uniform(200.0, 6000.0, 100000),
+                        rng.uniform(0.98, 1.02, 100000), 1.0 + rng.uniform(-1e-6, 1e-6, 20000),
+                        2.0 ** np.arange(-1022, 1024, 1.0), np.nextafter(2.0 ** np.arange(-1021, 1024, 1.0), 0.0),
+                        [1.0, 2.0, 0.5, 0.0, -0.0, -1.0, 5e-324, 1e-310, np.inf, -np.inf, np.nan,
+                         np.finfo(float).max, np.finfo(float).tiny]])
+    xt = torch.from_numpy(x).cuda()
+    y = torch.empty(2 * x.size, dtype=torch.float64, device="cuda")
+    rc = c2.L.flint_selftest_log(c2.h, x.size, C.c_void_p(xt.data_ptr()), C.c_void_p(y.data_ptr()), None)
+    assert rc == 0
+    torch.cuda.synchronize()
+    yy = y.cpu().numpy().reshape(-1, 2)
+    fin = np.isfinite(yy[:, 1])
+    err = np.abs(yy[fin, 0] - yy[fin, 1])
+    assert (err <= np.maximum(2 * np.spacing(np.abs(yy[fin, 1])), 2e-17)).all(), err.max()
+    same = ~fin
+    np.testing.assert_array_equal(np.isnan(yy[same, 0]), np.isnan(yy[same, 1]))
+    np.testing.assert_array_equal(yy[same & ~np.isnan(yy[:, 1]), 0], yy[same & ~np.isnan(yy[:, 1]), 1])
+
+
 def test_empty_batch(c2):
     Tt = torch.empty(0, dtype=torch.float64, device="cuda")
     Yt = torch.empty((0, c2.ns), dtype=torch.float64, device="cuda")
