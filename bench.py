@@ -784,6 +784,41 @@ def chem_peak_fp64():
     return out.value
 
 
+def run_fp64_math(args):
+    """FP64-pipe cost of the CUDA library's math functions on this GPU: time
+    per value of torch's elementwise kernels over a 2^27-element FP64 array
+    (compute-bound: a copy of the same array takes ~1.5 slots' time), in
+    FP64-pipe slots (the time of one DFMA per value at the measured DFMA
+    rate).  The kernels' own exp and log are written against these figures."""
+    import torch
+    dev = torch.device("cuda")
+    n = 1 << 27
+    x = torch.rand(n, dtype=torch.float64, device=dev) * 2000.0 + 300.0
+    y = x * 1e-3
+    z = x * 0.5 + 1.0
+    out = torch.empty_like(x)
+
+    def timed(f, reps=5):
+        f(); torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True); e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            f()
+        e1.record(); e1.synchronize()
+        return e0.elapsed_time(e1) / reps / 1e3
+
+    peak = chem_peak_fp64()                    # TFLOP/s (2 per DFMA)
+    slot = 2.0 / (peak * 1e12)                 # seconds per DFMA-value
+    fns = {"copy": lambda: out.copy_(x), "mul": lambda: torch.mul(x, x, out=out),
+           "log": lambda: torch.log(x, out=out), "log10": lambda: torch.log10(x, out=out),
+           "exp": lambda: torch.exp(y, out=out), "reciprocal": lambda: torch.reciprocal(x, out=out),
+           "div": lambda: torch.div(x, z, out=out), "sqrt": lambda: torch.sqrt(x, out=out)}
+    res = {k: timed(f) for k, f in fns.items()}
+    print(json.dumps({"workload": "fp64-math", "values": n, "dfma_peak_tflops": peak,
+                      "slots_per_value": {k: v / n / slot for k, v in res.items()},
+                      "ms": {k: v * 1e3 for k, v in res.items()}}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -794,7 +829,7 @@ def main():
     ap.add_argument("--workload", default="reactor",
                     choices=["reactor", "reactor-c5", "c1-wdot", "c1-wdotjac", "c2-wdot", "c2-wdotjac", "c5-wdot",
                              "c5-wdotjac",
-                             "c2-general"])
+                             "c2-general", "fp64-math"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-parity", action="store_true",
                     help="source-term workloads: skip the oracle check of the timed outputs")
@@ -819,6 +854,9 @@ def main():
             return
         args.cells = args.cells or CELLS
         run_ours(args)
+        return
+    if args.workload == "fp64-math":
+        run_fp64_math(args)
         return
     if args.workload != "reactor":
         run_kernel_workload(args)

@@ -149,7 +149,7 @@ static int pack(const flint_mech_desc* d, ImageLayout& L, std::vector<uint8_t>& 
   const int S = L.nsp, P = L.nrpad;
   int off = 0;
   auto sec = [&](int bytes) { int o = off; off = rup(off + bytes, 16); return o; };
-  L.o_mw = sec(8 * S); L.o_invmw = sec(8 * S); L.o_nasa = sec(8 * 16 * S);
+  L.o_mw = sec(8 * S); L.o_invmw = sec(8 * S); L.o_nasa = sec(8 * 16 * S); L.o_nasah = sec(8 * 16 * S);
   L.o_A = sec(8 * P); L.o_b = sec(8 * P); L.o_E = sec(8 * P);
   L.o_A0 = sec(8 * P); L.o_b0 = sec(8 * P); L.o_E0 = sec(8 * P); L.o_tr = sec(8 * 4 * P);
   L.o_rnu = sec(8 * 3 * P); L.o_rord = sec(8 * 3 * P); L.o_pnu = sec(8 * 3 * P);
@@ -174,6 +174,12 @@ static int pack(const flint_mech_desc* d, ImageLayout& L, std::vector<uint8_t>& 
       D(L.o_nasa)[(7 + j) * S + k] = c[10 + j];
     }
     D(L.o_nasa)[14 * S + k] = c[1];
+    for (int r = 0; r < 2; ++r) {   // low (c[3..9]) and high (c[10..16]) range
+      const double* a = c + 3 + 7 * r;
+      double* h = D(L.o_nasah) + 8 * r * S + k;
+      h[0] = a[1] / 2.0; h[S] = a[2] / 3.0; h[2 * S] = a[3] / 4.0; h[3 * S] = a[4] / 5.0;
+      h[4 * S] = a[2] / 2.0; h[5 * S] = a[3] / 3.0; h[6 * S] = a[4] / 4.0; h[7 * S] = 0.0;
+    }
     if (d->nasa9)
       for (int j = 0; j < 32; ++j) D(L.o_nasa9)[j * S + k] = d->nasa9[32 * k + j];
   }

@@ -42,6 +42,8 @@ struct ImageLayout {
   double inv_r_eos;                     // 1 / r_eos
   // species
   int o_mw, o_invmw, o_nasa;     // nasa: [16][nsp] : low a0..a6, high a0..a6, tmid, unused
+  int o_nasah;                   // [16][nsp]: low a1/2, a2/3, a3/4, a4/5, a2/2, a3/3, a4/4, 0; high the same
+                                 // (the h and s polynomials' coefficients, divided once on the host)
   // reactions (nrpad each)
   int o_A, o_b, o_E, o_A0, o_b0, o_E0, o_tr;   // tr: [4][nrpad] = a, 1/T3, 1/T1, T2
   // falloff: the image stores the low-pressure limit relative to the high-
@@ -71,7 +73,7 @@ struct ImageLayout {
 struct MechView {
   int ns, nr, nrpad, nsp, ntb;
   double r_eos, r_thermo, lnpref_rth, inv_r_eos;
-  const double *mw, *invmw, *nasa;
+  const double *mw, *invmw, *nasa, *nasah;
   const double *A, *b, *E, *A0, *b0, *E0, *tr;
   const double *rnu, *rord, *pnu, *dnu;
   const int *rsp, *psp, *cstart, *lr;
@@ -89,6 +91,7 @@ struct MechView {
     r_eos = L.r_eos; r_thermo = L.r_thermo; lnpref_rth = L.lnpref_rth; inv_r_eos = L.inv_r_eos;
     mw = (const double*)(base + L.o_mw); invmw = (const double*)(base + L.o_invmw);
     nasa = (const double*)(base + L.o_nasa);
+    nasah = (const double*)(base + L.o_nasah);
     A = (const double*)(base + L.o_A); b = (const double*)(base + L.o_b); E = (const double*)(base + L.o_E);
     A0 = (const double*)(base + L.o_A0); b0 = (const double*)(base + L.o_b0); E0 = (const double*)(base + L.o_E0);
     tr = (const double*)(base + L.o_tr);
@@ -229,12 +232,14 @@ __device__ inline SpThermo nasa7(const MechView& m, int k, double T, double lnT,
   if (m.nasa9) return nasa9(m, k, T, lnT, invT);   // warp-uniform: a property of the mechanism
   const int S = m.nsp;
   const double tmid = m.nasa[14 * S + k];
-  const double* a = m.nasa + ((T <= tmid) ? 0 : 7 * S) + k;
+  const bool lo = T <= tmid;
+  const double* a = m.nasa + (lo ? 0 : 7 * S) + k;
+  const double* c = m.nasah + (lo ? 0 : 8 * S) + k;   // a1/2, a2/3, a3/4, a4/5, a2/2, a3/3, a4/4
   double a0 = a[0], a1 = a[S], a2 = a[2 * S], a3 = a[3 * S], a4 = a[4 * S], a5 = a[5 * S], a6 = a[6 * S];
   SpThermo t;
-  t.cpR = a0 + T * (a1 + T * (a2 + T * (a3 + T * a4)));
-  t.hRT = a0 + T * (a1 * 0.5 + T * (a2 * (1.0 / 3.0) + T * (a3 * 0.25 + T * a4 * 0.2))) + a5 * invT;
-  t.sR = a0 * lnT + T * (a1 + T * (a2 * 0.5 + T * (a3 * (1.0 / 3.0) + T * a4 * 0.25))) + a6;
+  t.cpR = fma(T, fma(T, fma(T, fma(T, a4, a3), a2), a1), a0);
+  t.hRT = fma(a5, invT, fma(T, fma(T, fma(T, fma(T, c[3 * S], c[2 * S]), c[S]), c[0]), a0));
+  t.sR = fma(a0, lnT, fma(T, fma(T, fma(T, fma(T, c[6 * S], c[5 * S]), c[4 * S]), a1), a6));
   t.dcpR = a1 + T * (2.0 * a2 + T * (3.0 * a3 + T * 4.0 * a4));
   return t;
 }

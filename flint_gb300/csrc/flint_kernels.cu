@@ -274,6 +274,8 @@ __global__ void k_exp_selftest(const uint8_t* __restrict__ img, ImageLayout L, i
 cudaError_t launch_exp_selftest(const uint8_t* img, const ImageLayout& L, int64_t n, const double* x, double* y,
                                 cudaStream_t st) {
   if (n <= 0) return cudaSuccess;
+  cudaError_t e = set_smem((const void*)k_exp_selftest, L.bytes);
+  if (e != cudaSuccess) return e;
   k_exp_selftest<<<256, 256, L.bytes, st>>>(img, L, n, x, y);
   count_launch();
   return cudaGetLastError();
