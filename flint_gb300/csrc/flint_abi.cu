@@ -157,7 +157,7 @@ static int pack(const flint_mech_desc* d, ImageLayout& L, std::vector<uint8_t>& 
   L.o_pcode = sec(4 * P);
   L.o_tbd = sec(8 * L.ntb); L.o_tbp = sec(4 * (L.ntb + 1)); L.o_tbs = sec(4 * ntbl); L.o_tbv = sec(8 * ntbl);
   L.o_cstart = sec(4 * (S + 1)); L.o_lr = sec(4 * std::max(nlist, 1)); L.o_lnu = sec(8 * std::max(nlist, 1));
-  L.o_exptab = sec(8 * 64);
+  L.o_exptab = sec(8 * 256);
   L.o_nasa9 = d->nasa9 ? sec(8 * 32 * S) : -1;
   L.o_logtab = sec(8 * 3 * 129);
   L.nfall = nfall;
@@ -240,8 +240,8 @@ static int pack(const flint_mech_desc* d, ImageLayout& L, std::vector<uint8_t>& 
       for (auto& pr : lists[k]) { I(L.o_lr)[e] = pr.first; D(L.o_lnu)[e] = pr.second; ++e; }
   }
   I(L.o_cstart)[S] = e;
-  // 2^(j/64), rounded from extended precision, for the table-driven exp
-  for (int j = 0; j < 64; ++j) D(L.o_exptab)[j] = (double)exp2l((long double)j / 64.0L);
+  // 2^(j/256), rounded from extended precision, for the table-driven exp
+  for (int j = 0; j < 256; ++j) D(L.o_exptab)[j] = (double)exp2l((long double)j / 256.0L);
   // flog's table: c_j = 1/(1 + j/128) rounded to double, -ln c_j as hi + lo
   // (long double: at least 64 significant bits on either host)
   for (int j = 0; j <= 128; ++j) {

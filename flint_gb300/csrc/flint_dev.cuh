@@ -64,7 +64,7 @@ struct ImageLayout {
   int o_cstart;                  // int32 [nsp+1]
   int o_lr;                      // int32 [nlist]
   int o_lnu;                     // double [nlist]
-  int o_exptab;                  // double [64]: 2^(j/64)
+  int o_exptab;                  // double [256]: 2^(j/256)
   int nfall;                     // falloff reactions (the last nfall after sorting; <= 16)
   int o_nasa9;                   // NASA-9 thermo [32][nsp] (nranges, T0..T3, 3 x 9 coefficients); -1 = none
   int o_logtab;                  // double [129][3]: c_j ~ 1/(1 + j/128), -ln c_j as hi + lo (flog)
@@ -126,30 +126,31 @@ __device__ inline void stage_image(uint8_t* smem, const uint8_t* __restrict__ g,
 }
 
 // exp(x) by Tang's table-driven method (P. T. P. Tang, ACM TOMS 15(2), 1989):
-// x = (64 m + j) ln2/64 + r with |r| <= ln2/128, exp(x) = 2^m 2^(j/64) exp(r),
-// exp(r) - 1 by its degree-5 Taylor polynomial (truncation < 4e-17 relative).
-// ln2/64 is split into a 32-bit head and a tail (the classic fdlibm split of
-// ln2) so that n*head is exact.  2^(j/64) comes from the 64-entry table staged
-// with the mechanism.  10 FP64 operations; |x| >= 700, NaN and Inf take the
-// CUDA library path (the range test compares the high word as an integer, so
-// it costs no FP64-pipe slot: |x| < 700 exactly when it is below 0x4085E000,
-// the high word of 700.0).  Accuracy is tested against CUDA's exp
+// x = (256 m + j) ln2/256 + r with |r| <= ln2/512, exp(x) = 2^m 2^(j/256)
+// exp(r), exp(r) - 1 by its degree-4 Taylor polynomial (truncation < 4e-17
+// relative).  ln2/256 is split into a 32-bit head and a tail (the classic
+// fdlibm split of ln2) so that n*head is exact.  2^(j/256) comes from the
+// 256-entry table staged with the mechanism.  9 FP64 operations (the CUDA
+// library's exp measured ~18 FP64-pipe slots per value on this GPU); |x| >= 700,
+// NaN and Inf take the library path (the range test compares the high word as
+// an integer, so it costs no FP64-pipe slot: |x| < 700 exactly when it is below
+// 0x4085E000, the high word of 700.0).  Accuracy is tested against CUDA's exp
 // (tests/test_gpu_parity.py).
 __device__ __forceinline__ double fexp(double x, const double* __restrict__ tab) {
   if ((__double2hiint(x) & 0x7fffffff) >= 0x4085E000) return exp(x);
   const double SHIFT = 6755399441055744.0;               // 1.5 * 2^52
-  const double INV_L = 92.33248261689366;                // 64 / ln2
-  const double L_HI = 0.01083042469326756;               // 0x1.62e42fee00000p-7
-  const double L_LO = 2.9815858269852933e-12;            // 0x1.a39ef35793c76p-39
+  const double INV_L = 369.3299304675746;                // 256 / ln2
+  const double L_HI = 0.00270760617331689;               // 0x1.62e42fee00000p-9
+  const double L_LO = 7.453964567463233e-13;             // 0x1.a39ef35793c76p-41
   double kd = fma(x, INV_L, SHIFT);
   const int k = __double2loint(kd);
   kd -= SHIFT;
   double r = fma(kd, -L_HI, x);
   r = fma(kd, -L_LO, r);
-  const double p = r * fma(r, fma(r, fma(r, fma(r, 1.0 / 120.0, 1.0 / 24.0), 1.0 / 6.0), 0.5), 1.0);
-  const double t = tab[k & 63];
+  const double p = r * fma(r, fma(r, fma(r, 1.0 / 24.0, 1.0 / 6.0), 0.5), 1.0);
+  const double t = tab[k & 255];
   const double res = fma(t, p, t);
-  return __hiloint2double(__double2hiint(res) + (k >> 6) * 1048576, __double2loint(res));
+  return __hiloint2double(__double2hiint(res) + (k >> 8) * 1048576, __double2loint(res));
 }
 
 // ln x by a 129-point table (the table-driven method of P. T. P. Tang, ACM
