@@ -75,7 +75,7 @@ namespace flint {
 static int pack(const flint_mech_desc* d, ImageLayout& L, std::vector<uint8_t>& img) {
   const int ns = d->ns, nr = d->nr;
   if (ns < 1 || nr < 0) return fail(FLINT_ERR_ARG, "ns=%d nr=%d", ns, nr);
-  if (ns > 63) return fail(FLINT_ERR_MECH, "ns=%d: the kernels of this build support up to 63 species", ns);
+  if (ns > 63) return fail(FLINT_ERR_MECH, "ns=%d: the kernels support up to 63 species", ns);
   if (!d->mw || !d->nasa7 || (nr > 0 && (!d->rtype || !d->reversible || !d->arrh || !d->rsp || !d->rnu ||
                                          !d->rord || !d->psp || !d->pnu)))
     return fail(FLINT_ERR_ARG, "NULL array in mechanism description");
@@ -105,7 +105,7 @@ static int pack(const flint_mech_desc* d, ImageLayout& L, std::vector<uint8_t>& 
   if (ntb > 255) return fail(FLINT_ERR_MECH, "more than 255 third-body/falloff reactions");
   int nfall = 0;
   for (int r = 0; r < nr; ++r) nfall += d->rtype[r] >= 2;
-  if (nfall > 16) return fail(FLINT_ERR_MECH, "%d falloff reactions: this build supports up to 16", nfall);
+  if (nfall > 16) return fail(FLINT_ERR_MECH, "%d falloff reactions: the kernels support up to 16", nfall);
   L = ImageLayout{};
   L.ns = ns; L.nr = nr; L.nsp = rup(ns, 32); L.nrpad = rup(std::max(nr, 1), 32); L.ntb = std::max(ntb, 1);
   L.r_eos = d->r_eos; L.r_thermo = d->r_thermo; L.inv_r_eos = 1.0 / d->r_eos;
@@ -497,7 +497,7 @@ int flint_chemistry_source_batch(flint_mech_t h, int64_t n, double* roi, const d
   if (rc) return rc;
   if (n == 0) return FLINT_OK;
   if (!roi || !T || !omegadot) return fail(FLINT_ERR_ARG, "NULL array");
-  if (h->L.ns > 16) return fail(FLINT_ERR_MECH, "chemistry_source batch supports up to 16 species in this build");
+  if (h->L.ns > 16) return fail(FLINT_ERR_MECH, "chemistry_source batch supports up to 16 species");
   cudaError_t e = launch_chemistry_source(h->dimg, h->L, n, roi, T, omegadot, (cudaStream_t)stream);
   return e == cudaSuccess ? FLINT_OK : cuda_fail(e, "flint_chemistry_source_batch");
 }
