@@ -462,6 +462,18 @@ def calibrate(sur, d, target_dT=1.0, target_dY=1e-4, margin=0.5):
                        target_dT, target_dY, margin)
 
 
+def training_states(config, hard=False):
+    """The state generator of a training set: the workload's own distribution
+    (c2: the 31-species reactor states, c5: the 54-species scale-up states), or
+    with hard=True the same distribution restricted to the top half-decade of
+    dt, where the largest errors of a network trained on the plain
+    distribution lie."""
+    base = mechgen.c5_states if config == "c5" else mechgen.c3_states
+    if not hard:
+        return lambda n, mech, seed: base(n, mech, seed)
+    return lambda n, mech, seed: base(n, mech, seed, log10dt=(-4.5, -4.0))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("cmd", choices=["train", "calibrate"],
@@ -486,10 +498,8 @@ def main():
     args = ap.parse_args()
     import torch
     chem = Chemistry.from_config(args.config)
-    base = mechgen.c5_states if args.config == "c5" else mechgen.c3_states
-    states = lambda n, mech, seed: base(n, mech, seed)   # noqa: E731
-    hi = -4.0
-    hard_states = lambda n, mech, seed: base(n, mech, seed, log10dt=(hi - 0.5, hi))   # noqa: E731
+    states = training_states(args.config)
+    hard_states = training_states(args.config, hard=True)
     if args.cmd == "calibrate":
         sur = Surrogate.load(chem, args.checkpoint)
         v = generate(chem, args.val, seed=6000 + args.seed, states=states)
